@@ -1,0 +1,548 @@
+// acg_api.cu -- the C ABI (include/acg.h): data graphs, plans, the match.
+//
+// A match runs, on the caller's stream:
+//   cdist (vertex)  -> column stats  -> cdist (edge, dst-CSR order) -> stats
+//   static source pass (dEmin, B, quirk maxima) + destination pass (quirk maxima)
+//   init vertex pass (CV, MU0, first VF/VR)  -> stats
+//   num_iters x { fused edge + vertex pass -> stats }
+//   output: mu[v][p] -= S[p]
+// which is main.cu:107-247 (prep, loop, transpose) of the reference.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "acg.h"
+#include "acg_bp.cuh"
+#include "acg_device.cuh"
+#include "acg_internal.h"
+
+using namespace acg;
+
+struct acg_data {
+  int device = 0;
+  int Dn = 0, De = 0, Kv = 0, Ke = 0;
+  const double* node_feats = nullptr;  // caller's device memory
+  const double* edge_feats = nullptr;
+  Csr dcsr;                 // grouped by destination; other = source vertex
+  Csr scsr;                 // grouped by source; other = destination vertex
+  int* pos_in_dst = nullptr;  // [De] dst-CSR row of each src-CSR position
+  int num_sms = kNumSMs;
+  std::vector<DevBuf> owned;
+};
+
+struct acg_plan {
+  acg_data* data = nullptr;
+  int prec = ACG_PREC_FP64;
+  int Pn = 0, Pe = 0, Pp = 0, iters = 0;
+  const double* pv = nullptr;  // caller's pattern features (device)
+  const double* pe = nullptr;
+  int* pat = nullptr;          // pattern incidence (device)
+  Items ditems, sitems;
+  GroupShape gs{32, 1};
+  int iter_blocks = 1, row_blocks = 1, init_blocks = 1, cv_blocks = 1, ce_blocks = 1;
+  // work buffers (element type per precision)
+  void* dE = nullptr;
+  void* vf = nullptr;
+  void* vr[2] = {nullptr, nullptr};
+  void* dEmin = nullptr;
+  void* B = nullptr;
+  void* CV = nullptr;
+  void* Rbuf = nullptr;
+  void* Fbuf = nullptr;
+  void* part_iter = nullptr;
+  void* part_row = nullptr;
+  double* bpart = nullptr;
+  double* gv = nullptr;      // [3 Pn]
+  double* ge = nullptr;      // [Pe]
+  double* gi[2] = {nullptr, nullptr};  // [4 Pe + Pn]
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  int kernel_timing = 0;
+  std::vector<cudaEvent_t> kev;  // [2 * iters] around each iteration kernel
+  cudaStream_t last_stream = nullptr;
+  int64_t launches = 0;
+  bool ran = false;
+  std::vector<DevBuf> owned;
+};
+
+namespace {
+
+constexpr int kChunk = 256;
+
+__global__ void validate_edges_kernel(const uint64_t* __restrict__ srcs,
+                                      const uint64_t* __restrict__ dsts, long long m,
+                                      unsigned long long n, uint32_t* __restrict__ s32,
+                                      uint32_t* __restrict__ d32, int* __restrict__ bad) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const uint64_t s = srcs[i], d = dsts[i];
+  if (s >= n || d >= n) {
+    atomicOr(bad, 1);
+    s32[i] = 0;
+    d32[i] = 0;
+    return;
+  }
+  s32[i] = (uint32_t)s;
+  d32[i] = (uint32_t)d;
+}
+
+__global__ void invert_kernel(const int* __restrict__ eid, int m, int* __restrict__ inv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) inv[eid[i]] = i;
+}
+
+__global__ void compose_kernel(const int* __restrict__ seid, const int* __restrict__ inv, int m,
+                               int* __restrict__ pos) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < m) pos[j] = inv[seid[j]];
+}
+
+__global__ void mu_from_cv_kernel(double* __restrict__ mu, const void* __restrict__ cv, int fp64,
+                                  const double* __restrict__ gv, long long n, int Pn) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int p = (int)(i % Pn);
+  const double c = fp64 ? ((const double*)cv)[i] : (double)((const float*)cv)[i];
+  // CV holds dV - LSE(dV); MU0 = -dV - LSE(-dV)
+  mu[i] = -(c + gv[Pn + p]) - gv[2 * Pn + p];
+}
+
+int elem_bytes(int prec) { return prec == ACG_PREC_FP64 ? 8 : 4; }
+
+acg_status check_graph(const acg_graph* g, const char* what, bool need_feats) {
+  if (!g) return set_error(ACG_ERR_INVALID_ARGUMENT, "%s graph is null", what);
+  if (g->num_nodes > 0x7fffffffull || g->num_edges > 0x7fffffffull)
+    return set_error(ACG_ERR_UNSUPPORTED, "%s graph: more than 2^31-1 vertices or edges",
+                     what);
+  if (need_feats) {
+    if (g->num_nodes && g->node_feat_dim && !g->node_feats)
+      return set_error(ACG_ERR_INVALID_ARGUMENT, "%s graph: node_feats is null", what);
+    if (g->num_edges && g->edge_feat_dim && !g->edge_feats)
+      return set_error(ACG_ERR_INVALID_ARGUMENT, "%s graph: edge_feats is null", what);
+  }
+  if (g->num_edges && (!g->srcs || !g->dsts))
+    return set_error(ACG_ERR_INVALID_ARGUMENT, "%s graph: srcs/dsts is null", what);
+  return ACG_OK;
+}
+
+template <typename T>
+acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
+  acg_data* D = P->data;
+  const int Dn = D->Dn, Pn = P->Pn, Pe = P->Pe, Pp = P->Pp;
+  const long long De = D->De;
+  const long long lim = (long long)Pn * (long long)Dn;
+  P->launches = 0;
+  cudaEventRecord(P->ev[0], s);
+
+  // ---- cdist, vertex side (ac.hxx:33-56 via main.cu:109) + column stats
+  {
+    CdistVArgs<T> a{D->node_feats, P->pv, (T*)P->CV, P->bpart, Dn, Pn, D->Kv};
+    ACG_TRY(launch_cdist_v<T>(a, P->cv_blocks, s));
+    ACG_TRY(launch_finalize(P->bpart, P->cv_blocks, StatSpec{Pn, 2 * Pn}, P->gv, s));
+    P->launches += 2;
+  }
+  // ---- cdist, edge side (main.cu:110), rows in dst-CSR order
+  {
+    CdistEArgs<T> a{D->edge_feats, D->dcsr.eid, P->pe, (T*)P->dE, P->bpart, De, Pe, Pp, D->Ke, lim};
+    // With no data edges the kernel writes empty partials (-inf, 0).
+    ACG_TRY(launch_cdist_e<T>(a, P->ce_blocks, s));
+    ACG_TRY(launch_finalize(P->bpart, P->ce_blocks, StatSpec{0, Pe}, P->ge, s));
+    P->launches += 2;
+  }
+  cudaEventRecord(P->ev[1], s);
+  // ---- static per-vertex reductions
+  {
+    RowPassArgs<T> a{};
+    a.items = P->sitems.items;
+    a.nitems = P->sitems.nitems;
+    a.row_of = D->pos_in_dst;
+    a.eid_of_row = D->dcsr.eid;
+    a.dE = (const T*)P->dE;
+    a.partial = (T*)P->part_row;
+    a.hbase = P->sitems.hbase;
+    a.hcount = P->sitems.hcount;
+    a.hcounter = P->sitems.hcounter;
+    a.chunk = P->sitems.chunk;
+    a.off = D->scsr.off;
+    a.out_min = (T*)P->dEmin;
+    a.out_lse = (T*)P->B;
+    a.out_buf = (T*)P->Rbuf;
+    a.De = De;
+    a.lim = lim;
+    a.Dn = Dn;
+    a.Pe = Pe;
+    a.Pp = Pp;
+    a.src_mode = 1;
+    ACG_TRY(launch_row_pass<T>(a, P->gs, P->row_blocks, s));
+    a.items = P->ditems.items;
+    a.nitems = P->ditems.nitems;
+    a.row_of = nullptr;
+    a.hbase = P->ditems.hbase;
+    a.hcount = P->ditems.hcount;
+    a.hcounter = P->ditems.hcounter;
+    a.chunk = P->ditems.chunk;
+    a.off = D->dcsr.off;
+    a.out_min = nullptr;
+    a.out_lse = nullptr;
+    a.out_buf = (T*)P->Fbuf;
+    a.src_mode = 0;
+    ACG_TRY(launch_row_pass<T>(a, P->gs, P->row_blocks, s));
+    P->launches += 2;
+  }
+  // ---- init vertex pass
+  {
+    InitArgs<T> a{D->dcsr.off, D->scsr.off, (T*)P->CV, (const T*)P->Rbuf, (const T*)P->Fbuf,
+                  (const T*)P->B, (T*)P->vf, (T*)P->vr[0], P->gv, P->ge, P->bpart, P->pat,
+                  De, lim, Dn, Pn, Pe, Pp};
+    ACG_TRY(launch_init_vertex<T>(a, P->gs, P->init_blocks, s));
+    ACG_CUDA_TRY(cudaMemsetAsync(P->gi[0] + 4 * Pe, 0, sizeof(double) * Pn, s));
+    ACG_TRY(launch_finalize(P->bpart, P->init_blocks, StatSpec{2 * Pe, 2 * Pe}, P->gi[0], s));
+    P->launches += 2;
+  }
+  cudaEventRecord(P->ev[2], s);
+  // ---- BP iterations (main.cu:160-245)
+  for (int t = 1; t <= P->iters; ++t) {
+    IterArgs<T> a{};
+    a.items = P->ditems.items;
+    a.nitems = P->ditems.nitems;
+    a.src_of = D->dcsr.other;
+    a.d_off = D->dcsr.off;
+    a.s_off = D->scsr.off;
+    a.dE = (const T*)P->dE;
+    a.vr_in = (const T*)P->vr[(t - 1) & 1];
+    a.vr_out = (T*)P->vr[t & 1];
+    a.vf = (T*)P->vf;
+    a.dEmin = (const T*)P->dEmin;
+    a.B = (const T*)P->B;
+    a.CV = (const T*)P->CV;
+    a.partial = (T*)P->part_iter;
+    a.hbase = P->ditems.hbase;
+    a.hcount = P->ditems.hcount;
+    a.hcounter = P->ditems.hcounter;
+    a.chunk = P->ditems.chunk;
+    a.glob_in = P->gi[(t - 1) & 1];
+    a.bpart = P->bpart;
+    a.mu_raw = mu_out;
+    a.pat = P->pat;
+    a.Dn = Dn;
+    a.Pn = Pn;
+    a.Pe = Pe;
+    a.Pp = Pp;
+    a.last = t == P->iters;
+    if (P->kernel_timing) cudaEventRecord(P->kev[2 * (t - 1)], s);
+    ACG_TRY(launch_iter<T>(a, P->gs, P->iter_blocks, s));
+    if (P->kernel_timing) cudaEventRecord(P->kev[2 * (t - 1) + 1], s);
+    ACG_TRY(launch_finalize(P->bpart, P->iter_blocks, StatSpec{2 * Pe, 2 * Pe + Pn}, P->gi[t & 1], s));
+    P->launches += 2;
+  }
+  cudaEventRecord(P->ev[3], s);
+  // ---- output [Dn][Pn] (main.cu:247 transpose is implicit in the layout)
+  if (P->iters > 0) {
+    ACG_TRY(launch_mu_output(mu_out, P->gi[P->iters & 1] + 4 * Pe, Dn, Pn, s));
+  } else {
+    const long long n = (long long)Dn * Pn;
+    if (n > 0) {
+      mu_from_cv_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(mu_out, P->CV, P->prec == ACG_PREC_FP64, P->gv, n, Pn);
+      ACG_LAUNCH_CHECK();
+    }
+  }
+  P->launches += 1;
+  cudaEventRecord(P->ev[4], s);
+  return ACG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void acg_options_default(acg_options* opt) {
+  if (!opt) return;
+  std::memset(opt, 0, sizeof *opt);
+  opt->precision = ACG_PREC_FP64;
+  opt->num_iters = -1;
+}
+
+acg_status acg_data_create(const acg_graph* g, void* stream, acg_data** out) {
+  clear_error();
+  if (!out) return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_data_create: out is null");
+  *out = nullptr;
+  ACG_TRY(check_graph(g, "data", true));
+  cudaStream_t s = (cudaStream_t)stream;
+  std::unique_ptr<acg_data> D(new acg_data());
+  ACG_CUDA_TRY(cudaGetDevice(&D->device));
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, D->device) == cudaSuccess && sms > 0)
+    D->num_sms = sms;
+  D->Dn = (int)g->num_nodes;
+  D->De = (int)g->num_edges;
+  D->Kv = (int)g->node_feat_dim;
+  D->Ke = (int)g->edge_feat_dim;
+  D->node_feats = g->node_feats;
+  D->edge_feats = g->edge_feats;
+  const int m = D->De, n = D->Dn;
+  uint32_t *s32 = nullptr, *d32 = nullptr;
+  int* bad = nullptr;
+  auto fail = [&](acg_status st) {
+    if (s32) cudaFree(s32);
+    if (d32) cudaFree(d32);
+    if (bad) cudaFree(bad);
+    dev_free_all(&D->owned);
+    return st;
+  };
+  if (cudaMalloc(&s32, sizeof(uint32_t) * (size_t)(m ? m : 1)) != cudaSuccess ||
+      cudaMalloc(&d32, sizeof(uint32_t) * (size_t)(m ? m : 1)) != cudaSuccess ||
+      cudaMalloc(&bad, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(set_error(ACG_ERR_OUT_OF_MEMORY, "acg_data_create: temporary allocation failed"));
+  }
+  cudaMemsetAsync(bad, 0, sizeof(int), s);
+  if (m > 0) {
+    validate_edges_kernel<<<ceil_div(m, 256), 256, 0, s>>>(g->srcs, g->dsts, m, (unsigned long long)n, s32, d32, bad);
+    if (cudaGetLastError() != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "validate launch failed"));
+  }
+  int hbad = 0;
+  if (cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return fail(set_error(ACG_ERR_CUDA, "acg_data_create: %s", cudaGetErrorString(cudaGetLastError())));
+  if (hbad)
+    return fail(set_error(ACG_ERR_INDEX_OUT_OF_RANGE,
+                          "data graph: an edge endpoint is >= num_nodes (%d)", n));
+  acg_status st = build_csr(d32, s32, n, m, &D->dcsr, &D->owned, s);
+  if (st == ACG_OK) st = build_csr(s32, d32, n, m, &D->scsr, &D->owned, s);
+  if (st == ACG_OK) st = dev_alloc(&D->owned, sizeof(int) * (size_t)m, (void**)&D->pos_in_dst, s);
+  if (st == ACG_OK && m > 0) {
+    int* inv = reinterpret_cast<int*>(s32);  // reuse: no longer needed
+    invert_kernel<<<ceil_div(m, 256), 256, 0, s>>>(D->dcsr.eid, m, inv);
+    compose_kernel<<<ceil_div(m, 256), 256, 0, s>>>(D->scsr.eid, inv, m, D->pos_in_dst);
+    if (cudaGetLastError() != cudaSuccess) st = set_error(ACG_ERR_CUDA, "csr compose launch failed");
+  }
+  if (st == ACG_OK && cudaStreamSynchronize(s) != cudaSuccess)
+    st = set_error(ACG_ERR_CUDA, "acg_data_create: %s", cudaGetErrorString(cudaGetLastError()));
+  if (st != ACG_OK) return fail(st);
+  cudaFree(s32);
+  cudaFree(d32);
+  cudaFree(bad);
+  *out = D.release();
+  return ACG_OK;
+}
+
+acg_status acg_data_destroy(acg_data* D) {
+  if (!D) return ACG_OK;
+  dev_free_all(&D->owned);
+  delete D;
+  return ACG_OK;
+}
+
+acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* opt,
+                           void* stream, acg_plan** out) {
+  clear_error();
+  if (!out) return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_plan_create: out is null");
+  *out = nullptr;
+  if (!D) return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_plan_create: data is null");
+  ACG_TRY(check_graph(pg, "pattern", true));
+  acg_options o;
+  acg_options_default(&o);
+  if (opt) o = *opt;
+  if (o.precision != ACG_PREC_FP64 && o.precision != ACG_PREC_MIXED)
+    return set_error(ACG_ERR_INVALID_ARGUMENT, "unknown precision %d", o.precision);
+  if (pg->num_nodes == 0) return set_error(ACG_ERR_INVALID_ARGUMENT, "pattern has no vertices");
+  if (pg->node_feat_dim != (uint64_t)D->Kv || pg->edge_feat_dim != (uint64_t)D->Ke)
+    return set_error(ACG_ERR_INVALID_ARGUMENT,
+                     "feature dims differ: data %d/%d, pattern %llu/%llu", D->Kv, D->Ke,
+                     (unsigned long long)pg->node_feat_dim, (unsigned long long)pg->edge_feat_dim);
+  if (pg->num_nodes > 128 || pg->num_edges > 256)
+    return set_error(ACG_ERR_UNSUPPORTED,
+                     "pattern with %llu vertices / %llu edges: at most 128 / 256 are supported",
+                     (unsigned long long)pg->num_nodes, (unsigned long long)pg->num_edges);
+  if (D->Kv > 1024 || D->Ke > 1024)
+    return set_error(ACG_ERR_UNSUPPORTED, "feature dimension above 1024");
+  cudaStream_t s = (cudaStream_t)stream;
+  std::unique_ptr<acg_plan> P(new acg_plan());
+  P->data = D;
+  P->prec = o.precision;
+  P->Pn = (int)pg->num_nodes;
+  P->Pe = (int)pg->num_edges;
+  P->iters = o.num_iters < 0 ? P->Pn : o.num_iters;
+  P->pv = pg->node_feats;
+  P->pe = pg->edge_feats;
+  const int eb = elem_bytes(P->prec);
+  const int W = 16 / eb;
+  P->Pp = std::max(W, (P->Pe + W - 1) / W * W);
+  const int Pn = P->Pn, Pe = P->Pe, Pp = P->Pp, Dn = D->Dn, De = D->De;
+
+  // pattern incidence (host build from the device endpoint arrays)
+  std::vector<uint64_t> ps(Pe), pd(Pe);
+  if (Pe > 0) {
+    ACG_CUDA_TRY(cudaMemcpyAsync(ps.data(), pg->srcs, 8 * (size_t)Pe, cudaMemcpyDeviceToHost, s));
+    ACG_CUDA_TRY(cudaMemcpyAsync(pd.data(), pg->dsts, 8 * (size_t)Pe, cudaMemcpyDeviceToHost, s));
+    ACG_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  std::vector<int> pat(pattern_ints(Pn, Pe));
+  {
+    int* psrc = pat.data();
+    int* pdst = psrc + Pe;
+    int* inoff = pdst + Pe;
+    int* inq = inoff + Pn + 1;
+    int* outoff = inq + Pe;
+    int* outq = outoff + Pn + 1;
+    for (int q = 0; q < Pe; ++q) {
+      if (ps[q] >= (uint64_t)Pn || pd[q] >= (uint64_t)Pn)
+        return set_error(ACG_ERR_INDEX_OUT_OF_RANGE, "pattern edge %d endpoint >= %d", q, Pn);
+      psrc[q] = (int)ps[q];
+      pdst[q] = (int)pd[q];
+      inoff[pd[q] + 1]++;
+      outoff[ps[q] + 1]++;
+    }
+    for (int p = 0; p < Pn; ++p) {
+      inoff[p + 1] += inoff[p];
+      outoff[p + 1] += outoff[p];
+    }
+    std::vector<int> ci(inoff, inoff + Pn), co(outoff, outoff + Pn);
+    for (int q = 0; q < Pe; ++q) {
+      inq[ci[pdst[q]]++] = q;
+      outq[co[psrc[q]]++] = q;
+    }
+  }
+  auto fail = [&](acg_status st) {
+    dev_free_all(&P->owned);
+    return st;
+  };
+  acg_status st = ACG_OK;
+  auto alloc = [&](size_t bytes, void** p) {
+    if (st == ACG_OK) st = dev_alloc(&P->owned, bytes, p, s);
+  };
+  alloc(sizeof(int) * pat.size(), (void**)&P->pat);
+  if (st != ACG_OK) return fail(st);
+  ACG_CUDA_TRY(cudaMemcpyAsync(P->pat, pat.data(), sizeof(int) * pat.size(), cudaMemcpyHostToDevice, s));
+
+  st = build_items(D->dcsr, kChunk, &P->ditems, &P->owned, s);
+  if (st == ACG_OK) st = build_items(D->scsr, kChunk, &P->sitems, &P->owned, s);
+  if (st != ACG_OK) return fail(st);
+
+  P->gs = choose_shape(eb, Pp, Pn);
+  const int GPB = 256 / P->gs.G;
+  const int occ = eb == 8 ? iter_max_blocks<double>(P->gs, Pn, Pe, Pp)
+                          : iter_max_blocks<float>(P->gs, Pn, Pe, Pp);
+  const int nsm = D->num_sms;
+  P->iter_blocks = std::max(1, std::min(ceil_div(std::max(1, P->ditems.nitems), GPB), nsm * occ));
+  P->row_blocks = std::max(1, std::min(ceil_div(std::max(1, std::max(P->ditems.nitems, P->sitems.nitems)), GPB), nsm * 4));
+  P->init_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), GPB), nsm * 4));
+  P->cv_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), 256 / Pn), nsm * 8));
+  P->ce_blocks = std::max(1, std::min(ceil_div(std::max(1, De), 256 / Pp), nsm * 8));
+
+  const size_t vrow = (size_t)Dn * Pp * eb;
+  alloc((size_t)De * Pp * eb, &P->dE);
+  alloc(vrow, &P->vf);
+  alloc(vrow, &P->vr[0]);
+  alloc(vrow, &P->vr[1]);
+  alloc(vrow, &P->dEmin);
+  alloc(vrow, &P->B);
+  alloc(vrow, &P->Rbuf);
+  alloc(vrow, &P->Fbuf);
+  alloc((size_t)Dn * Pn * eb, &P->CV);
+  alloc((size_t)std::max(1, P->ditems.npartial) * Pp * eb, &P->part_iter);
+  alloc((size_t)std::max(1, std::max(P->ditems.npartial, P->sitems.npartial)) * 4 * Pp * eb, &P->part_row);
+  const size_t bp = std::max({(size_t)(6 * Pe + 2 * Pn) * P->iter_blocks,
+                              (size_t)5 * Pn * P->cv_blocks, (size_t)2 * Pe * P->ce_blocks,
+                              (size_t)6 * Pe * P->init_blocks});
+  alloc(sizeof(double) * bp, (void**)&P->bpart);
+  alloc(sizeof(double) * 3 * Pn, (void**)&P->gv);
+  alloc(sizeof(double) * std::max(1, Pe), (void**)&P->ge);
+  alloc(sizeof(double) * (4 * Pe + Pn), (void**)&P->gi[0]);
+  alloc(sizeof(double) * (4 * Pe + Pn), (void**)&P->gi[1]);
+  if (st != ACG_OK) return fail(st);
+  for (auto& e : P->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "cudaEventCreate failed"));
+  P->kernel_timing = o.kernel_timing;
+  if (P->kernel_timing) {
+    P->kev.assign(2 * (size_t)P->iters, nullptr);
+    for (auto& e : P->kev)
+      if (cudaEventCreate(&e) != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "cudaEventCreate failed"));
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess)
+    return fail(set_error(ACG_ERR_CUDA, "acg_plan_create: %s", cudaGetErrorString(cudaGetLastError())));
+  *out = P.release();
+  return ACG_OK;
+}
+
+acg_status acg_plan_destroy(acg_plan* P) {
+  if (!P) return ACG_OK;
+  for (auto& e : P->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : P->kev)
+    if (e) cudaEventDestroy(e);
+  dev_free_all(&P->owned);
+  delete P;
+  return ACG_OK;
+}
+
+acg_status acg_match(acg_plan* P, double* mu_out, void* stream) {
+  clear_error();
+  if (!P) return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_match: plan is null");
+  if (!mu_out && (long long)P->data->Dn * P->Pn > 0)
+    return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_match: mu_out is null");
+  cudaStream_t s = (cudaStream_t)stream;
+  P->last_stream = s;
+  if (P->data->Dn == 0) return ACG_OK;
+  acg_status st = P->prec == ACG_PREC_FP64 ? run_match<double>(P, mu_out, s)
+                                           : run_match<float>(P, mu_out, s);
+  P->ran = st == ACG_OK;
+  return st;
+}
+
+acg_status acg_plan_stats(acg_plan* P, acg_stats* out) {
+  clear_error();
+  if (!P || !out) return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_plan_stats: null argument");
+  std::memset(out, 0, sizeof *out);
+  if (!P->ran) return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_plan_stats: no match has run");
+  ACG_CUDA_TRY(cudaEventSynchronize(P->ev[4]));
+  float t01 = 0, t12 = 0, t23 = 0, t04 = 0;
+  cudaEventElapsedTime(&t01, P->ev[0], P->ev[1]);
+  cudaEventElapsedTime(&t12, P->ev[1], P->ev[2]);
+  cudaEventElapsedTime(&t23, P->ev[2], P->ev[3]);
+  cudaEventElapsedTime(&t04, P->ev[0], P->ev[4]);
+  out->ms_cdist = t01;
+  out->ms_init = t12;
+  out->ms_iters = t23;
+  out->ms_total = t04;
+  const double eb = elem_bytes(P->prec);
+  const double Dn = P->data->Dn, De = P->data->De, Pe = P->Pe, Pn = P->Pn;
+  // Algorithmic bytes of one fused iteration launch (unpadded Pe): per in-edge
+  // its dE row and source index; per vertex the gathered VR row once, the
+  // VF/dEmin/B and CV reads, the VF/VR writes, CSR offsets and the work item.
+  const double edge = De * (Pe * eb + 4.0);
+  const double vert = Dn * (Pe * eb + 3 * Pe * eb + Pn * eb + 2 * Pe * eb + 8.0) +
+                      (double)P->ditems.nitems * 16.0;
+  out->bytes_per_edge_pass = edge + vert;
+  out->bytes_iters = out->bytes_per_edge_pass * P->iters;
+  out->launches = P->launches;
+  out->num_iters = P->iters;
+  if (P->kernel_timing) {
+    double sum = 0;
+    for (int t = 0; t < P->iters; ++t) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, P->kev[2 * t], P->kev[2 * t + 1]);
+      sum += ms;
+    }
+    out->ms_iter_kernels = sum;
+  }
+  return ACG_OK;
+}
+
+acg_status acg_match_graphs(const acg_graph* data, const acg_graph* pattern,
+                            const acg_options* opt, double* mu_out, void* stream) {
+  acg_data* D = nullptr;
+  ACG_TRY(acg_data_create(data, stream, &D));
+  acg_plan* P = nullptr;
+  acg_status st = acg_plan_create(D, pattern, opt, stream, &P);
+  if (st == ACG_OK) st = acg_match(P, mu_out, stream);
+  if (st == ACG_OK && cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess)
+    st = set_error(ACG_ERR_CUDA, "acg_match_graphs: %s", cudaGetErrorString(cudaGetLastError()));
+  acg_plan_destroy(P);
+  acg_data_destroy(D);
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,986 @@
+// acg_bp.cu -- the belief-propagation kernels of the matcher (SIMT part).
+//
+// Reference semantics (src/main.cu:107-247, src/ac.hxx:17-186), with pattern
+// edge q = (src_q -> dst_q), data edge e = (s_e -> t_e), L(x) the row
+// log-softmax over the data axis and CE = L(dE):
+//   VF[q,v] = MU[dst_q,v] - FMax[q,v]          VR[q,v] = MU[src_q,v] - RMax[q,v]
+//   RE[q,e] = VF[q,s_e] - CE[q,e]              FE[q,e] = VR[q,s_e] - CE[q,e]
+//   RMax[q,v] = max(max_v' VF[q,v'], max_{e: s_e = v} L(RE)[q,e])
+//   FMax[q,v] = max(max_v' VR[q,v'], max_{e: t_e = v} L(FE)[q,e])
+//   MU[p,v] = L(-CV[p,v] + sum_{q: dst_q=p} FMax[q,v] + sum_{q: src_q=p} RMax[q,v])
+//
+// Both RE and FE gather at the edge's SOURCE (main.cu:184-185), so with
+//   B[v,q]     = log sum_{e: s_e = v} exp(-dE[q,e])   (static)
+//   dEmin[v,q] = min_{e: s_e = v} dE[q,e]             (static)
+// the edge-sized work of an iteration collapses exactly to
+//   log sum_e exp(RE[q,e]) = LSE_CE[q] + log sum_v exp(VF[q,v] + B[v,q])
+//   max_{e: s_e = v} L(RE)  = VF[q,v] - dEmin[v,q] - log sum_v' exp(VF[q,v'] + B[v',q])
+//   max_{e: t_e = v} L(FE)  = max_{e: t_e = v}(VR[q,s_e] - dE[q,e])
+//                              - log sum_v' exp(VR[q,v'] + B[v',q])
+// (LSE_CE cancels).  The only per-iteration edge work left is the segmented
+// (max, -) reduction over each vertex's in-edges in the destination-sorted
+// CSR, gathering the VR rows of the sources; no exp/log per edge remains.
+//
+// Global dependencies: each iteration needs column maxima / log-sum-exps of the
+// previous VF, VR and MU.  They are carried unshifted: VF' = MU_raw[dst] -
+// FMax, VR' = MU_raw[src] - RMax with MU_raw the un-normalised MU, and the
+// previous column log-sum-exp S[p] of MU_raw is applied as a per-q constant
+// (c_F[q] = S[dst_q], c_R[q] = S[src_q]):
+//   RMax = max(mVF'[q] - c_F[q], VF'[v,q] - dEmin[v,q] - lR[q])
+//   FMax = max(mVR'[q] - c_R[q], max_e(VR'[s_e,q] - dE[e,q]) - lF[q])
+// with lR = LSE_v(VF' + B), lF = LSE_v(VR' + B).  So one fused kernel per
+// iteration computes FMax, RMax, MU_raw and the next VF', VR' for each vertex,
+// plus block partials of the next column statistics; stat_finalize combines
+// those partials in a fixed order (results are deterministic).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "acg_bp.cuh"
+#include "acg_device.cuh"
+
+namespace acg {
+
+namespace {
+
+template <typename T>
+struct Vec;
+template <>
+struct Vec<double> {
+  using type = double2;
+  static constexpr int W = 2;
+};
+template <>
+struct Vec<float> {
+  using type = float4;
+  static constexpr int W = 4;
+};
+
+template <typename T>
+__device__ __forceinline__ T& lane_of(typename Vec<T>::type& v, int w) {
+  return reinterpret_cast<T*>(&v)[w];
+}
+template <typename T>
+__device__ __forceinline__ T lane_of(const typename Vec<T>::type& v, int w) {
+  return reinterpret_cast<const T*>(&v)[w];
+}
+
+template <typename T>
+__device__ __forceinline__ typename Vec<T>::type vzero() {
+  typename Vec<T>::type z;
+#pragma unroll
+  for (int w = 0; w < Vec<T>::W; ++w) lane_of<T>(z, w) = T(0);
+  return z;
+}
+
+// Shared-memory carving; the host computes sizes with the same rounding.
+struct Carve {
+  unsigned char* p;
+  template <typename U>
+  __device__ __forceinline__ U* take(size_t n) {
+    U* r = reinterpret_cast<U*>(p);
+    p += (n * sizeof(U) + 15) & ~size_t(15);
+    return r;
+  }
+};
+inline size_t carve_bytes(size_t n, size_t elem) { return (n * elem + 15) & ~size_t(15); }
+
+template <int G>
+struct Grp {
+  int lane, lig, gw;
+  unsigned mask;
+  __device__ __forceinline__ Grp() {
+    lane = threadIdx.x & 31;
+    lig = lane & (G - 1);
+    gw = lane / G;
+    mask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (gw * G));
+  }
+};
+
+__device__ __forceinline__ double shfl_xor_d(double x, int o) {
+  return __shfl_xor_sync(0xffffffffu, x, o);
+}
+
+__device__ __forceinline__ void lse_merge(double& m, double& s, double m2, double s2) {
+  LseD a{m, s};
+  a.merge(m2, s2);
+  m = a.m;
+  s = a.s;
+}
+
+// Combine, across the groups of a warp, values held by lanes with the same
+// in-group index.  G == 32 is a no-op.
+template <int G>
+__device__ __forceinline__ double warp_group_max(double x) {
+#pragma unroll
+  for (int o = G; o < 32; o <<= 1) x = fmax(x, shfl_xor_d(x, o));
+  return x;
+}
+template <int G>
+__device__ __forceinline__ void warp_group_lse(double& m, double& s) {
+#pragma unroll
+  for (int o = G; o < 32; o <<= 1) {
+    const double m2 = shfl_xor_d(m, o), s2 = shfl_xor_d(s, o);
+    lse_merge(m, s, m2, s2);
+  }
+}
+
+// After every warp wrote its per-slot values to red[warp][slot], combine the
+// warps in order and write the block's partials [slot][block].
+__device__ void block_partials_out(const double* red, int nwarps, StatSpec spec,
+                                   double* bpart) {
+  const int slots = spec.slots();
+  for (int j = threadIdx.x; j < spec.nmax + spec.nlse; j += blockDim.x) {
+    if (j < spec.nmax) {
+      double m = -CUDART_INF;
+      for (int w = 0; w < nwarps; ++w) m = fmax(m, red[w * slots + j]);
+      bpart[(size_t)j * gridDim.x + blockIdx.x] = m;
+    } else {
+      const int sm = spec.nmax + 2 * (j - spec.nmax);
+      double m = -CUDART_INF, s = 0.0;
+      for (int w = 0; w < nwarps; ++w) lse_merge(m, s, red[w * slots + sm], red[w * slots + sm + 1]);
+      bpart[(size_t)sm * gridDim.x + blockIdx.x] = m;
+      bpart[(size_t)(sm + 1) * gridDim.x + blockIdx.x] = s;
+    }
+  }
+}
+
+// ------------------------------------------------------------- finalize
+__global__ void __launch_bounds__(256)
+stat_finalize_kernel(const double* __restrict__ bpart, int nblocks, StatSpec spec,
+                     double* __restrict__ out) {
+  __shared__ double sm[8], ss[8];
+  const int o = blockIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (o < spec.nmax) {
+    double m = -CUDART_INF;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) m = fmax(m, bpart[(size_t)o * nblocks + b]);
+#pragma unroll
+    for (int k = 16; k >= 1; k >>= 1) m = fmax(m, shfl_xor_d(m, k));
+    if (lane == 0) sm[w] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double r = sm[0];
+      for (int k = 1; k < 8; ++k) r = fmax(r, sm[k]);
+      out[o] = r;
+    }
+  } else {
+    const int sl = spec.nmax + 2 * (o - spec.nmax);
+    double m = -CUDART_INF, s = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+      lse_merge(m, s, bpart[(size_t)sl * nblocks + b], bpart[(size_t)(sl + 1) * nblocks + b]);
+#pragma unroll
+    for (int k = 16; k >= 1; k >>= 1) {
+      const double m2 = shfl_xor_d(m, k), s2 = shfl_xor_d(s, k);
+      lse_merge(m, s, m2, s2);
+    }
+    if (lane == 0) {
+      sm[w] = m;
+      ss[w] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      LseD r;
+      r.init();
+      for (int k = 0; k < 8; ++k) r.merge(sm[k], ss[k]);
+      out[o] = r.value();
+    }
+  }
+}
+
+// --------------------------------------------------------- the iteration
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kNPV = 4;  // pattern vertices per lane: Pn <= 4 * G
+
+template <typename T, int G, int NQV>
+__global__ void __launch_bounds__(kThreads)
+iter_kernel(const IterArgs<T> a) {
+  using VT = typename Vec<T>::type;
+  constexpr int W = Vec<T>::W;
+  constexpr int NQ = NQV * W;
+  constexpr int GPB = kThreads / G;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int Pe = a.Pe, Pn = a.Pn, Pp = a.Pp;
+  Carve cv{smem};
+  int* s_pat = cv.take<int>(pattern_ints(Pn, Pe));
+  T* s_fillF = cv.take<T>(Pe);
+  T* s_fillR = cv.take<T>(Pe);
+  T* s_lF = cv.take<T>(Pe);
+  T* s_lFlo = cv.take<T>(Pe);
+  T* s_lR = cv.take<T>(Pe);
+  T* s_lRlo = cv.take<T>(Pe);
+  T* s_grp = cv.take<T>((size_t)GPB * (2 * Pp + Pn));
+  double* s_red = cv.take<double>((size_t)kWarps * (6 * Pe + 2 * Pn));
+  const int* s_psrc = s_pat;
+  const int* s_pdst = s_pat + Pe;
+  const int* s_inoff = s_pat + 2 * Pe;
+  const int* s_inq = s_inoff + Pn + 1;
+  const int* s_outoff = s_inq + Pe;
+  const int* s_outq = s_outoff + Pn + 1;
+
+  for (int t = threadIdx.x; t < pattern_ints(Pn, Pe); t += kThreads) s_pat[t] = a.pat[t];
+  __syncthreads();
+  {
+    const double* g = a.glob_in;  // mVF | mVR | lR | lF | S
+    for (int q = threadIdx.x; q < Pe; q += kThreads) {
+      const double cR = g[4 * Pe + s_psrc[q]], cF = g[4 * Pe + s_pdst[q]];
+      s_fillF[q] = (T)(g[Pe + q] - cR);
+      s_fillR[q] = (T)(g[q] - cF);
+      const double lr = g[2 * Pe + q], lf = g[3 * Pe + q];
+      s_lR[q] = (T)lr;
+      s_lRlo[q] = (T)(lr - (double)(T)lr);
+      s_lF[q] = (T)lf;
+      s_lFlo[q] = (T)(lf - (double)(T)lf);
+    }
+  }
+  __syncthreads();
+
+  const Grp<G> gr;
+  const int gib = threadIdx.x / G;
+  T* my_F = s_grp + (size_t)gib * (2 * Pp + Pn);
+  T* my_R = my_F + Pp;
+  T* my_MU = my_R + Pp;
+
+  T mxF[NQ], mxR[NQ];
+  OnlineLse<T> lr[NQ], lf[NQ], lmu[kNPV];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    mxF[k] = neg_inf<T>();
+    mxR[k] = neg_inf<T>();
+    lr[k].init();
+    lf[k].init();
+  }
+#pragma unroll
+  for (int j = 0; j < kNPV; ++j) lmu[j].init();
+
+  const int gstride = gridDim.x * GPB;
+  for (int it = blockIdx.x * GPB + gib; it < a.nitems; it += gstride) {
+    const int4 item = a.items[it];
+    const int v = item.x, i0 = item.y, i1 = item.z, h = item.w;
+
+    // ---- segmented max over in-edges: M'[q] = max_e VR'[s_e][q] - dE[e][q]
+    T acc[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) acc[k] = neg_inf<T>();
+    for (int base = i0; base < i1; base += G) {
+      const int nb = min(G, i1 - base);
+      const int my_s = gr.lig < nb ? __ldg(a.src_of + base + gr.lig) : 0;
+      int j = 0;
+      for (; j + 4 <= nb; j += 4) {
+        VT vr[4][NQV], de[4][NQV];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int s = __shfl_sync(gr.mask, my_s, j + u, G);
+          const VT* rv = reinterpret_cast<const VT*>(a.vr_in + (size_t)s * Pp);
+          const VT* re = reinterpret_cast<const VT*>(a.dE + (size_t)(base + j + u) * Pp);
+#pragma unroll
+          for (int k = 0; k < NQV; ++k) {
+            const int qv = gr.lig + G * k;
+            if (qv * W < Pp) {
+              vr[u][k] = __ldg(rv + qv);
+              de[u][k] = __ldcs(re + qv);
+            } else {
+              vr[u][k] = vzero<T>();
+              de[u][k] = vzero<T>();
+            }
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int k = 0; k < NQV; ++k)
+#pragma unroll
+            for (int w = 0; w < W; ++w)
+              acc[k * W + w] = fmax(acc[k * W + w], lane_of<T>(vr[u][k], w) - lane_of<T>(de[u][k], w));
+      }
+      for (; j < nb; ++j) {
+        const int s = __shfl_sync(gr.mask, my_s, j, G);
+        const VT* rv = reinterpret_cast<const VT*>(a.vr_in + (size_t)s * Pp);
+        const VT* re = reinterpret_cast<const VT*>(a.dE + (size_t)(base + j) * Pp);
+#pragma unroll
+        for (int k = 0; k < NQV; ++k) {
+          const int qv = gr.lig + G * k;
+          if (qv * W < Pp) {
+            VT x = __ldg(rv + qv), y = __ldcs(re + qv);
+#pragma unroll
+            for (int w = 0; w < W; ++w)
+              acc[k * W + w] = fmax(acc[k * W + w], lane_of<T>(x, w) - lane_of<T>(y, w));
+          }
+        }
+      }
+    }
+
+    // ---- heavy vertex: publish this chunk; the last chunk to arrive combines
+    if (h >= 0) {
+      const int c = (i0 - __ldg(a.d_off + v)) / a.chunk;
+      T* prow = a.partial + (size_t)(__ldg(a.hbase + h) + c) * Pp;
+#pragma unroll
+      for (int k = 0; k < NQV; ++k) {
+        const int qv = gr.lig + G * k;
+        if (qv * W < Pp) {
+          VT x;
+#pragma unroll
+          for (int w = 0; w < W; ++w) lane_of<T>(x, w) = acc[k * W + w];
+          reinterpret_cast<VT*>(prow)[qv] = x;
+        }
+      }
+      __threadfence();
+      __syncwarp(gr.mask);
+      unsigned old = 0;
+      if (gr.lig == 0) old = atomicAdd(a.hcounter + h, 1u);
+      old = __shfl_sync(gr.mask, old, 0, G);
+      const int cnt = __ldg(a.hcount + h);
+      if ((int)old != cnt - 1) continue;  // another chunk finishes this vertex
+      __threadfence();
+      const T* p0 = a.partial + (size_t)__ldg(a.hbase + h) * Pp;
+      for (int r = 0; r < cnt; ++r) {
+        const VT* pr = reinterpret_cast<const VT*>(p0 + (size_t)r * Pp);
+#pragma unroll
+        for (int k = 0; k < NQV; ++k) {
+          const int qv = gr.lig + G * k;
+          if (qv * W < Pp) {
+            VT x = __ldcg(pr + qv);
+#pragma unroll
+            for (int w = 0; w < W; ++w) acc[k * W + w] = fmax(acc[k * W + w], lane_of<T>(x, w));
+          }
+        }
+      }
+      if (gr.lig == 0) a.hcounter[h] = 0u;  // every chunk arrived: reset for the next launch
+    }
+
+    // ---- vertex epilogue: FMax, RMax, MU_raw, next VF', VR'
+    const int indeg = __ldg(a.d_off + v + 1) - __ldg(a.d_off + v);
+    const int outdeg = __ldg(a.s_off + v + 1) - __ldg(a.s_off + v);
+    const size_t vrow = (size_t)v * Pp;
+    VT bv[NQV];
+#pragma unroll
+    for (int k = 0; k < NQV; ++k) {
+      const int qv = gr.lig + G * k;
+      VT vfv = vzero<T>(), emv = vzero<T>();
+      bv[k] = vzero<T>();
+      if (qv * W < Pp) {
+        vfv = reinterpret_cast<const VT*>(a.vf + vrow)[qv];
+        emv = __ldg(reinterpret_cast<const VT*>(a.dEmin + vrow) + qv);
+        bv[k] = __ldg(reinterpret_cast<const VT*>(a.B + vrow) + qv);
+      }
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        const int q = qv * W + w;
+        if (q < Pe) {
+          T F = s_fillF[q];
+          if (indeg > 0) F = fmax(F, (acc[k * W + w] - s_lF[q]) - s_lFlo[q]);
+          T R = s_fillR[q];
+          if (outdeg > 0)
+            R = fmax(R, ((lane_of<T>(vfv, w) - lane_of<T>(emv, w)) - s_lR[q]) - s_lRlo[q]);
+          my_F[q] = F;
+          my_R[q] = R;
+        }
+      }
+    }
+    __syncwarp(gr.mask);
+#pragma unroll
+    for (int j = 0; j < kNPV; ++j) {
+      const int p = gr.lig + G * j;
+      if (p < Pn) {
+        T mu = -__ldg(a.CV + (size_t)v * Pn + p);
+        for (int t = s_inoff[p]; t < s_inoff[p + 1]; ++t) mu += my_F[s_inq[t]];
+        for (int t = s_outoff[p]; t < s_outoff[p + 1]; ++t) mu += my_R[s_outq[t]];
+        my_MU[p] = mu;
+        lmu[j].add(mu);
+        if (a.last) a.mu_raw[(size_t)v * Pn + p] = (double)mu;
+      }
+    }
+    __syncwarp(gr.mask);
+    if (!a.last) {
+#pragma unroll
+      for (int k = 0; k < NQV; ++k) {
+        const int qv = gr.lig + G * k;
+        VT nf = vzero<T>(), nr = vzero<T>();
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+          const int q = qv * W + w;
+          if (q < Pe) {
+            const T f = my_MU[s_pdst[q]] - my_F[q];
+            const T r = my_MU[s_psrc[q]] - my_R[q];
+            lane_of<T>(nf, w) = f;
+            lane_of<T>(nr, w) = r;
+            mxF[k * W + w] = fmax(mxF[k * W + w], f);
+            mxR[k * W + w] = fmax(mxR[k * W + w], r);
+            const T b = lane_of<T>(bv[k], w);
+            lr[k * W + w].add(f + b);
+            lf[k * W + w].add(r + b);
+          }
+        }
+        if (qv * W < Pp) {
+          reinterpret_cast<VT*>(a.vf + vrow)[qv] = nf;
+          reinterpret_cast<VT*>(a.vr_out + vrow)[qv] = nr;
+        }
+      }
+    }
+    __syncwarp(gr.mask);
+  }
+
+  // ---- block partials: mVF, mVR (max), lR, lF, S (lse)
+  const StatSpec spec{2 * Pe, 2 * Pe + Pn};
+  const int slots = spec.slots();
+  double* red = s_red + (size_t)(threadIdx.x >> 5) * slots;
+#pragma unroll
+  for (int k = 0; k < NQV; ++k)
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      const int q = (gr.lig + G * k) * W + w;
+      const double f = warp_group_max<G>((double)mxF[k * W + w]);
+      const double r = warp_group_max<G>((double)mxR[k * W + w]);
+      double m1 = lr[k * W + w].mval(), s1 = lr[k * W + w].sval();
+      double m2 = lf[k * W + w].mval(), s2 = lf[k * W + w].sval();
+      warp_group_lse<G>(m1, s1);
+      warp_group_lse<G>(m2, s2);
+      if (gr.gw == 0 && q < Pe) {
+        red[q] = f;
+        red[Pe + q] = r;
+        red[spec.nmax + 2 * q] = m1;
+        red[spec.nmax + 2 * q + 1] = s1;
+        red[spec.nmax + 2 * (Pe + q)] = m2;
+        red[spec.nmax + 2 * (Pe + q) + 1] = s2;
+      }
+    }
+#pragma unroll
+  for (int j = 0; j < kNPV; ++j) {
+    const int p = gr.lig + G * j;
+    double m = lmu[j].mval(), s = lmu[j].sval();
+    warp_group_lse<G>(m, s);
+    if (gr.gw == 0 && p < Pn) {
+      red[spec.nmax + 2 * (2 * Pe + p)] = m;
+      red[spec.nmax + 2 * (2 * Pe + p) + 1] = s;
+    }
+  }
+  __syncthreads();
+  block_partials_out(s_red, kWarps, spec, a.bpart);
+}
+
+// ----------------------------------------------------------- cdist (SIMT)
+// Difference form sqrt(sum_k (x_k - y_k)^2), as ac.hxx:33-56, in T.
+template <typename T>
+__global__ void __launch_bounds__(256)
+cdist_v_kernel(const CdistVArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int Pn = a.Pn, Kv = a.Kv;
+  double* s_pv = reinterpret_cast<double*>(smem);
+  double* s_red = s_pv + ((Pn * Kv + 1) & ~1);
+  for (int t = threadIdx.x; t < Pn * Kv; t += blockDim.x) s_pv[t] = a.pv[t];
+  __syncthreads();
+  const int R = 256 / Pn;  // vertices per block step
+  const int p = threadIdx.x % Pn, rl = threadIdx.x / Pn;
+  double mx = -CUDART_INF;
+  OnlineLse<double> lp, ln;
+  lp.init();
+  ln.init();
+  if (rl < R) {
+    for (long long v = (long long)blockIdx.x * R + rl; v < a.Dn; v += (long long)gridDim.x * R) {
+      const double* x = a.dv + (size_t)v * Kv;
+      const double* y = s_pv + p * Kv;
+      T acc = T(0);
+      for (int k = 0; k < Kv; ++k) {
+        const T d = (T)y[k] - (T)__ldg(x + k);
+        acc += d * d;
+      }
+      const T dist = sqrt(acc);
+      a.dV[(size_t)v * Pn + p] = dist;
+      const double dd = (double)dist;
+      mx = fmax(mx, -dd);
+      lp.add(dd);
+      ln.add(-dd);
+    }
+  }
+  // per-p block reduction over the R rows, in row order
+  const int slots = 5 * Pn;  // nmax = Pn, nlse = 2 Pn
+  double* red = s_red;       // [R][5]
+  if (rl < R) {
+    red[(rl * Pn + p) * 5 + 0] = mx;
+    red[(rl * Pn + p) * 5 + 1] = lp.m;
+    red[(rl * Pn + p) * 5 + 2] = lp.s;
+    red[(rl * Pn + p) * 5 + 3] = ln.m;
+    red[(rl * Pn + p) * 5 + 4] = ln.s;
+  }
+  __syncthreads();
+  (void)slots;
+  for (int pp = threadIdx.x; pp < Pn; pp += blockDim.x) {
+    double m = -CUDART_INF, am = -CUDART_INF, as = 0.0, bm = -CUDART_INF, bs = 0.0;
+    for (int r = 0; r < R; ++r) {
+      const double* e = red + (r * Pn + pp) * 5;
+      m = fmax(m, e[0]);
+      lse_merge(am, as, e[1], e[2]);
+      lse_merge(bm, bs, e[3], e[4]);
+    }
+    const int nmax = Pn;
+    a.bpart[(size_t)pp * gridDim.x + blockIdx.x] = m;
+    a.bpart[(size_t)(nmax + 2 * pp) * gridDim.x + blockIdx.x] = am;
+    a.bpart[(size_t)(nmax + 2 * pp + 1) * gridDim.x + blockIdx.x] = as;
+    a.bpart[(size_t)(nmax + 2 * (Pn + pp)) * gridDim.x + blockIdx.x] = bm;
+    a.bpart[(size_t)(nmax + 2 * (Pn + pp) + 1) * gridDim.x + blockIdx.x] = bs;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+cdist_e_kernel(const CdistEArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int Pe = a.Pe, Pp = a.Pp, Ke = a.Ke;
+  double* s_pe = reinterpret_cast<double*>(smem);
+  double* s_red = s_pe + ((Pe * Ke + 1) & ~1);
+  for (int t = threadIdx.x; t < Pe * Ke; t += blockDim.x) s_pe[t] = a.pe[t];
+  __syncthreads();
+  const int R = 256 / Pp;
+  const int q = threadIdx.x % Pp, rl = threadIdx.x / Pp;
+  OnlineLse<double> lb;
+  lb.init();
+  if (rl < R) {
+    const long long qbase = (long long)q * a.De;
+    for (long long i = (long long)blockIdx.x * R + rl; i < a.De; i += (long long)gridDim.x * R) {
+      T dist = T(0);
+      if (q < Pe) {
+        const int e = __ldg(a.eid + i);
+        const double* x = a.ef + (size_t)e * Ke;
+        const double* y = s_pe + q * Ke;
+        T acc = T(0);
+        for (int k = 0; k < Ke; ++k) {
+          const T d = (T)y[k] - (T)__ldg(x + k);
+          acc += d * d;
+        }
+        dist = sqrt(acc);
+        if (qbase + e < a.lim) lb.add(-(double)dist);
+      }
+      a.dE[(size_t)i * Pp + q] = dist;
+    }
+  }
+  double* red = s_red;  // [R][Pp][2]
+  if (rl < R) {
+    red[(rl * Pp + q) * 2 + 0] = lb.m;
+    red[(rl * Pp + q) * 2 + 1] = lb.s;
+  }
+  __syncthreads();
+  for (int qq = threadIdx.x; qq < Pe; qq += blockDim.x) {
+    double m = -CUDART_INF, s = 0.0;
+    for (int r = 0; r < R; ++r) lse_merge(m, s, red[(r * Pp + qq) * 2], red[(r * Pp + qq) * 2 + 1]);
+    a.bpart[(size_t)(2 * qq) * gridDim.x + blockIdx.x] = m;
+    a.bpart[(size_t)(2 * qq + 1) * gridDim.x + blockIdx.x] = s;
+  }
+}
+
+// ------------------------------------------------------ static row passes
+template <typename T, int G, int NQV>
+__global__ void __launch_bounds__(kThreads)
+row_pass_kernel(const RowPassArgs<T> a) {
+  using VT = typename Vec<T>::type;
+  constexpr int W = Vec<T>::W;
+  constexpr int NQ = NQV * W;
+  constexpr int GPB = kThreads / G;
+  const int Pe = a.Pe, Pp = a.Pp;
+  const Grp<G> gr;
+  const int gib = threadIdx.x / G;
+  const int gstride = gridDim.x * GPB;
+  for (int it = blockIdx.x * GPB + gib; it < a.nitems; it += gstride) {
+    const int4 item = a.items[it];
+    const int v = item.x, i0 = item.y, i1 = item.z, h = item.w;
+    T mn[NQ], bx[NQ];
+    OnlineLse<T> ls[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      mn[k] = pos_inf<T>();
+      bx[k] = neg_inf<T>();
+      ls[k].init();
+    }
+    for (int j = i0; j < i1; ++j) {
+      const int r = a.src_mode ? __ldg(a.row_of + j) : j;
+      const long long e = __ldg(a.eid_of_row + r);
+      const VT* row = reinterpret_cast<const VT*>(a.dE + (size_t)r * Pp);
+#pragma unroll
+      for (int k = 0; k < NQV; ++k) {
+        const int qv = gr.lig + G * k;
+        if (qv * W < Pp) {
+          const VT x = __ldg(row + qv);
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            const int q = qv * W + w;
+            const T d = lane_of<T>(x, w);
+            const T buf = ((long long)q * a.De + e < a.lim) ? -d : T(0);
+            bx[k * W + w] = fmax(bx[k * W + w], buf);
+            if (a.src_mode) {
+              mn[k * W + w] = fmin(mn[k * W + w], d);
+              ls[k * W + w].add(-d);
+            }
+          }
+        }
+      }
+    }
+    if (h >= 0) {
+      const int c = (i0 - __ldg(a.off + v)) / a.chunk;
+      T* prow = a.partial + (size_t)(__ldg(a.hbase + h) + c) * 4 * Pp;
+#pragma unroll
+      for (int k = 0; k < NQV; ++k)
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+          const int q = (gr.lig + G * k) * W + w;
+          if (q < Pp) {
+            prow[q] = mn[k * W + w];
+            prow[Pp + q] = (T)ls[k * W + w].mval();
+            prow[2 * Pp + q] = (T)ls[k * W + w].sval();
+            prow[3 * Pp + q] = bx[k * W + w];
+          }
+        }
+      __threadfence();
+      __syncwarp(gr.mask);
+      unsigned old = 0;
+      if (gr.lig == 0) old = atomicAdd(a.hcounter + h, 1u);
+      old = __shfl_sync(gr.mask, old, 0, G);
+      const int cnt = __ldg(a.hcount + h);
+      if ((int)old != cnt - 1) continue;
+      __threadfence();
+      const T* p0 = a.partial + (size_t)__ldg(a.hbase + h) * 4 * Pp;
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        mn[k] = pos_inf<T>();
+        bx[k] = neg_inf<T>();
+      }
+      double lm[NQ], lsum[NQ];
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        lm[k] = -CUDART_INF;
+        lsum[k] = 0.0;
+      }
+      for (int r = 0; r < cnt; ++r) {
+        const T* pr = p0 + (size_t)r * 4 * Pp;
+#pragma unroll
+        for (int k = 0; k < NQV; ++k)
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            const int q = (gr.lig + G * k) * W + w;
+            if (q < Pp) {
+              mn[k * W + w] = fmin(mn[k * W + w], __ldcg(pr + q));
+              lse_merge(lm[k * W + w], lsum[k * W + w], (double)__ldcg(pr + Pp + q),
+                        (double)__ldcg(pr + 2 * Pp + q));
+              bx[k * W + w] = fmax(bx[k * W + w], __ldcg(pr + 3 * Pp + q));
+            }
+          }
+      }
+      if (gr.lig == 0) a.hcounter[h] = 0u;
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        ls[k].init();
+        ls[k].m = (T)lm[k];
+        ls[k].s = (T)lsum[k];
+      }
+    }
+    const size_t vrow = (size_t)v * Pp;
+#pragma unroll
+    for (int k = 0; k < NQV; ++k)
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        const int q = (gr.lig + G * k) * W + w;
+        if (q < Pp) {
+          a.out_buf[vrow + q] = bx[k * W + w];
+          if (a.src_mode) {
+            a.out_min[vrow + q] = mn[k * W + w];
+            const double m = ls[k * W + w].mval(), s = ls[k * W + w].sval();
+            a.out_lse[vrow + q] = (m > -CUDART_INF && s > 0.0) ? (T)(m + log(s)) : neg_inf<T>();
+          }
+        }
+      }
+  }
+}
+
+// ------------------------------------------------------ init vertex pass
+// CV = dV - LSE_v(dV), MU0 = -dV - LSE_v(-dV) (main.cu:112,116-117);
+// RMax0/FMax0 from the quirk buffer maxima (main.cu:113-114,119-120,135-146);
+// then VF, VR of the first iteration (main.cu:165-176) and their statistics.
+template <typename T, int G, int NQV>
+__global__ void __launch_bounds__(kThreads)
+init_vertex_kernel(const InitArgs<T> a) {
+  constexpr int W = Vec<T>::W;
+  constexpr int NQ = NQV * W;
+  constexpr int GPB = kThreads / G;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int Pe = a.Pe, Pn = a.Pn, Pp = a.Pp;
+  Carve cv{smem};
+  int* s_pat = cv.take<int>(pattern_ints(Pn, Pe));
+  double* s_lse1 = cv.take<double>(Pn);
+  double* s_lse2 = cv.take<double>(Pn);
+  double* s_vfmax0 = cv.take<double>(Pe);
+  double* s_vrmax0 = cv.take<double>(Pe);
+  double* s_lbuf = cv.take<double>(Pe);
+  T* s_grp = cv.take<T>((size_t)GPB * Pn);
+  double* s_red = cv.take<double>((size_t)kWarps * 6 * Pe);
+  const int* s_psrc = s_pat;
+  const int* s_pdst = s_pat + Pe;
+  for (int t = threadIdx.x; t < pattern_ints(Pn, Pe); t += kThreads) s_pat[t] = a.pat[t];
+  __syncthreads();
+  for (int p = threadIdx.x; p < Pn; p += kThreads) {
+    s_lse1[p] = a.gv[Pn + p];
+    s_lse2[p] = a.gv[2 * Pn + p];
+  }
+  for (int q = threadIdx.x; q < Pe; q += kThreads) {
+    s_vfmax0[q] = a.gv[s_pdst[q]] - a.gv[2 * Pn + s_pdst[q]];
+    s_vrmax0[q] = a.gv[s_psrc[q]] - a.gv[2 * Pn + s_psrc[q]];
+    // zeros of quirk row q: elements with flat index >= lim
+    long long covered = a.lim - (long long)q * a.De;
+    covered = covered < 0 ? 0 : (covered > a.De ? a.De : covered);
+    LseD r;  // LSE of the whole quirk row: covered part (ge) plus its zeros
+    r.init();
+    if (a.ge[q] > -CUDART_INF) r.merge(a.ge[q], 1.0);
+    const long long zeros = a.De - covered;
+    if (zeros > 0) r.merge(0.0, (double)zeros);
+    s_lbuf[q] = r.value();
+  }
+  __syncthreads();
+  const Grp<G> gr;
+  const int gib = threadIdx.x / G;
+  T* my_MU = s_grp + (size_t)gib * Pn;
+  T mxF[NQ], mxR[NQ];
+  OnlineLse<T> lr[NQ], lf[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    mxF[k] = neg_inf<T>();
+    mxR[k] = neg_inf<T>();
+    lr[k].init();
+    lf[k].init();
+  }
+  const int gstride = gridDim.x * GPB;
+  for (int v = blockIdx.x * GPB + gib; v < a.Dn; v += gstride) {
+    for (int p = gr.lig; p < Pn; p += G) {
+      const double dv = (double)a.CV[(size_t)v * Pn + p];
+      a.CV[(size_t)v * Pn + p] = (T)(dv - s_lse1[p]);
+      my_MU[p] = (T)(-dv - s_lse2[p]);
+    }
+    __syncwarp(gr.mask);
+    const int indeg = a.d_off[v + 1] - a.d_off[v];
+    const int outdeg = a.s_off[v + 1] - a.s_off[v];
+    const size_t vrow = (size_t)v * Pp;
+#pragma unroll
+    for (int k = 0; k < NQV; ++k)
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        const int q = (gr.lig + G * k) * W + w;
+        if (q < Pp) {
+          T f = T(0), r = T(0);
+          if (q < Pe) {
+            double R0 = s_vfmax0[q], F0 = s_vrmax0[q];
+            if (outdeg > 0) R0 = fmax(R0, (double)a.Rbuf[vrow + q] - s_lbuf[q]);
+            if (indeg > 0) F0 = fmax(F0, (double)a.Fbuf[vrow + q] - s_lbuf[q]);
+            f = (T)((double)my_MU[s_pdst[q]] - F0);
+            r = (T)((double)my_MU[s_psrc[q]] - R0);
+            const T b = a.B[vrow + q];
+            mxF[k * W + w] = fmax(mxF[k * W + w], f);
+            mxR[k * W + w] = fmax(mxR[k * W + w], r);
+            lr[k * W + w].add(f + b);
+            lf[k * W + w].add(r + b);
+          }
+          a.vf[vrow + q] = f;
+          a.vr[vrow + q] = r;
+        }
+      }
+    __syncwarp(gr.mask);
+  }
+  const StatSpec spec{2 * Pe, 2 * Pe};
+  const int slots = spec.slots();
+  double* red = s_red + (size_t)(threadIdx.x >> 5) * slots;
+#pragma unroll
+  for (int k = 0; k < NQV; ++k)
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      const int q = (gr.lig + G * k) * W + w;
+      const double f = warp_group_max<G>((double)mxF[k * W + w]);
+      const double r = warp_group_max<G>((double)mxR[k * W + w]);
+      double m1 = lr[k * W + w].mval(), s1 = lr[k * W + w].sval();
+      double m2 = lf[k * W + w].mval(), s2 = lf[k * W + w].sval();
+      warp_group_lse<G>(m1, s1);
+      warp_group_lse<G>(m2, s2);
+      if (gr.gw == 0 && q < Pe) {
+        red[q] = f;
+        red[Pe + q] = r;
+        red[spec.nmax + 2 * q] = m1;
+        red[spec.nmax + 2 * q + 1] = s1;
+        red[spec.nmax + 2 * (Pe + q)] = m2;
+        red[spec.nmax + 2 * (Pe + q) + 1] = s2;
+      }
+    }
+  __syncthreads();
+  block_partials_out(s_red, kWarps, spec, a.bpart);
+}
+
+__global__ void mu_output_kernel(double* __restrict__ mu, const double* __restrict__ S,
+                                 long long n, int Pn) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) mu[i] -= S[i % Pn];
+}
+
+template <typename T>
+size_t iter_smem(GroupShape gs, int pn, int pe, int pp) {
+  const int GPB = kThreads / gs.G;
+  return carve_bytes(pattern_ints(pn, pe), sizeof(int)) + 6 * carve_bytes(pe, sizeof(T)) +
+         carve_bytes((size_t)GPB * (2 * pp + pn), sizeof(T)) +
+         carve_bytes((size_t)kWarps * (6 * pe + 2 * pn), sizeof(double));
+}
+
+template <typename T>
+size_t init_smem(GroupShape gs, int pn, int pe) {
+  const int GPB = kThreads / gs.G;
+  return carve_bytes(pattern_ints(pn, pe), sizeof(int)) + 2 * carve_bytes(pn, sizeof(double)) +
+         3 * carve_bytes(pe, sizeof(double)) + carve_bytes((size_t)GPB * pn, sizeof(T)) +
+         carve_bytes((size_t)kWarps * 6 * pe, sizeof(double));
+}
+
+// Dispatch over the instantiated group shapes.
+#define ACG_SHAPES(X) \
+  X(8, 1) X(16, 1) X(32, 1) X(32, 2) X(32, 3) X(32, 4)
+
+template <typename T, typename F>
+acg_status dispatch_shape(GroupShape gs, F&& f);
+
+}  // namespace
+
+GroupShape choose_shape(int elem_bytes, int pp, int pn) {
+  const int W = 16 / elem_bytes;
+  const int nvec = (pp + W - 1) / W;
+  const int gmin_p = (pn + kNPV - 1) / kNPV;
+  GroupShape gs{32, 1};
+  for (int g : {8, 16, 32})
+    if (g >= nvec && g >= gmin_p) {
+      gs.G = g;
+      gs.NQV = 1;
+      return gs;
+    }
+  gs.G = 32;
+  gs.NQV = (nvec + 31) / 32;
+  return gs;
+}
+
+template <typename T>
+size_t iter_smem_bytes(GroupShape gs, int pn, int pe, int pp) {
+  return iter_smem<T>(gs, pn, pe, pp);
+}
+
+#define ACG_ITER_CASE(G_, N_)                                                           \
+  if (gs.G == G_ && gs.NQV == N_) {                                                     \
+    const size_t sm = iter_smem<T>(gs, a.Pn, a.Pe, a.Pp);                               \
+    if (sm > 48 * 1024)                                                                 \
+      cudaFuncSetAttribute(iter_kernel<T, G_, N_>,                                      \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);       \
+    iter_kernel<T, G_, N_><<<blocks, kThreads, sm, s>>>(a);                             \
+    ACG_LAUNCH_CHECK();                                                                 \
+    return ACG_OK;                                                                      \
+  }
+
+template <typename T>
+acg_status launch_iter(const IterArgs<T>& a, GroupShape gs, int blocks, cudaStream_t s) {
+  ACG_SHAPES(ACG_ITER_CASE)
+  return set_error(ACG_ERR_UNSUPPORTED, "no iteration kernel for G=%d NQV=%d", gs.G, gs.NQV);
+}
+
+#define ACG_OCC_CASE(G_, N_)                                                            \
+  if (gs.G == G_ && gs.NQV == N_) {                                                     \
+    int nb = 0;                                                                         \
+    const size_t sm = iter_smem<T>(gs, pn, pe, pp);                                     \
+    if (sm > 48 * 1024)                                                                 \
+      cudaFuncSetAttribute(iter_kernel<T, G_, N_>,                                      \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);       \
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, iter_kernel<T, G_, N_>,      \
+                                                      kThreads, sm) != cudaSuccess)     \
+      nb = 1;                                                                           \
+    return (nb < 1 ? 1 : nb);                                                           \
+  }
+
+template <typename T>
+int iter_max_blocks(GroupShape gs, int pn, int pe, int pp) {
+  ACG_SHAPES(ACG_OCC_CASE)
+  return 1;
+}
+
+#define ACG_ROW_CASE(G_, N_)                                                            \
+  if (gs.G == G_ && gs.NQV == N_) {                                                     \
+    row_pass_kernel<T, G_, N_><<<blocks, kThreads, 0, s>>>(a);                          \
+    ACG_LAUNCH_CHECK();                                                                 \
+    return ACG_OK;                                                                      \
+  }
+
+template <typename T>
+acg_status launch_row_pass(const RowPassArgs<T>& a, GroupShape gs, int blocks, cudaStream_t s) {
+  if (a.nitems == 0) return ACG_OK;
+  ACG_SHAPES(ACG_ROW_CASE)
+  return set_error(ACG_ERR_UNSUPPORTED, "no row-pass kernel for G=%d NQV=%d", gs.G, gs.NQV);
+}
+
+#define ACG_INIT_CASE(G_, N_)                                                           \
+  if (gs.G == G_ && gs.NQV == N_) {                                                     \
+    const size_t sm = init_smem<T>(gs, a.Pn, a.Pe);                                     \
+    if (sm > 48 * 1024)                                                                 \
+      cudaFuncSetAttribute(init_vertex_kernel<T, G_, N_>,                               \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);       \
+    init_vertex_kernel<T, G_, N_><<<blocks, kThreads, sm, s>>>(a);                      \
+    ACG_LAUNCH_CHECK();                                                                 \
+    return ACG_OK;                                                                      \
+  }
+
+template <typename T>
+acg_status launch_init_vertex(const InitArgs<T>& a, GroupShape gs, int blocks, cudaStream_t s) {
+  ACG_SHAPES(ACG_INIT_CASE)
+  return set_error(ACG_ERR_UNSUPPORTED, "no init kernel for G=%d NQV=%d", gs.G, gs.NQV);
+}
+
+acg_status launch_finalize(const double* bpart, int nblocks, StatSpec spec, double* out,
+                           cudaStream_t s) {
+  const int n = spec.outs();
+  if (n == 0) return ACG_OK;
+  stat_finalize_kernel<<<n, 256, 0, s>>>(bpart, nblocks, spec, out);
+  ACG_LAUNCH_CHECK();
+  return ACG_OK;
+}
+
+template <typename T>
+acg_status launch_cdist_v(const CdistVArgs<T>& a, int blocks, cudaStream_t s) {
+  const int R = 256 / a.Pn;
+  const size_t sm = sizeof(double) * (((size_t)a.Pn * a.Kv + 1) & ~size_t(1)) +
+                    sizeof(double) * (size_t)R * a.Pn * 5;
+  if (sm > 48 * 1024)
+    cudaFuncSetAttribute(cdist_v_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cdist_v_kernel<T><<<blocks, 256, sm, s>>>(a);
+  ACG_LAUNCH_CHECK();
+  return ACG_OK;
+}
+
+template <typename T>
+acg_status launch_cdist_e(const CdistEArgs<T>& a, int blocks, cudaStream_t s) {
+  const int R = 256 / a.Pp;
+  const size_t sm = sizeof(double) * (((size_t)a.Pe * a.Ke + 1) & ~size_t(1)) +
+                    sizeof(double) * (size_t)R * a.Pp * 2;
+  if (sm > 48 * 1024)
+    cudaFuncSetAttribute(cdist_e_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cdist_e_kernel<T><<<blocks, 256, sm, s>>>(a);
+  ACG_LAUNCH_CHECK();
+  return ACG_OK;
+}
+
+acg_status launch_mu_output(double* mu, const double* S, long long Dn, int Pn, cudaStream_t s) {
+  const long long n = Dn * Pn;
+  if (n == 0) return ACG_OK;
+  mu_output_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(mu, S, n, Pn);
+  ACG_LAUNCH_CHECK();
+  return ACG_OK;
+}
+
+template acg_status launch_iter<double>(const IterArgs<double>&, GroupShape, int, cudaStream_t);
+template acg_status launch_iter<float>(const IterArgs<float>&, GroupShape, int, cudaStream_t);
+template int iter_max_blocks<double>(GroupShape, int, int, int);
+template int iter_max_blocks<float>(GroupShape, int, int, int);
+template size_t iter_smem_bytes<double>(GroupShape, int, int, int);
+template size_t iter_smem_bytes<float>(GroupShape, int, int, int);
+template acg_status launch_row_pass<double>(const RowPassArgs<double>&, GroupShape, int, cudaStream_t);
+template acg_status launch_row_pass<float>(const RowPassArgs<float>&, GroupShape, int, cudaStream_t);
+template acg_status launch_init_vertex<double>(const InitArgs<double>&, GroupShape, int, cudaStream_t);
+template acg_status launch_init_vertex<float>(const InitArgs<float>&, GroupShape, int, cudaStream_t);
+template acg_status launch_cdist_v<double>(const CdistVArgs<double>&, int, cudaStream_t);
+template acg_status launch_cdist_v<float>(const CdistVArgs<float>&, int, cudaStream_t);
+template acg_status launch_cdist_e<double>(const CdistEArgs<double>&, int, cudaStream_t);
+template acg_status launch_cdist_e<float>(const CdistEArgs<float>&, int, cudaStream_t);
+
+}  // namespace acg

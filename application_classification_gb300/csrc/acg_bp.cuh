@@ -1,0 +1,150 @@
+// acg_bp.cuh -- declarations of the matcher kernels (acg_bp.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "acg_internal.h"
+
+namespace acg {
+
+// Pattern incidence, as one int array on the device:
+//   psrc[Pe] pdst[Pe] in_off[Pn+1] in_q[Pe] out_off[Pn+1] out_q[Pe]
+// in_q lists, for each pattern vertex p, the pattern edges q with dst_q == p
+// (ascending q); out_q those with src_q == p.
+__host__ __device__ inline int pattern_ints(int pn, int pe) { return 4 * pe + 2 * (pn + 1); }
+
+// Statistics produced by a kernel as per-block partials and combined by
+// stat_finalize: `nmax` maxima, then `nlse` log-sum-exps (each an (m, s) pair
+// in the partial buffer).  Partial layout: slot-major, [slot][block].
+struct StatSpec {
+  int nmax;
+  int nlse;
+  __host__ __device__ int slots() const { return nmax + 2 * nlse; }
+  __host__ __device__ int outs() const { return nmax + nlse; }
+};
+
+// Arguments of one BP iteration (the fused edge + vertex pass).
+template <typename T>
+struct IterArgs {
+  const int4* items;
+  int nitems;
+  const int* src_of;    // [De] source vertex at each dst-CSR position
+  const int* d_off;     // [Dn+1] dst-CSR offsets
+  const int* s_off;     // [Dn+1] src-CSR offsets
+  const T* dE;          // [De][Pp] distances in dst-CSR order
+  const T* vr_in;       // [Dn][Pp] unshifted VR of the previous iteration
+  T* vr_out;            // [Dn][Pp] unshifted VR of this iteration
+  T* vf;                // [Dn][Pp] unshifted VF (read, then overwritten)
+  const T* dEmin;       // [Dn][Pp] min over out-edges of dE (static)
+  const T* B;           // [Dn][Pp] log sum over out-edges of exp(-dE) (static)
+  const T* CV;          // [Dn][Pn] normalised vertex cost
+  T* partial;           // [npartial][Pp] chunk maxima of heavy vertices
+  const int* hbase;
+  const int* hcount;
+  unsigned* hcounter;
+  int chunk;
+  const double* glob_in;  // [mVF|mVR|lR|lF|S] of the previous iteration
+  double* bpart;          // block partials of this iteration
+  double* mu_raw;         // [Dn][Pn] unnormalised mu (last iteration only)
+  const int* pat;         // pattern incidence
+  int Dn, Pn, Pe, Pp;
+  int last;
+};
+
+// Launch configuration chosen per (value type, Pp, Pn).
+struct GroupShape {
+  int G;    // lanes per vertex
+  int NQV;  // 16-byte vectors per lane
+};
+GroupShape choose_shape(int elem_bytes, int pp, int pn);
+
+template <typename T>
+acg_status launch_iter(const IterArgs<T>& a, GroupShape gs, int blocks, cudaStream_t s);
+template <typename T>
+int iter_max_blocks(GroupShape gs, int pn, int pe, int pp);
+template <typename T>
+size_t iter_smem_bytes(GroupShape gs, int pn, int pe, int pp);
+
+acg_status launch_finalize(const double* bpart, int nblocks, StatSpec spec, double* out,
+                           cudaStream_t s);
+
+// ---- initialisation kernels
+template <typename T>
+struct CdistVArgs {
+  const double* dv;  // [Dn][Kv]
+  const double* pv;  // [Pn][Kv]
+  T* dV;             // [Dn][Pn] raw distances (normalised in place by init_vertex)
+  double* bpart;     // stats: max(-dV) (Pn), LSE(dV) (Pn), LSE(-dV) (Pn)
+  int Dn, Pn, Kv;
+};
+template <typename T>
+acg_status launch_cdist_v(const CdistVArgs<T>& a, int blocks, cudaStream_t s);
+
+template <typename T>
+struct CdistEArgs {
+  const double* ef;   // [De][Ke] original edge order
+  const int* eid;     // [De] original edge id at each dst-CSR position
+  const double* pe;   // [Pe][Ke]
+  T* dE;              // [De][Pp] out, dst-CSR order
+  double* bpart;      // stats: LSE over covered elements of -dE (Pe)
+  long long De;
+  int Pe, Pp, Ke;
+  long long lim;      // Pn * Dn: flat positions below it hold -dE in the quirk buffer
+};
+template <typename T>
+acg_status launch_cdist_e(const CdistEArgs<T>& a, int blocks, cudaStream_t s);
+
+// Static per-vertex reductions over a CSR of dE rows.
+//   src mode: dEmin, B = LSE(-dE), Rbuf = max of the quirk buffer, over out-edges
+//   dst mode: Fbuf = max of the quirk buffer, over in-edges
+template <typename T>
+struct RowPassArgs {
+  const int4* items;
+  int nitems;
+  const int* row_of;  // src mode: dst-CSR row of each src-CSR position; dst mode: null
+  const int* eid_of_row;  // [De] original edge id of each dst-CSR row
+  const T* dE;
+  T* partial;         // [npartial][4][Pp]
+  const int* hbase;
+  const int* hcount;
+  unsigned* hcounter;
+  int chunk;
+  const int* off;     // CSR offsets (for chunk index)
+  T* out_min;         // src: dEmin
+  T* out_lse;         // src: B
+  T* out_buf;         // src: Rbuf, dst: Fbuf
+  long long De;
+  long long lim;
+  int Dn, Pe, Pp;
+  int src_mode;
+};
+template <typename T>
+acg_status launch_row_pass(const RowPassArgs<T>& a, GroupShape gs, int blocks, cudaStream_t s);
+
+template <typename T>
+struct InitArgs {
+  const int* d_off;
+  const int* s_off;
+  T* CV;               // [Dn][Pn]: raw dV in, normalised cost out
+  const T* Rbuf;       // [Dn][Pp]
+  const T* Fbuf;       // [Dn][Pp]
+  const T* B;          // [Dn][Pp]
+  T* vf;               // [Dn][Pp] out: VF of iteration 1
+  T* vr;               // [Dn][Pp] out: VR of iteration 1
+  const double* gv;    // [maxneg(Pn) | lse_pos(Pn) | lse_neg(Pn)]
+  const double* ge;    // [Pe] LSE over covered quirk elements
+  double* bpart;       // stats: mVF, mVR (max), lR, lF (lse)
+  const int* pat;
+  long long De;
+  long long lim;
+  int Dn, Pn, Pe, Pp;
+};
+template <typename T>
+acg_status launch_init_vertex(const InitArgs<T>& a, GroupShape gs, int blocks, cudaStream_t s);
+
+// mu[v][p] -= S[p]
+acg_status launch_mu_output(double* mu, const double* S, long long Dn, int Pn, cudaStream_t s);
+
+}  // namespace acg

@@ -1,0 +1,366 @@
+// acg_csr.cu -- graph-structure primitives: exclusive scan, stable LSD radix
+// sort, CSR offsets and the chunked work-item lists.
+//
+// The reference has no CSR: it scatters every (pattern edge, data edge) value
+// with a compare-and-swap max into the endpoint's slot (ac.hxx:115-149,
+// helpers.hxx:36-55).  Here both orderings of the data edges -- grouped by
+// destination and grouped by source -- are built once per data graph, so every
+// edge->vertex message becomes a segmented reduction with no atomics.
+//
+// All of this is integer, HBM-bound work; the sort is stable so that each CSR
+// segment lists its edges in increasing original edge id, which makes every
+// later floating-point reduction order (and so every result) deterministic.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
+#include "acg_device.cuh"
+#include "acg_internal.h"
+
+namespace acg {
+
+acg_status dev_alloc(std::vector<DevBuf>* owned, size_t bytes, void** out, cudaStream_t s) {
+  if (bytes == 0) bytes = 16;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(ACG_ERR_OUT_OF_MEMORY, "cudaMalloc(%zu) failed: %s", bytes,
+                     cudaGetErrorString(e));
+  }
+  e = cudaMemsetAsync(p, 0, bytes, s);
+  if (e != cudaSuccess) {
+    cudaFree(p);
+    return set_error(ACG_ERR_CUDA, "cudaMemsetAsync failed: %s", cudaGetErrorString(e));
+  }
+  owned->push_back({p, bytes});
+  *out = p;
+  return ACG_OK;
+}
+
+void dev_free_all(std::vector<DevBuf>* owned) {
+  for (auto& b : *owned)
+    if (b.p) cudaFree(b.p);
+  owned->clear();
+}
+
+// ---------------------------------------------------------------- scan
+namespace {
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanPerThread = 4;
+constexpr int kScanTile = kScanThreads * kScanPerThread;
+
+// Exclusive scan of one tile per block; writes the tile total to sums[block].
+__global__ void __launch_bounds__(kScanThreads)
+scan_tile_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, size_t n,
+                 uint32_t* __restrict__ sums) {
+  __shared__ uint32_t warp_tot[kScanThreads / 32];
+  const size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanPerThread;
+  uint32_t v[kScanPerThread];
+  uint32_t t = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPerThread; ++k) {
+    v[k] = (base + k < n) ? in[base + k] : 0u;
+    t += v[k];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t inc = t;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) warp_tot[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = warp_tot[lane];
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    warp_tot[lane] = wi - w;  // exclusive prefix of warp totals
+    if (lane == 31 && sums) sums[blockIdx.x] = wi;
+  }
+  __syncthreads();
+  uint32_t run = warp_tot[warp] + inc - t;
+#pragma unroll
+  for (int k = 0; k < kScanPerThread; ++k) {
+    if (base + k < n) out[base + k] = run;
+    run += v[k];
+  }
+}
+
+__global__ void scan_add_kernel(uint32_t* __restrict__ out, size_t n,
+                                const uint32_t* __restrict__ offs) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += offs[i / kScanTile];
+}
+
+}  // namespace
+
+acg_status scan_exclusive_u32(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s) {
+  if (n == 0) return ACG_OK;
+  const size_t nb = (n + kScanTile - 1) / kScanTile;
+  if (nb == 1) {
+    scan_tile_kernel<<<1, kScanThreads, 0, s>>>(in, out, n, nullptr);
+    ACG_LAUNCH_CHECK();
+    return ACG_OK;
+  }
+  uint32_t* sums = nullptr;
+  ACG_CUDA_TRY(cudaMallocAsync((void**)&sums, nb * sizeof(uint32_t), s));
+  scan_tile_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, sums);
+  ACG_LAUNCH_CHECK();
+  acg_status st = scan_exclusive_u32(sums, sums, nb, s);
+  if (st == ACG_OK) {
+    scan_add_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, n, sums);
+    if (cudaGetLastError() != cudaSuccess) st = set_error(ACG_ERR_CUDA, "scan_add launch failed");
+  }
+  cudaFreeAsync(sums, s);
+  return st;
+}
+
+// ----------------------------------------------------------- radix sort
+// One warp owns one tile of kSortTile consecutive keys.  Pass structure:
+// per-tile digit histograms (digit-major) -> exclusive scan -> stable scatter
+// in which each warp walks its tile 32 keys at a time, ranking equal digits
+// with __match_any_sync so that the original order is kept.
+namespace {
+
+constexpr int kSortTile = 4096;
+constexpr int kSortWarps = 8;
+
+__global__ void __launch_bounds__(kSortWarps * 32)
+radix_hist_kernel(const uint32_t* __restrict__ keys, size_t n, int shift, int ntiles,
+                  uint32_t* __restrict__ hist) {
+  __shared__ uint32_t h[kSortWarps][256];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int tile = blockIdx.x * kSortWarps + w;
+  for (int d = lane; d < 256; d += 32) h[w][d] = 0;
+  __syncwarp();
+  if (tile < ntiles) {
+    const size_t lo = (size_t)tile * kSortTile;
+    const size_t hi = min(n, lo + kSortTile);
+    for (size_t i = lo + lane; i < hi; i += 32) atomicAdd(&h[w][(keys[i] >> shift) & 255u], 1u);
+    __syncwarp();
+    for (int d = lane; d < 256; d += 32) hist[(size_t)d * ntiles + tile] = h[w][d];
+  }
+}
+
+__global__ void __launch_bounds__(kSortWarps * 32)
+radix_scatter_kernel(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                     uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, size_t n,
+                     int shift, int ntiles, const uint32_t* __restrict__ offs) {
+  __shared__ uint32_t cnt[kSortWarps][256];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int tile = blockIdx.x * kSortWarps + w;
+  if (tile >= ntiles) return;  // whole warp leaves together
+  for (int d = lane; d < 256; d += 32) cnt[w][d] = offs[(size_t)d * ntiles + tile];
+  __syncwarp();
+  const size_t lo = (size_t)tile * kSortTile;
+  const size_t hi = min(n, lo + kSortTile);
+  const unsigned lt = lanemask_lt();
+  for (size_t b = lo; b < hi; b += 32) {
+    const size_t i = b + lane;
+    const bool valid = i < hi;
+    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+    uint32_t k = 0, v = 0, d = 0, pos = 0;
+    unsigned peers = 0;
+    if (valid) {
+      k = kin[i];
+      v = vin[i];
+      d = (k >> shift) & 255u;
+      peers = __match_any_sync(vmask, d);
+      pos = cnt[w][d] + __popc(peers & lt);
+    }
+    __syncwarp();
+    if (valid && (peers & lt) == 0) cnt[w][d] += __popc(peers);  // group leader
+    __syncwarp();
+    if (valid) {
+      kout[pos] = k;
+      vout[pos] = v;
+    }
+  }
+}
+
+}  // namespace
+
+acg_status radix_sort_pairs_u32(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp,
+                                uint32_t* vals_tmp, size_t n, int bits, cudaStream_t s) {
+  if (n <= 1 || bits <= 0) return ACG_OK;
+  const int ntiles = (int)((n + kSortTile - 1) / kSortTile);
+  const size_t hn = (size_t)ntiles * 256;
+  uint32_t* hist = nullptr;
+  ACG_CUDA_TRY(cudaMallocAsync((void**)&hist, hn * sizeof(uint32_t), s));
+  uint32_t *ka = keys, *va = vals, *kb = keys_tmp, *vb = vals_tmp;
+  acg_status st = ACG_OK;
+  const unsigned blocks = (unsigned)((ntiles + kSortWarps - 1) / kSortWarps);
+  for (int shift = 0; shift < bits && st == ACG_OK; shift += 8) {
+    radix_hist_kernel<<<blocks, kSortWarps * 32, 0, s>>>(ka, n, shift, ntiles, hist);
+    if (cudaGetLastError() != cudaSuccess) {
+      st = set_error(ACG_ERR_CUDA, "radix_hist launch failed");
+      break;
+    }
+    st = scan_exclusive_u32(hist, hist, hn, s);
+    if (st != ACG_OK) break;
+    radix_scatter_kernel<<<blocks, kSortWarps * 32, 0, s>>>(ka, va, kb, vb, n, shift, ntiles, hist);
+    if (cudaGetLastError() != cudaSuccess) {
+      st = set_error(ACG_ERR_CUDA, "radix_scatter launch failed");
+      break;
+    }
+    std::swap(ka, kb);
+    std::swap(va, vb);
+  }
+  if (st == ACG_OK && ka != keys) {
+    cudaMemcpyAsync(keys, ka, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(vals, va, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
+  }
+  cudaFreeAsync(hist, s);
+  return st;
+}
+
+// ------------------------------------------------------------------ CSR
+namespace {
+
+__global__ void iota_kernel(uint32_t* __restrict__ v, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = (uint32_t)i;
+}
+
+// off[v] = first position whose key >= v, for v in [0, n]; keys sorted.
+__global__ void csr_offsets_kernel(const uint32_t* __restrict__ keys, int m, int n,
+                                   int* __restrict__ off) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > m) return;
+  const long long prev = i > 0 ? (long long)keys[i - 1] : -1;
+  const long long cur = i < m ? (long long)keys[i] : (long long)n;
+  for (long long v = prev + 1; v <= cur; ++v) off[v] = (int)i;
+}
+
+__global__ void gather_other_kernel(const uint32_t* __restrict__ eid,
+                                    const uint32_t* __restrict__ other, int m,
+                                    int* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) out[i] = (int)other[eid[i]];
+}
+
+}  // namespace
+
+acg_status build_csr(const uint32_t* key, const uint32_t* other, int n, int m, Csr* out,
+                     std::vector<DevBuf>* owned, cudaStream_t s) {
+  out->n = n;
+  out->m = m;
+  ACG_TRY(dev_alloc(owned, sizeof(int) * ((size_t)n + 1), (void**)&out->off, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * (size_t)m, (void**)&out->eid, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * (size_t)m, (void**)&out->other, s));
+  const size_t mm = m > 0 ? (size_t)m : 1;
+  uint32_t *k = nullptr, *k2 = nullptr, *v2 = nullptr;
+  ACG_CUDA_TRY(cudaMallocAsync((void**)&k, mm * sizeof(uint32_t), s));
+  ACG_CUDA_TRY(cudaMallocAsync((void**)&k2, mm * sizeof(uint32_t), s));
+  ACG_CUDA_TRY(cudaMallocAsync((void**)&v2, mm * sizeof(uint32_t), s));
+  acg_status st = ACG_OK;
+  uint32_t* vals = reinterpret_cast<uint32_t*>(out->eid);
+  if (m > 0) {
+    cudaMemcpyAsync(k, key, (size_t)m * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
+    iota_kernel<<<ceil_div(m, 256), 256, 0, s>>>(vals, (size_t)m);
+    int bits = 0;
+    while (bits < 32 && ((uint64_t)(n > 0 ? n - 1 : 0) >> bits) != 0) ++bits;
+    st = radix_sort_pairs_u32(k, vals, k2, v2, (size_t)m, bits, s);
+  }
+  if (st == ACG_OK) {
+    csr_offsets_kernel<<<ceil_div((long long)m + 1, 256), 256, 0, s>>>(k, m, n, out->off);
+    if (m > 0) gather_other_kernel<<<ceil_div(m, 256), 256, 0, s>>>(vals, other, m, out->other);
+    if (cudaGetLastError() != cudaSuccess) st = set_error(ACG_ERR_CUDA, "csr launch failed");
+  }
+  cudaFreeAsync(k, s);
+  cudaFreeAsync(k2, s);
+  cudaFreeAsync(v2, s);
+  return st;
+}
+
+// ---------------------------------------------------------------- items
+namespace {
+
+__global__ void item_counts_kernel(const int* __restrict__ off, int n, int chunk,
+                                   uint32_t* __restrict__ nch, uint32_t* __restrict__ heavy,
+                                   uint32_t* __restrict__ hch) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  const int deg = off[v + 1] - off[v];
+  const int c = deg <= chunk ? 1 : (deg + chunk - 1) / chunk;
+  nch[v] = (uint32_t)c;
+  heavy[v] = c > 1 ? 1u : 0u;
+  hch[v] = c > 1 ? (uint32_t)c : 0u;
+}
+
+__global__ void item_fill_kernel(const int* __restrict__ off, int n, int chunk,
+                                 const uint32_t* __restrict__ item_off,
+                                 const uint32_t* __restrict__ hidx,
+                                 const uint32_t* __restrict__ hrow, int4* __restrict__ items,
+                                 int* __restrict__ hbase, int* __restrict__ hcount) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  const int i0 = off[v], i1 = off[v + 1];
+  const int deg = i1 - i0;
+  const int c = deg <= chunk ? 1 : (deg + chunk - 1) / chunk;
+  const int h = c > 1 ? (int)hidx[v] : -1;
+  if (h >= 0) {
+    hbase[h] = (int)hrow[v];
+    hcount[h] = c;
+  }
+  const uint32_t base = item_off[v];
+  for (int j = 0; j < c; ++j) {
+    const int a = i0 + j * chunk;
+    const int b = c > 1 ? min(i1, a + chunk) : i1;
+    items[base + j] = make_int4(v, a, b, h);
+  }
+}
+
+}  // namespace
+
+acg_status build_items(const Csr& csr, int chunk, Items* out, std::vector<DevBuf>* owned,
+                       cudaStream_t s) {
+  const int n = csr.n;
+  out->chunk = chunk;
+  if (n == 0) {
+    out->nitems = out->nheavy = out->npartial = 0;
+    ACG_TRY(dev_alloc(owned, 16, (void**)&out->items, s));
+    ACG_TRY(dev_alloc(owned, 16, (void**)&out->hbase, s));
+    ACG_TRY(dev_alloc(owned, 16, (void**)&out->hcount, s));
+    ACG_TRY(dev_alloc(owned, 16, (void**)&out->hcounter, s));
+    return ACG_OK;
+  }
+  const size_t nn = (size_t)n + 1;  // one extra slot so the scan yields totals
+  uint32_t* tmp = nullptr;
+  ACG_CUDA_TRY(cudaMallocAsync((void**)&tmp, 3 * nn * sizeof(uint32_t), s));
+  uint32_t *nch = tmp, *heavy = tmp + nn, *hch = tmp + 2 * nn;
+  cudaMemsetAsync(tmp, 0, 3 * nn * sizeof(uint32_t), s);
+  item_counts_kernel<<<ceil_div(n, 256), 256, 0, s>>>(csr.off, n, chunk, nch, heavy, hch);
+  ACG_LAUNCH_CHECK();
+  ACG_TRY(scan_exclusive_u32(nch, nch, nn, s));
+  ACG_TRY(scan_exclusive_u32(heavy, heavy, nn, s));
+  ACG_TRY(scan_exclusive_u32(hch, hch, nn, s));
+  uint32_t tot[3];
+  ACG_CUDA_TRY(cudaMemcpyAsync(&tot[0], nch + n, 4, cudaMemcpyDeviceToHost, s));
+  ACG_CUDA_TRY(cudaMemcpyAsync(&tot[1], heavy + n, 4, cudaMemcpyDeviceToHost, s));
+  ACG_CUDA_TRY(cudaMemcpyAsync(&tot[2], hch + n, 4, cudaMemcpyDeviceToHost, s));
+  ACG_CUDA_TRY(cudaStreamSynchronize(s));
+  out->nitems = (int)tot[0];
+  out->nheavy = (int)tot[1];
+  out->npartial = (int)tot[2];
+  ACG_TRY(dev_alloc(owned, sizeof(int4) * (size_t)out->nitems, (void**)&out->items, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * (size_t)out->nheavy, (void**)&out->hbase, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * (size_t)out->nheavy, (void**)&out->hcount, s));
+  ACG_TRY(dev_alloc(owned, sizeof(unsigned) * (size_t)out->nheavy, (void**)&out->hcounter, s));
+  item_fill_kernel<<<ceil_div(n, 256), 256, 0, s>>>(csr.off, n, chunk, nch, heavy, hch,
+                                                    out->items, out->hbase, out->hcount);
+  ACG_LAUNCH_CHECK();
+  cudaFreeAsync(tmp, s);
+  return ACG_OK;
+}
+
+}  // namespace acg

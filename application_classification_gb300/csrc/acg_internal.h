@@ -1,0 +1,66 @@
+// acg_internal.h -- internal (non-ABI) declarations shared by the CUDA sources.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "acg.h"
+#include "acg_common.h"
+
+namespace acg {
+
+// Device buffer owned by a data/plan object.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+// A CSR ordering of the data edges.  Position i in [off[v], off[v+1]) is an
+// edge whose grouping endpoint is v; positions inside a segment are in
+// increasing original edge id (the sort is stable).
+struct Csr {
+  int n = 0;               // vertices
+  int m = 0;               // edges
+  int* off = nullptr;      // [n + 1]
+  int* eid = nullptr;      // [m] original edge id at each position
+  int* other = nullptr;    // [m] the other endpoint at each position
+};
+
+// Work items of one CSR: item = {vertex, first position, end position, heavy
+// vertex index or -1}.  A vertex with more than `chunk` edges is split into
+// ceil(deg / chunk) items that each reduce into a partial row; the last one to
+// finish combines the partial rows (no waiting, see the kernels).
+struct Items {
+  int4* items = nullptr;   // [nitems]
+  int nitems = 0;
+  int chunk = 0;
+  int nheavy = 0;          // vertices split into chunks
+  int npartial = 0;        // partial rows = total chunks of heavy vertices
+  int* hbase = nullptr;    // [nheavy] first partial row of heavy vertex h
+  int* hcount = nullptr;   // [nheavy] number of chunks of heavy vertex h
+  unsigned* hcounter = nullptr;  // [nheavy] arrival counters, zero between launches
+};
+
+// ---- primitives (acg_csr.cu)
+// Exclusive scan of n uint32 values (in and out may alias); stream ordered.
+acg_status scan_exclusive_u32(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s);
+// Stable LSD radix sort of (key, value) pairs on the low `bits` key bits.
+// Sorted result ends in keys/vals; keys_tmp/vals_tmp are scratch of size n.
+acg_status radix_sort_pairs_u32(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp,
+                                uint32_t* vals_tmp, size_t n, int bits, cudaStream_t s);
+// Build the CSR grouping edges by `key[e]` (the other endpoint is `other[e]`).
+acg_status build_csr(const uint32_t* key, const uint32_t* other, int n, int m, Csr* out,
+                     std::vector<DevBuf>* owned, cudaStream_t s);
+// Work items for a CSR with the given chunk length (synchronises `s`).
+acg_status build_items(const Csr& csr, int chunk, Items* out, std::vector<DevBuf>* owned,
+                       cudaStream_t s);
+
+// Allocate `bytes` (>= 1) of device memory, zero it, record it in `owned`.
+acg_status dev_alloc(std::vector<DevBuf>* owned, size_t bytes, void** out, cudaStream_t s);
+void dev_free_all(std::vector<DevBuf>* owned);
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace acg

@@ -1,0 +1,172 @@
+"""Python host API over the C ABI: the reference's driver flow with device-resident graphs.
+
+The reference's ``main`` (src/main.cu:66-257) loads two graphs to the device,
+runs the matcher and copies ``MU`` back.  Here:
+
+* :class:`DeviceGraph` holds a graph's arrays on a CUDA device (what
+  ``loadGraph`` does, main.cu:54-62),
+* :class:`DataGraph` is ``acg_data`` (the data graph with its two CSR
+  orderings, built once and shared by every pattern),
+* :class:`Plan` is ``acg_plan`` (one pattern against one data graph),
+* :func:`match` is the one-shot host-to-host call.
+
+PyTorch provides device memory and streams only; every kernel is the native
+library's.  There is no CPU fallback: without CUDA these raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .graph import Graph
+
+PRECISIONS = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
+
+
+def _torch():
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("CUDA is not available: the matcher runs on the GPU only")
+    return torch
+
+
+def _stream_ptr(stream) -> int:
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+class DeviceGraph:
+    """A graph's four arrays on a CUDA device (f64 features, u64 endpoints)."""
+
+    def __init__(self, g: Graph, device="cuda", pinned: bool = False, stream=None):
+        torch = _torch()
+        self.num_nodes, self.node_feat_dim = g.node_feats.shape
+        self.num_edges, self.edge_feat_dim = g.edge_feats.shape
+
+        def up(a, dtype):
+            t = torch.from_numpy(a.view(np.int64) if a.dtype == np.uint64 else a)
+            if pinned:
+                t = t.pin_memory()
+            return t.to(device, non_blocking=pinned)
+
+        self.node_feats = up(g.node_feats, None)
+        self.edge_feats = up(g.edge_feats, None)
+        self.srcs = up(g.srcs, None)
+        self.dsts = up(g.dsts, None)
+
+    @classmethod
+    def from_tensors(cls, node_feats, edge_feats, srcs, dsts) -> "DeviceGraph":
+        """Wrap device tensors (f64 [N][Kv], f64 [M][Ke], int64/uint64 [M] x2)."""
+        self = cls.__new__(cls)
+        self.num_nodes, self.node_feat_dim = node_feats.shape
+        self.num_edges, self.edge_feat_dim = edge_feats.shape
+        self.node_feats, self.edge_feats, self.srcs, self.dsts = node_feats, edge_feats, srcs, dsts
+        return self
+
+    def c_graph(self) -> _lib.Graph:
+        g = _lib.Graph()
+        g.num_nodes, g.node_feat_dim = self.num_nodes, self.node_feat_dim
+        g.num_edges, g.edge_feat_dim = self.num_edges, self.edge_feat_dim
+        g.node_feats = self.node_feats.data_ptr()
+        g.edge_feats = self.edge_feats.data_ptr()
+        g.srcs = self.srcs.data_ptr()
+        g.dsts = self.dsts.data_ptr()
+        return g
+
+
+class DataGraph:
+    """``acg_data``: a data graph prepared for matching (CSR orderings)."""
+
+    def __init__(self, graph, stream=None):
+        self.dev = graph if isinstance(graph, DeviceGraph) else DeviceGraph(graph)
+        self._c = self.dev.c_graph()
+        self.handle = C.c_void_p()
+        _lib.check(_lib.lib().acg_data_create(C.byref(self._c), _stream_ptr(stream),
+                                              C.byref(self.handle)), "acg_data_create")
+
+    @property
+    def num_nodes(self) -> int:
+        return self.dev.num_nodes
+
+    def close(self):
+        if self.handle:
+            _lib.lib().acg_data_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Plan:
+    """``acg_plan``: one pattern matched against one :class:`DataGraph`."""
+
+    def __init__(self, data: DataGraph, pattern, precision: str = "fp64", num_iters: int = -1,
+                 stream=None, kernel_timing: bool = False):
+        self.data = data
+        self.pat = pattern if isinstance(pattern, DeviceGraph) else DeviceGraph(pattern)
+        self._c = self.pat.c_graph()
+        opt = _lib.Options()
+        _lib.lib().acg_options_default(C.byref(opt))
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
+        opt.precision = PRECISIONS[precision]
+        opt.num_iters = num_iters
+        opt.kernel_timing = 1 if kernel_timing else 0
+        self.precision = precision
+        self.handle = C.c_void_p()
+        _lib.check(_lib.lib().acg_plan_create(data.handle, C.byref(self._c), C.byref(opt),
+                                              _stream_ptr(stream), C.byref(self.handle)),
+                   "acg_plan_create")
+
+    def run(self, out=None, stream=None):
+        """Run the match; returns (or fills) a [Dn][Pn] float64 device tensor."""
+        torch = _torch()
+        if out is None:
+            out = torch.empty((self.data.num_nodes, self.pat.num_nodes), dtype=torch.float64,
+                              device=self.data.dev.node_feats.device)
+        _lib.check(_lib.lib().acg_match(self.handle, C.c_void_p(out.data_ptr()),
+                                        _stream_ptr(stream)), "acg_match")
+        return out
+
+    def stats(self) -> dict:
+        st = _lib.Stats()
+        _lib.check(_lib.lib().acg_plan_stats(self.handle, C.byref(st)), "acg_plan_stats")
+        return {k: getattr(st, k) for k, _ in _lib.Stats._fields_}
+
+    def close(self):
+        if self.handle:
+            _lib.lib().acg_plan_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def match(data: Graph, pattern: Graph, precision: str = "fp64", num_iters: int = -1,
+          device: str = "cuda") -> np.ndarray:
+    """One-shot match of host graphs; returns mu as a [Dn][Pn] float64 numpy array.
+
+    This is the reference's whole program between reading the two graph files
+    and printing ``MU`` (main.cu:71-257), through ``acg_match_graphs``."""
+    torch = _torch()
+    dg, pg = DeviceGraph(data, device), DeviceGraph(pattern, device)
+    out = torch.empty((dg.num_nodes, pg.num_nodes), dtype=torch.float64, device=device)
+    opt = _lib.Options()
+    _lib.lib().acg_options_default(C.byref(opt))
+    opt.precision = PRECISIONS[precision]
+    opt.num_iters = num_iters
+    cd, cp = dg.c_graph(), pg.c_graph()
+    _lib.check(_lib.lib().acg_match_graphs(C.byref(cd), C.byref(cp), C.byref(opt),
+                                           C.c_void_p(out.data_ptr()), _stream_ptr(None)),
+               "acg_match_graphs")
+    return out.cpu().numpy()

@@ -1,0 +1,425 @@
+#!/usr/bin/env python3
+"""Benchmark of the ApplicationClassification match on GB300.
+
+One step = one whole match (cdist, initial normalisers and edge maxima, every
+BP iteration, output in [Dn][Pn]) of the named synthetic workload, with the
+data graph's CSR orderings built beforehand (they are per data graph, shared by
+every pattern).  Prints one JSON line:
+
+  value       match ms, job level: (max-over-ranks time of the K timed
+              steps) / (K * ranks); inputs resident in HBM, larger than L2
+  e2e         the same metric through the one-shot C-ABI call
+              (acg_match_graphs) from pinned host buffers: every step copies
+              both graphs host->device, builds the CSRs, matches and copies mu
+              back to the host
+  roofline    the dominant kernel (the fused BP iteration) against the
+              measured HBM copy bandwidth
+  plain_fp64  the same match computed entirely in FP64, with the error of
+              the mixed result against it
+  cpu_baseline  the CPU oracle (a pass-by-pass restatement of the reference)
+              on a bounded sample of the workload, scaled to a whole match
+
+``--impl reference`` times the CPU oracle instead (the reference program's
+own CPU build needs its sources, which only the development machine has).
+Multi-GPU runs are independent replicas (one match per rank, no collective in
+the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    # name: (description, sample workload for the CPU baseline)
+    "rmat22": ("RMAT scale 22 (4,194,304 vertices, edge factor 16, a=.57 b=c=.19, dedup, "
+               "no self-loops), planted pattern 32 vertices / 64 edges, 13/17-dim N(0,1) features, "
+               "seed 2", "rmat15_32_64"),
+    "rmat18": ("RMAT scale 18 (262,144 vertices, edge factor 16), planted pattern 16 / 32, "
+               "13/17-dim N(0,1) features, seed 1", "rmat14_16_32"),
+    "rmat20": ("RMAT scale 20, planted pattern 16 / 32, seed 3", "rmat14_16_32"),
+    "er1k": ("Erdos-Renyi 1,000 vertices / 20,000 edges, planted pattern 10 / 20, seed 0",
+             "er1k"),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="rmat22", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(backend):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def max_over_ranks(x: float, ws: int, device=None) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ----------------------------------------------------------------- clocks
+class Clocks:
+    """nvidia-smi samples every 200 ms while running (clock and throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.gpu)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        time.sleep(0.25)
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {}
+
+
+def ncu_traffic(workload: str, precision: str):
+    """Per-launch DRAM bytes of the iteration kernel from a committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    return d.get(f"{workload}/{precision}")
+
+
+# ----------------------------------------------------------- CPU baseline
+def cpu_sample(workload: str, threads: int | None = None):
+    """Time the CPU oracle on the bounded sample; returns (ms per full match, info)."""
+    from application_classification_gb300 import graph
+    from oracle import oracle
+
+    full = _work_units(workload)
+    sample = WORKLOADS[workload][1]
+    d, p, _ = graph.workload(sample)
+    nt = threads or os.cpu_count() or 1
+    _, el_us = oracle.match(d, p, threads=nt, return_elapsed=True)
+    units = _units(d.num_nodes, d.num_edges, p.num_nodes, p.num_edges)
+    ms = el_us / 1e3 * full / units
+    info = {"sample": f"{sample}: {d.num_nodes} vertices / {d.num_edges} edges, pattern "
+                      f"{p.num_nodes}/{p.num_edges}; {el_us/1e6:.2f} s measured, scaled by "
+                      f"(De+Dn)*Pe*(Pn+1) to the full workload (x{full/units:.1f})",
+            "cores": nt, "sample_s": el_us / 1e6}
+    return ms, info
+
+
+def _units(dn, de, pn, pe):
+    return (de + dn) * max(pe, 1) * (pn + 1)
+
+
+_SHAPES = {"rmat22": (4194304, 67108864 * 0.945, 32, 64), "rmat18": (262144, 3939126, 16, 32),
+           "rmat20": (1048576, 16087353, 16, 32), "er1k": (1000, 20000, 10, 20)}
+
+
+def _work_units(workload):
+    dn, de, pn, pe = _SHAPES[workload]
+    return _units(dn, de, pn, pe)
+
+
+# ------------------------------------------------------------------- ours
+def run_ours(args, ws, rank, local):
+    import numpy as np
+    import torch
+
+    from application_classification_gb300 import _lib, graph, matcher
+    import ctypes as C
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+    t0 = time.time()
+    d, p, truth = graph.workload(args.workload)
+    gen_s = time.time() - t0
+    _SHAPES[args.workload] = (d.num_nodes, d.num_edges, p.num_nodes, p.num_edges)
+
+    # ---- device-resident match
+    dg = matcher.DataGraph(d)
+    plan = matcher.Plan(dg, p, args.precision, kernel_timing=True)
+    out = torch.empty((d.num_nodes, p.num_nodes), dtype=torch.float64, device=dev)
+    for _ in range(args.warmup):
+        plan.run(out)
+    torch.cuda.synchronize()
+    barrier(ws)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ms_kernels = []
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            plan.run(out)
+            ms_kernels.append(None)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier(ws)
+    ms_total = ev0.elapsed_time(ev1)
+    st = plan.stats()  # last match of the timed region
+    ms_total = max_over_ranks(ms_total, ws, dev)
+    value = ms_total / (args.steps * ws)
+    mu_mixed = out.cpu().numpy()
+
+    # per-launch duration of the iteration kernel, over the timed matches
+    iter_ms = []
+    for _ in range(min(args.steps, 3)):
+        plan.run(out)
+        iter_ms.append(plan.stats()["ms_iter_kernels"] / max(1, st["num_iters"]))
+    launch_ms = statistics.median(iter_ms)
+    bytes_launch = st["bytes_per_edge_pass"]
+    peaks = measured_peaks()
+    peak = peaks.get("hbm_gbs")
+    achieved = bytes_launch / (launch_ms * 1e-3) / 1e9
+    traffic = ncu_traffic(args.workload, args.precision)
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1),
+                "peak": peak if peak else 6800.0, "unit": "GB/s",
+                "frac": round(achieved / (peak if peak else 6800.0), 4),
+                "traffic": traffic, "kernel": "iter_kernel (fused BP iteration)",
+                "launch_ms": round(launch_ms, 4), "algorithmic_bytes_per_launch": bytes_launch,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peak else "fallback 6.8 TB/s"}
+
+    result = {
+        "metric": "match ms (one whole ApplicationClassification match, "
+                  f"{args.precision} precision)",
+        "value": round(value, 4), "unit": "ms", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_total / args.steps, 4),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][0]}",
+                   "data_vertices": d.num_nodes, "data_edges": d.num_edges,
+                   "pattern_vertices": p.num_nodes, "pattern_edges": p.num_edges,
+                   "precision": args.precision, "bp_iterations": int(st["num_iters"]),
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (edge cost matrix "
+                         f"{d.num_edges * p.num_edges * (4 if args.precision == 'mixed' else 8) / 1e9:.2f} GB "
+                         "streamed every iteration)",
+                   "csr_prebuilt": True, "generation_s": round(gen_s, 1)},
+        "phases_ms": {k: round(st[k], 3) for k in ("ms_cdist", "ms_init", "ms_iters", "ms_total")},
+        "roofline": roofline,
+        "gpu_launches": int(st["launches"]) * args.steps,
+        "clocks": clk.summary(),
+    }
+
+    # ---- plain FP64 on the same input
+    if not args.no_fp64 and args.precision == "mixed":
+        pl64 = matcher.Plan(dg, p, "fp64")
+        out64 = torch.empty_like(out)
+        pl64.run(out64)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.fp64_steps):
+            pl64.run(out64)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1) / args.fp64_steps
+        mu64 = out64.cpu().numpy()
+        s64 = pl64.stats()
+        diff = np.abs(mu_mixed - mu64)
+        a64, am = mu64.argmax(1), mu_mixed.argmax(1)
+        srt = np.sort(mu64, axis=1)
+        tie = (srt[:, -1] - srt[:, -2]) <= 1e-9 * np.maximum(1, np.abs(srt[:, -1]))
+        result["plain_fp64"] = {
+            "ms": round(ms64, 3), "speedup_mixed_vs_fp64": round(ms64 / value, 2),
+            "phases_ms": {k: round(s64[k], 3) for k in ("ms_cdist", "ms_init", "ms_iters")},
+            "max_abs_dmu": float(diff.max()), "max_abs_mu": float(np.abs(mu64).max()),
+            "argmax_identical_except_ties": bool(((a64 == am) | tie).all()),
+            "argmax_mismatch_rows": int((a64 != am).sum()),
+            "planted_recovered": int(sum(int(mu64[:, i].argmax()) == int(truth[i])
+                                         for i in range(p.num_nodes))),
+        }
+        del pl64, out64
+
+    # ---- end to end through the one-shot C-ABI call, host buffers
+    if not args.no_e2e:
+        def pinned(a):
+            t = torch.from_numpy(a.view(np.int64) if a.dtype == np.uint64 else a)
+            return t.pin_memory()
+
+        hs = [pinned(x) for x in (d.node_feats, d.edge_feats, d.srcs, d.dsts,
+                                  p.node_feats, p.edge_feats, p.srcs, p.dsts)]
+        ds = [torch.empty_like(h, device=dev) for h in hs]
+        mu_host = torch.empty((d.num_nodes, p.num_nodes), dtype=torch.float64).pin_memory()
+        opt = _lib.Options()
+        _lib.lib().acg_options_default(C.byref(opt))
+        opt.precision = matcher.PRECISIONS[args.precision]
+        gd = matcher.DeviceGraph.from_tensors(*ds[:4]).c_graph()
+        gp = matcher.DeviceGraph.from_tensors(*ds[4:]).c_graph()
+
+        def e2e_step():
+            for h, dd in zip(hs, ds):
+                dd.copy_(h, non_blocking=True)
+            _lib.check(_lib.lib().acg_match_graphs(C.byref(gd), C.byref(gp), C.byref(opt),
+                                                   C.c_void_p(out.data_ptr()),
+                                                   C.c_void_p(stream.cuda_stream)), "e2e")
+            mu_host.copy_(out, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        barrier(ws)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(ws)
+        e2e_ms = max_over_ranks(e0.elapsed_time(e1), ws, dev) / (args.e2e_steps * ws)
+        result["e2e"] = {"value": round(e2e_ms, 3), "unit": "ms",
+                         "h2d_bytes_per_step": int(sum(h.numel() * h.element_size() for h in hs)),
+                         "d2h_bytes_per_step": int(mu_host.numel() * 8),
+                         "steps": args.e2e_steps,
+                         "includes": "H2D of both graphs, CSR build, allocation, match, D2H of mu"}
+        del hs, ds
+
+    # ---- CPU baseline (rank 0, N=1 only)
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        ms, info = cpu_sample(args.workload)
+        result["cpu_baseline"] = {"value": round(ms, 1), "unit": "ms", "cores": info["cores"],
+                                  "kind": "port", "sample": info["sample"]}
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+
+
+# -------------------------------------------------------------- reference
+def run_reference(args, ws, rank):
+    """The CPU oracle (restatement of the reference program) on a bounded sample."""
+    if rank != 0:
+        return
+    from application_classification_gb300 import graph
+    from oracle import oracle
+
+    full = _work_units(args.workload)
+    sample = WORKLOADS[args.workload][1]
+    d, p, _ = graph.workload(sample)
+    nt = os.cpu_count() or 1
+    units = _units(d.num_nodes, d.num_edges, p.num_nodes, p.num_edges)
+    for _ in range(args.warmup):
+        oracle.match(d, p, threads=nt)
+    els = []
+    t0 = time.time()
+    for _ in range(args.steps):
+        _, el = oracle.match(d, p, threads=nt, return_elapsed=True)
+        els.append(el / 1e3)
+    wall = time.time() - t0
+    ms_sample = sum(els) / len(els)
+    value = ms_sample * full / units
+    print(json.dumps({
+        "impl": "reference",
+        "metric": "match ms (one whole ApplicationClassification match, "
+                  f"{args.precision} precision)",
+        "value": round(value, 1), "unit": "ms", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_sample, 2), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][0]}",
+                   "precision": "fp64 (the reference computes in FP64)"},
+        "cpu_baseline": {"value": round(value, 1), "unit": "ms", "cores": nt, "kind": "port",
+                         "sample": f"{sample}: {d.num_nodes} vertices / {d.num_edges} edges, "
+                                   f"pattern {p.num_nodes}/{p.num_edges}, {ms_sample/1e3:.2f} s per "
+                                   f"sample match, scaled by (De+Dn)*Pe*(Pn+1) x{full/units:.1f}"},
+        "e2e": {"value": round(value, 1), "unit": "ms", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "wall_s": round(wall, 1),
+    }), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        ws, rank, _ = dist_setup("gloo")
+        run_reference(args, ws, rank)
+    else:
+        ws, rank, local = dist_setup("nccl")
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,149 @@
+/*
+ * acg.h -- C ABI of the GB300 ApplicationClassification matcher.
+ *
+ * The reference (porumbes/application_classification) has no library API: its
+ * hot path is the set of `ac::` functions in src/ac.hxx:17-186 plus the inline
+ * Thrust lambdas that src/main.cu:107-247 calls between them.  This header
+ * replaces that whole path -- cdist, the row log-softmax normalisers, the
+ * edge->vertex max messages, the VR/VF/mu updates and the final transpose --
+ * with whole-pipeline entry points, because the GB300 kernels fuse across the
+ * reference's per-op boundaries.
+ *
+ * Conventions
+ *   - Graph arrays passed to acg_data_create / acg_plan_create are DEVICE
+ *     pointers owned by the caller, exactly what `loadGraph` produces
+ *     (main.cu:54-62).  They must stay valid until the object built from them
+ *     is destroyed.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *     stream).  All device work of a call is enqueued on it.  Calls return once
+ *     the work is enqueued, except where stated.
+ *   - Every entry point returns an acg_status; 0 means success.  A failing
+ *     call leaves a message for acg_last_error() (thread-local).
+ *   - One host thread per plan at a time.
+ */
+#ifndef ACG_H
+#define ACG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum acg_status {
+  ACG_OK = 0,
+  ACG_ERR_INVALID_ARGUMENT = 1, /* null pointer, zero-sized pattern, bad option */
+  ACG_ERR_OUT_OF_MEMORY = 2,    /* a device or host allocation failed */
+  ACG_ERR_INDEX_OUT_OF_RANGE = 3, /* an edge endpoint >= num_nodes */
+  ACG_ERR_CUDA = 4,             /* a CUDA runtime call failed */
+  ACG_ERR_UNSUPPORTED = 5,      /* size or feature outside what is built */
+  ACG_ERR_IO = 6,               /* file missing, truncated or malformed */
+  ACG_ERR_DEVICE_TIMEOUT = 7    /* a bounded device-side wait gave up */
+} acg_status;
+
+/* Mirrors `struct Graph` (src/main.cu:8-19): u64 sizes, f64 row-major
+ * features, u64 edge endpoints.  Multi-edges and self-loops are allowed. */
+typedef struct acg_graph {
+  uint64_t num_nodes;
+  uint64_t node_feat_dim;
+  uint64_t num_edges;
+  uint64_t edge_feat_dim;
+  const double* node_feats;  /* [num_nodes][node_feat_dim] */
+  const double* edge_feats;  /* [num_edges][edge_feat_dim] */
+  const uint64_t* srcs;      /* [num_edges] */
+  const uint64_t* dsts;      /* [num_edges] */
+} acg_graph;
+
+/* Arithmetic used by a plan.
+ *  ACG_PREC_FP64  : every value and every operation in FP64, as the reference
+ *                   (helpers.hxx:3-4 `Real = double`).
+ *  ACG_PREC_MIXED : cost matrices on the tensor cores (BF16 hi/lo split, FP32
+ *                   accumulate, exact FP32 recompute of near pairs), belief
+ *                   propagation in FP32, column log-sum-exp normalisers
+ *                   accumulated in FP64. */
+typedef enum acg_precision {
+  ACG_PREC_FP64 = 0,
+  ACG_PREC_MIXED = 1
+} acg_precision;
+
+typedef struct acg_options {
+  int32_t precision;  /* acg_precision */
+  int32_t num_iters;  /* BP iterations; < 0 means pattern num_nodes, which is
+                         what the reference runs (main.cu:160) */
+  int32_t kernel_timing; /* nonzero: bracket every iteration-kernel launch with
+                            CUDA events (acg_stats.ms_iter_kernels) */
+  int32_t reserved[5];
+} acg_options;
+
+/* Fill `opt` with the defaults (FP64, num_iters = -1). */
+void acg_options_default(acg_options* opt);
+
+/* Opaque handles. */
+typedef struct acg_data acg_data; /* a data graph prepared for matching */
+typedef struct acg_plan acg_plan; /* one pattern against one acg_data */
+
+/* Timings and traffic of the last acg_match on a plan (filled by
+ * acg_plan_stats, which synchronises the plan's stream). */
+typedef struct acg_stats {
+  double ms_total;        /* cdist + init + iterations + output */
+  double ms_cdist;
+  double ms_init;
+  double ms_iters;
+  double bytes_iters;     /* algorithmic bytes of all iterations */
+  double bytes_per_edge_pass; /* algorithmic bytes of one iteration-kernel launch */
+  double ms_iter_kernels; /* summed duration of the iteration-kernel launches
+                             (only with acg_options.kernel_timing, else 0) */
+  int64_t launches;       /* kernels launched by the last acg_match */
+  int64_t num_iters;
+} acg_stats;
+
+/* ---------------- data graph ------------------------------------------- */
+/* Validate the data graph (every endpoint < num_nodes, else
+ * ACG_ERR_INDEX_OUT_OF_RANGE), build its two CSR orderings (edges sorted
+ * stably by destination and by source, int32 positions) and keep them for
+ * every plan made from it.  Replaces nothing in the reference, which scatters
+ * with atomics instead (ac.hxx:115-149, helpers.hxx:36-55).
+ * Synchronises `stream` (it reads back the validation result). */
+acg_status acg_data_create(const acg_graph* data, void* stream, acg_data** out);
+acg_status acg_data_destroy(acg_data* data);
+
+/* ---------------- plan / match ----------------------------------------- */
+/* Make a plan for matching `pattern` against `data`.  Allocates every device
+ * workspace the match needs (the reference allocates its 13 buffers in
+ * main.cu:80-99).  Pattern endpoints must be < pattern num_nodes.
+ * Synchronises `stream`. */
+acg_status acg_plan_create(acg_data* data, const acg_graph* pattern,
+                           const acg_options* opt, void* stream,
+                           acg_plan** out);
+acg_status acg_plan_destroy(acg_plan* plan);
+
+/* Run the whole match: cdist of vertex and edge features, the initial
+ * normalisers and edge maxima, `num_iters` BP iterations and the output in
+ * [data num_nodes][pattern num_nodes] row-major order -- the `MU` matrix the
+ * reference prints (main.cu:107-247).  `mu_out` is caller-owned device
+ * memory of num_nodes * pattern_nodes doubles. */
+acg_status acg_match(acg_plan* plan, double* mu_out, void* stream);
+
+/* Statistics of the last acg_match (synchronises the plan's stream). */
+acg_status acg_plan_stats(acg_plan* plan, acg_stats* out);
+
+/* One-shot convenience: data create + plan create + match + destroy.  The
+ * drop-in for the body of the reference's main() between loadGraph and the
+ * result copy (main.cu:77-247).  Synchronises `stream`. */
+acg_status acg_match_graphs(const acg_graph* data, const acg_graph* pattern,
+                            const acg_options* opt, double* mu_out,
+                            void* stream);
+
+/* ---------------- errors ----------------------------------------------- */
+const char* acg_status_string(acg_status s);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* acg_last_error(void);
+
+/* Library version string, e.g. "acg 0.1.0 sm_103a". */
+const char* acg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ACG_H */

@@ -1,0 +1,46 @@
+"""Size-independent properties at the benchmark sizes (GPU).
+
+At full size the oracle would take minutes, so these check what must hold for
+any input: every column of exp(mu) sums to one (mu is a column log-softmax over
+the data vertices, main.cu:241), the mixed path stays within 1e-4 of the FP64
+path with the same argmax, the planted pattern is recovered, and a repeated
+match is bit-identical.
+"""
+import numpy as np
+import pytest
+
+from application_classification_gb300 import graph, matcher
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def rmat18():
+    return graph.workload("rmat18")
+
+
+def _colsum_err(mu):
+    m = mu.max(0)
+    return np.abs(np.log(np.exp(mu - m).sum(0)) + m).max()
+
+
+def test_rmat18_fp64_vs_mixed(cuda, rmat18):
+    d, p, truth = rmat18
+    dg = matcher.DataGraph(d)
+    mu64 = matcher.Plan(dg, p, "fp64").run().cpu().numpy()
+    mu32 = matcher.Plan(dg, p, "mixed").run().cpu().numpy()
+    assert np.isfinite(mu64).all() and np.isfinite(mu32).all()
+    assert _colsum_err(mu64) < 1e-10
+    assert _colsum_err(mu32) < 1e-6
+    assert np.abs(mu32 - mu64).max() <= 1e-4
+    assert (mu32.argmax(1) == mu64.argmax(1)).mean() > 0.999999
+    # the planted vertices are the best match of each pattern vertex
+    assert all(int(mu64[:, i].argmax()) == int(truth[i]) for i in range(p.num_nodes))
+
+
+def test_rmat18_repeatable(cuda, rmat18):
+    d, p, _ = rmat18
+    pl = matcher.Plan(matcher.DataGraph(d), p, "mixed")
+    a = pl.run().cpu().numpy()
+    b = pl.run().cpu().numpy()
+    assert np.array_equal(a, b)
