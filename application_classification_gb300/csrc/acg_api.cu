@@ -18,6 +18,8 @@
 #include "acg_bp.cuh"
 #include "acg_device.cuh"
 #include "acg_internal.h"
+#include "acg_cdist.cuh"
+#include "acg_iter.cuh"
 
 using namespace acg;
 
@@ -30,19 +32,62 @@ struct acg_data {
   Csr scsr;                 // grouped by source; other = destination vertex
   int* pos_in_dst = nullptr;  // [De] dst-CSR row of each src-CSR position
   int num_sms = kNumSMs;
+  // FP32 copies of the features for the mixed path, built on first use:
+  // nodes [Dn][Kv], edges [De][ke32] in dst-CSR order.
+  float* nf32 = nullptr;
+  float* ef32 = nullptr;
+  int ke32 = 0;
   std::vector<DevBuf> owned;
 };
+
+namespace {
+acg_status ensure_f32(acg_data* D, cudaStream_t s) {
+  if (D->nf32) return ACG_OK;
+  D->ke32 = (D->Ke + 3) / 4 * 4;
+  float *nf = nullptr, *ef = nullptr;
+  ACG_TRY(dev_alloc(&D->owned, sizeof(float) * (size_t)D->Dn * std::max(1, D->Kv), (void**)&nf, s));
+  ACG_TRY(dev_alloc(&D->owned, sizeof(float) * (size_t)D->De * std::max(1, D->ke32), (void**)&ef, s));
+  ACG_TRY(launch_convert_rows(D->node_feats, nullptr, D->Dn, D->Kv, nf, D->Kv, s));
+  ACG_TRY(launch_convert_rows(D->edge_feats, D->dcsr.eid, D->De, D->Ke, ef, D->ke32, s));
+  D->nf32 = nf;
+  D->ef32 = ef;
+  return ACG_OK;
+}
+
+// cdist of the vertex and edge features, per precision.
+template <typename T>
+struct Cdist;
+template <>
+struct Cdist<double> {
+  static acg_status run(acg_plan* P, acg_data* D, long long lim, cudaStream_t s);
+};
+template <>
+struct Cdist<float> {
+  static acg_status run(acg_plan* P, acg_data* D, long long lim, cudaStream_t s);
+};
+}  // namespace
 
 struct acg_plan {
   acg_data* data = nullptr;
   int prec = ACG_PREC_FP64;
-  int Pn = 0, Pe = 0, Pp = 0, iters = 0;
+  int Pn = 0, Pe = 0, Pp = 0, Pnp = 0, iters = 0;
   const double* pv = nullptr;  // caller's pattern features (device)
   const double* pe = nullptr;
   int* pat = nullptr;          // pattern incidence (device)
-  Items ditems, sitems;
-  GroupShape gs{32, 1};
-  int iter_blocks = 1, row_blocks = 1, init_blocks = 1, cv_blocks = 1, ce_blocks = 1;
+  Items ditems, sitems;      // work items of the static row passes
+  GroupShape gs{32, 1};      // group shape of the row-pass and init kernels
+  int row_blocks = 1, init_blocks = 1, cv_blocks = 1, ce_blocks = 1;
+  // work of the edge phase: items (vertices with in-edges, chunks of heavy
+  // vertices) and the heavy vertices whose chunk maxima are combined
+  WarpShape ws{32, 1};
+  int4* witems = nullptr;
+  int nwitems = 0, wchunk = 0;
+  int edge_blocks = 1, vert_blocks = 1;
+  int* wsplit = nullptr;     // [edge warps + 1] item range of each edge-phase warp
+  int* th_base = nullptr;    // [nheavy] first partial row
+  int* th_count = nullptr;   // [nheavy] chunks
+  int* th_vert = nullptr;    // [nheavy] vertex
+  int th_n = 0, th_npartial = 0;
   // work buffers (element type per precision)
   void* dE = nullptr;
   void* vf = nullptr;
@@ -52,6 +97,7 @@ struct acg_plan {
   void* CV = nullptr;
   void* Rbuf = nullptr;
   void* Fbuf = nullptr;
+  void* M = nullptr;          // [Dn][Pp] edge-phase maxima
   void* part_iter = nullptr;
   void* part_row = nullptr;
   double* bpart = nullptr;
@@ -100,11 +146,12 @@ __global__ void compose_kernel(const int* __restrict__ seid, const int* __restri
 }
 
 __global__ void mu_from_cv_kernel(double* __restrict__ mu, const void* __restrict__ cv, int fp64,
-                                  const double* __restrict__ gv, long long n, int Pn) {
+                                  const double* __restrict__ gv, long long n, int Pn, int Pnp) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int p = (int)(i % Pn);
-  const double c = fp64 ? ((const double*)cv)[i] : (double)((const float*)cv)[i];
+  const long long ci = (i / Pn) * Pnp + p;
+  const double c = fp64 ? ((const double*)cv)[ci] : (double)((const float*)cv)[ci];
   // CV holds dV - LSE(dV); MU0 = -dV - LSE(-dV)
   mu[i] = -(c + gv[Pn + p]) - gv[2 * Pn + p];
 }
@@ -127,6 +174,88 @@ acg_status check_graph(const acg_graph* g, const char* what, bool need_feats) {
   return ACG_OK;
 }
 
+// Work items of the edge phase and their split over `nwarps` warps (host side,
+// from the dst-CSR offsets): every vertex with in-edges is an item; a vertex
+// whose in-edges would take a large share of one warp's work is split into
+// chunks whose maxima go to partial rows.  Item cost = load steps + overhead;
+// warp ranges are contiguous and of near-equal cost.
+acg_status build_edge_items(acg_plan* P, int nwarps, cudaStream_t s) {
+  acg_data* D = P->data;
+  const int n = D->Dn;
+  std::vector<int> off((size_t)n + 1);
+  ACG_CUDA_TRY(cudaMemcpyAsync(off.data(), D->dcsr.off, sizeof(int) * ((size_t)n + 1),
+                               cudaMemcpyDeviceToHost, s));
+  ACG_CUDA_TRY(cudaStreamSynchronize(s));
+  const int step = edge_step(P->ws);
+  const double kOver = 3.0;  // per-item cost in steps (item load, combine, store)
+  double total = 0;
+  for (int v = 0; v < n; ++v) {
+    const int deg = off[v + 1] - off[v];
+    if (deg) total += (deg + step - 1) / step + kOver;
+  }
+  const double per_warp = total / std::max(1, nwarps);
+  const long long cs = std::max(4LL, (long long)(per_warp / 4));  // chunk, in steps
+  const int chunk = (int)std::min<long long>(1LL << 24, cs * step);
+  P->wchunk = chunk;
+  std::vector<int4> items;
+  std::vector<double> cost;
+  std::vector<int> hb, hc, hv;
+  items.reserve((size_t)n / 2 + 16);
+  cost.reserve((size_t)n / 2 + 16);
+  int npart = 0;
+  for (int v = 0; v < n; ++v) {
+    const int deg = off[v + 1] - off[v];
+    if (deg == 0) continue;
+    if (deg > chunk) {
+      const int c = (deg + chunk - 1) / chunk;
+      hb.push_back(npart);
+      hc.push_back(c);
+      hv.push_back(v);
+      for (int j = 0; j < c; ++j) {
+        const int a = off[v] + j * chunk, b = std::min(off[v + 1], a + chunk);
+        items.push_back(make_int4(v, a, b, npart + j));
+        cost.push_back((b - a + step - 1) / step + kOver);
+      }
+      npart += c;
+    } else {
+      items.push_back(make_int4(v, off[v], off[v + 1], -1));
+      cost.push_back((deg + step - 1) / step + kOver);
+    }
+  }
+  std::vector<int> split((size_t)nwarps + 1, (int)items.size());
+  split[0] = 0;
+  {
+    double acc = 0, target = 0;
+    for (double c : cost) target += c;
+    target /= std::max(1, nwarps);
+    int w = 1;
+    for (size_t i = 0; i < items.size() && w < nwarps; ++i) {
+      acc += cost[i];
+      while (w < nwarps && acc >= target * w) split[w++] = (int)i + 1;
+    }
+  }
+  P->nwitems = (int)items.size();
+  P->th_n = (int)hv.size();
+  P->th_npartial = npart;
+  ACG_TRY(dev_alloc(&P->owned, sizeof(int4) * items.size(), (void**)&P->witems, s));
+  ACG_TRY(dev_alloc(&P->owned, sizeof(int) * split.size(), (void**)&P->wsplit, s));
+  ACG_TRY(dev_alloc(&P->owned, sizeof(int) * hv.size(), (void**)&P->th_base, s));
+  ACG_TRY(dev_alloc(&P->owned, sizeof(int) * hv.size(), (void**)&P->th_count, s));
+  ACG_TRY(dev_alloc(&P->owned, sizeof(int) * hv.size(), (void**)&P->th_vert, s));
+  if (!items.empty())
+    ACG_CUDA_TRY(cudaMemcpyAsync(P->witems, items.data(), sizeof(int4) * items.size(),
+                                 cudaMemcpyHostToDevice, s));
+  ACG_CUDA_TRY(cudaMemcpyAsync(P->wsplit, split.data(), sizeof(int) * split.size(),
+                               cudaMemcpyHostToDevice, s));
+  if (!hv.empty()) {
+    ACG_CUDA_TRY(cudaMemcpyAsync(P->th_base, hb.data(), sizeof(int) * hb.size(), cudaMemcpyHostToDevice, s));
+    ACG_CUDA_TRY(cudaMemcpyAsync(P->th_count, hc.data(), sizeof(int) * hc.size(), cudaMemcpyHostToDevice, s));
+    ACG_CUDA_TRY(cudaMemcpyAsync(P->th_vert, hv.data(), sizeof(int) * hv.size(), cudaMemcpyHostToDevice, s));
+  }
+  ACG_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die here
+  return ACG_OK;
+}
+
 template <typename T>
 acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
   acg_data* D = P->data;
@@ -136,21 +265,8 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
   P->launches = 0;
   cudaEventRecord(P->ev[0], s);
 
-  // ---- cdist, vertex side (ac.hxx:33-56 via main.cu:109) + column stats
-  {
-    CdistVArgs<T> a{D->node_feats, P->pv, (T*)P->CV, P->bpart, Dn, Pn, D->Kv};
-    ACG_TRY(launch_cdist_v<T>(a, P->cv_blocks, s));
-    ACG_TRY(launch_finalize(P->bpart, P->cv_blocks, StatSpec{Pn, 2 * Pn}, P->gv, s));
-    P->launches += 2;
-  }
-  // ---- cdist, edge side (main.cu:110), rows in dst-CSR order
-  {
-    CdistEArgs<T> a{D->edge_feats, D->dcsr.eid, P->pe, (T*)P->dE, P->bpart, De, Pe, Pp, D->Ke, lim};
-    // With no data edges the kernel writes empty partials (-inf, 0).
-    ACG_TRY(launch_cdist_e<T>(a, P->ce_blocks, s));
-    ACG_TRY(launch_finalize(P->bpart, P->ce_blocks, StatSpec{0, Pe}, P->ge, s));
-    P->launches += 2;
-  }
+  // ---- cdist (ac.hxx:33-56 via main.cu:109-110) + column stats
+  ACG_TRY(Cdist<T>::run(P, D, lim, s));
   cudaEventRecord(P->ev[1], s);
   // ---- static per-vertex reductions
   {
@@ -163,7 +279,8 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
     a.partial = (T*)P->part_row;
     a.hbase = P->sitems.hbase;
     a.hcount = P->sitems.hcount;
-    a.hcounter = P->sitems.hcounter;
+    a.hvert = P->sitems.hvert;
+    a.nheavy = P->sitems.nheavy;
     a.chunk = P->sitems.chunk;
     a.off = D->scsr.off;
     a.out_min = (T*)P->dEmin;
@@ -175,66 +292,55 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
     a.Pe = Pe;
     a.Pp = Pp;
     a.src_mode = 1;
-    ACG_TRY(launch_row_pass<T>(a, P->gs, P->row_blocks, s));
+    ACG_TRY(launch_row_pass<T>(a, P->gs, P->row_blocks, false, s));
+    ACG_TRY(launch_row_pass<T>(a, P->gs, P->row_blocks, true, s));
     a.items = P->ditems.items;
     a.nitems = P->ditems.nitems;
     a.row_of = nullptr;
     a.hbase = P->ditems.hbase;
     a.hcount = P->ditems.hcount;
-    a.hcounter = P->ditems.hcounter;
+    a.hvert = P->ditems.hvert;
+    a.nheavy = P->ditems.nheavy;
     a.chunk = P->ditems.chunk;
     a.off = D->dcsr.off;
     a.out_min = nullptr;
     a.out_lse = nullptr;
     a.out_buf = (T*)P->Fbuf;
     a.src_mode = 0;
-    ACG_TRY(launch_row_pass<T>(a, P->gs, P->row_blocks, s));
-    P->launches += 2;
+    ACG_TRY(launch_row_pass<T>(a, P->gs, P->row_blocks, false, s));
+    ACG_TRY(launch_row_pass<T>(a, P->gs, P->row_blocks, true, s));
+    P->launches += 2 + (P->sitems.nheavy > 0) + (P->ditems.nheavy > 0);
   }
   // ---- init vertex pass
   {
     InitArgs<T> a{D->dcsr.off, D->scsr.off, (T*)P->CV, (const T*)P->Rbuf, (const T*)P->Fbuf,
                   (const T*)P->B, (T*)P->vf, (T*)P->vr[0], P->gv, P->ge, P->bpart, P->pat,
-                  De, lim, Dn, Pn, Pe, Pp};
+                  De, lim, Dn, Pn, Pe, Pp, P->Pnp};
     ACG_TRY(launch_init_vertex<T>(a, P->gs, P->init_blocks, s));
     ACG_CUDA_TRY(cudaMemsetAsync(P->gi[0] + 4 * Pe, 0, sizeof(double) * Pn, s));
     ACG_TRY(launch_finalize(P->bpart, P->init_blocks, StatSpec{2 * Pe, 2 * Pe}, P->gi[0], s));
     P->launches += 2;
   }
   cudaEventRecord(P->ev[2], s);
-  // ---- BP iterations (main.cu:160-245)
+  // ---- BP iterations (main.cu:160-245): edge phase, heavy combine, vertex phase
   for (int t = 1; t <= P->iters; ++t) {
-    IterArgs<T> a{};
-    a.items = P->ditems.items;
-    a.nitems = P->ditems.nitems;
-    a.src_of = D->dcsr.other;
-    a.d_off = D->dcsr.off;
-    a.s_off = D->scsr.off;
-    a.dE = (const T*)P->dE;
-    a.vr_in = (const T*)P->vr[(t - 1) & 1];
-    a.vr_out = (T*)P->vr[t & 1];
-    a.vf = (T*)P->vf;
-    a.dEmin = (const T*)P->dEmin;
-    a.B = (const T*)P->B;
-    a.CV = (const T*)P->CV;
-    a.partial = (T*)P->part_iter;
-    a.hbase = P->ditems.hbase;
-    a.hcount = P->ditems.hcount;
-    a.hcounter = P->ditems.hcounter;
-    a.chunk = P->ditems.chunk;
-    a.glob_in = P->gi[(t - 1) & 1];
-    a.bpart = P->bpart;
-    a.mu_raw = mu_out;
-    a.pat = P->pat;
-    a.Dn = Dn;
-    a.Pn = Pn;
-    a.Pe = Pe;
-    a.Pp = Pp;
-    a.last = t == P->iters;
     if (P->kernel_timing) cudaEventRecord(P->kev[2 * (t - 1)], s);
-    ACG_TRY(launch_iter<T>(a, P->gs, P->iter_blocks, s));
+    if (Pe > 0) {
+      EdgeMaxArgs<T> ea{P->witems, P->nwitems, P->wsplit, D->dcsr.other,
+                        (const T*)P->dE, (const T*)P->vr[(t - 1) & 1], (T*)P->M,
+                        (T*)P->part_iter, Pp};
+      ACG_TRY(launch_edge_max<T>(ea, P->ws, P->edge_blocks, s));
+      ACG_TRY(launch_heavy_combine<T>((const T*)P->part_iter, P->th_base, P->th_count,
+                                      P->th_vert, P->th_n, Pp, (T*)P->M, s));
+      P->launches += 1 + (P->th_n > 0);
+    }
     if (P->kernel_timing) cudaEventRecord(P->kev[2 * (t - 1) + 1], s);
-    ACG_TRY(launch_finalize(P->bpart, P->iter_blocks, StatSpec{2 * Pe, 2 * Pe + Pn}, P->gi[t & 1], s));
+    VertexUpdArgs<T> va{D->dcsr.off, (const T*)P->M, (T*)P->vf, (T*)P->vr[t & 1],
+                        (const T*)P->dEmin, (const T*)P->B, (const T*)P->CV,
+                        P->gi[(t - 1) & 1], P->bpart, mu_out, P->pat,
+                        Dn, Pn, Pe, Pp, P->Pnp, t == P->iters};
+    ACG_TRY(launch_vertex_update<T>(va, P->vert_blocks, s));
+    ACG_TRY(launch_finalize(P->bpart, P->vert_blocks, StatSpec{2 * Pe, 2 * Pe + Pn}, P->gi[t & 1], s));
     P->launches += 2;
   }
   cudaEventRecord(P->ev[3], s);
@@ -244,13 +350,37 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
   } else {
     const long long n = (long long)Dn * Pn;
     if (n > 0) {
-      mu_from_cv_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(mu_out, P->CV, P->prec == ACG_PREC_FP64, P->gv, n, Pn);
+      mu_from_cv_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(mu_out, P->CV, P->prec == ACG_PREC_FP64, P->gv, n, Pn, P->Pnp);
       ACG_LAUNCH_CHECK();
     }
   }
   P->launches += 1;
   cudaEventRecord(P->ev[4], s);
   return ACG_OK;
+}
+
+template <typename T, typename F>
+acg_status run_cdist(acg_plan* P, acg_data* D, long long lim, const F* nf, int nfs, const F* ef,
+                     int efs, bool gather, cudaStream_t s) {
+  CdistRbArgs<T, F> av{nf, nullptr, nullptr, P->pv, (T*)P->CV, P->bpart, D->Dn, D->De, lim,
+                       D->Kv, nfs, P->Pn, P->Pnp, P->Pnp};
+  ACG_TRY(launch_cdist_rb(av, kCdistVertex, P->cv_blocks, s));
+  ACG_TRY(launch_finalize(P->bpart, P->cv_blocks, StatSpec{P->Pn, 2 * P->Pn}, P->gv, s));
+  // rows in dst-CSR order; with no data edges the kernel writes empty partials
+  CdistRbArgs<T, F> ae{ef, gather ? D->dcsr.eid : nullptr, D->dcsr.eid, P->pe, (T*)P->dE,
+                       P->bpart, D->De, D->De, lim, D->Ke, efs, P->Pe, P->Pp, P->Pp};
+  ACG_TRY(launch_cdist_rb(ae, kCdistEdge, P->ce_blocks, s));
+  ACG_TRY(launch_finalize(P->bpart, P->ce_blocks, StatSpec{0, P->Pe}, P->ge, s));
+  P->launches += 4;
+  return ACG_OK;
+}
+
+acg_status Cdist<double>::run(acg_plan* P, acg_data* D, long long lim, cudaStream_t s) {
+  return run_cdist<double, double>(P, D, lim, D->node_feats, D->Kv, D->edge_feats, D->Ke, true, s);
+}
+
+acg_status Cdist<float>::run(acg_plan* P, acg_data* D, long long lim, cudaStream_t s) {
+  return run_cdist<float, float>(P, D, lim, D->nf32, D->Kv, D->ef32, D->ke32, false, s);
 }
 
 }  // namespace
@@ -370,6 +500,7 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
   const int eb = elem_bytes(P->prec);
   const int W = 16 / eb;
   P->Pp = std::max(W, (P->Pe + W - 1) / W * W);
+  P->Pnp = (P->Pn + W - 1) / W * W;
   const int Pn = P->Pn, Pe = P->Pe, Pp = P->Pp, Dn = D->Dn, De = D->De;
 
   // pattern incidence (host build from the device endpoint arrays)
@@ -417,20 +548,30 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
   if (st != ACG_OK) return fail(st);
   ACG_CUDA_TRY(cudaMemcpyAsync(P->pat, pat.data(), sizeof(int) * pat.size(), cudaMemcpyHostToDevice, s));
 
+  if (P->prec == ACG_PREC_MIXED) st = ensure_f32(D, s);
+  if (st != ACG_OK) return fail(st);
   st = build_items(D->dcsr, kChunk, &P->ditems, &P->owned, s);
   if (st == ACG_OK) st = build_items(D->scsr, kChunk, &P->sitems, &P->owned, s);
   if (st != ACG_OK) return fail(st);
 
+  P->ws = choose_warp_shape(eb, Pp);
+  // edge phase: 6 blocks of 8 warps per SM (40 registers per thread)
+  P->edge_blocks = D->num_sms * 6;
+  st = build_edge_items(P.get(), P->edge_blocks * 8, s);
+  if (st != ACG_OK) return fail(st);
   P->gs = choose_shape(eb, Pp, Pn);
   const int GPB = 256 / P->gs.G;
-  const int occ = eb == 8 ? iter_max_blocks<double>(P->gs, Pn, Pe, Pp)
-                          : iter_max_blocks<float>(P->gs, Pn, Pe, Pp);
   const int nsm = D->num_sms;
-  P->iter_blocks = std::max(1, std::min(ceil_div(std::max(1, P->ditems.nitems), GPB), nsm * occ));
+  {
+    const int bps = eb == 8 ? vertex_update_blocks_per_sm<double>(Pn, Pe, Pp)
+                            : vertex_update_blocks_per_sm<float>(Pn, Pe, Pp);
+    const int V = 256 / (Pp / (16 / eb));
+    P->vert_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), V), nsm * bps));
+  }
   P->row_blocks = std::max(1, std::min(ceil_div(std::max(1, std::max(P->ditems.nitems, P->sitems.nitems)), GPB), nsm * 4));
   P->init_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), GPB), nsm * 4));
-  P->cv_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), 256 / Pn), nsm * 8));
-  P->ce_blocks = std::max(1, std::min(ceil_div(std::max(1, De), 256 / Pp), nsm * 8));
+  P->cv_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), 64), nsm * 2));
+  P->ce_blocks = std::max(1, std::min(ceil_div(std::max(1, De), 64), nsm * 2));
 
   const size_t vrow = (size_t)Dn * Pp * eb;
   alloc((size_t)De * Pp * eb, &P->dE);
@@ -441,10 +582,11 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
   alloc(vrow, &P->B);
   alloc(vrow, &P->Rbuf);
   alloc(vrow, &P->Fbuf);
-  alloc((size_t)Dn * Pn * eb, &P->CV);
-  alloc((size_t)std::max(1, P->ditems.npartial) * Pp * eb, &P->part_iter);
+  alloc((size_t)Dn * P->Pnp * eb, &P->CV);
+  alloc(vrow, &P->M);
+  alloc((size_t)std::max(1, P->th_npartial) * Pp * eb, &P->part_iter);
   alloc((size_t)std::max(1, std::max(P->ditems.npartial, P->sitems.npartial)) * 4 * Pp * eb, &P->part_row);
-  const size_t bp = std::max({(size_t)(6 * Pe + 2 * Pn) * P->iter_blocks,
+  const size_t bp = std::max({(size_t)(6 * Pe + 2 * Pn) * P->vert_blocks,
                               (size_t)5 * Pn * P->cv_blocks, (size_t)2 * Pe * P->ce_blocks,
                               (size_t)6 * Pe * P->init_blocks});
   alloc(sizeof(double) * bp, (void**)&P->bpart);

@@ -83,7 +83,9 @@ struct Carve {
     return r;
   }
 };
-inline size_t carve_bytes(size_t n, size_t elem) { return (n * elem + 15) & ~size_t(15); }
+__host__ __device__ inline size_t carve_bytes(size_t n, size_t elem) {
+  return (n * elem + 15) & ~size_t(15);
+}
 
 template <int G>
 struct Grp {
@@ -101,12 +103,6 @@ __device__ __forceinline__ double shfl_xor_d(double x, int o) {
   return __shfl_xor_sync(0xffffffffu, x, o);
 }
 
-__device__ __forceinline__ void lse_merge(double& m, double& s, double m2, double s2) {
-  LseD a{m, s};
-  a.merge(m2, s2);
-  m = a.m;
-  s = a.s;
-}
 
 // Combine, across the groups of a warp, values held by lanes with the same
 // in-group index.  G == 32 is a no-op.
@@ -126,23 +122,10 @@ __device__ __forceinline__ void warp_group_lse(double& m, double& s) {
 }
 
 // After every warp wrote its per-slot values to red[warp][slot], combine the
-// warps in order and write the block's partials [slot][block].
+// warps in order and write the block's partials [slot][ncols].
 __device__ void block_partials_out(const double* red, int nwarps, StatSpec spec,
-                                   double* bpart) {
-  const int slots = spec.slots();
-  for (int j = threadIdx.x; j < spec.nmax + spec.nlse; j += blockDim.x) {
-    if (j < spec.nmax) {
-      double m = -CUDART_INF;
-      for (int w = 0; w < nwarps; ++w) m = fmax(m, red[w * slots + j]);
-      bpart[(size_t)j * gridDim.x + blockIdx.x] = m;
-    } else {
-      const int sm = spec.nmax + 2 * (j - spec.nmax);
-      double m = -CUDART_INF, s = 0.0;
-      for (int w = 0; w < nwarps; ++w) lse_merge(m, s, red[w * slots + sm], red[w * slots + sm + 1]);
-      bpart[(size_t)sm * gridDim.x + blockIdx.x] = m;
-      bpart[(size_t)(sm + 1) * gridDim.x + blockIdx.x] = s;
-    }
-  }
+                                   double* bpart, int ncols, int col) {
+  write_block_partials(red, nwarps, spec.nmax, spec.nlse, bpart, ncols, col);
 }
 
 // ------------------------------------------------------------- finalize
@@ -193,282 +176,19 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kNPV = 4;  // pattern vertices per lane: Pn <= 4 * G
 
-template <typename T, int G, int NQV>
-__global__ void __launch_bounds__(kThreads)
-iter_kernel(const IterArgs<T> a) {
-  using VT = typename Vec<T>::type;
-  constexpr int W = Vec<T>::W;
-  constexpr int NQ = NQV * W;
-  constexpr int GPB = kThreads / G;
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int Pe = a.Pe, Pn = a.Pn, Pp = a.Pp;
-  Carve cv{smem};
-  int* s_pat = cv.take<int>(pattern_ints(Pn, Pe));
-  T* s_fillF = cv.take<T>(Pe);
-  T* s_fillR = cv.take<T>(Pe);
-  T* s_lF = cv.take<T>(Pe);
-  T* s_lFlo = cv.take<T>(Pe);
-  T* s_lR = cv.take<T>(Pe);
-  T* s_lRlo = cv.take<T>(Pe);
-  T* s_grp = cv.take<T>((size_t)GPB * (2 * Pp + Pn));
-  double* s_red = cv.take<double>((size_t)kWarps * (6 * Pe + 2 * Pn));
-  const int* s_psrc = s_pat;
-  const int* s_pdst = s_pat + Pe;
-  const int* s_inoff = s_pat + 2 * Pe;
-  const int* s_inq = s_inoff + Pn + 1;
-  const int* s_outoff = s_inq + Pe;
-  const int* s_outq = s_outoff + Pn + 1;
-
-  for (int t = threadIdx.x; t < pattern_ints(Pn, Pe); t += kThreads) s_pat[t] = a.pat[t];
-  __syncthreads();
-  {
-    const double* g = a.glob_in;  // mVF | mVR | lR | lF | S
-    for (int q = threadIdx.x; q < Pe; q += kThreads) {
-      const double cR = g[4 * Pe + s_psrc[q]], cF = g[4 * Pe + s_pdst[q]];
-      s_fillF[q] = (T)(g[Pe + q] - cR);
-      s_fillR[q] = (T)(g[q] - cF);
-      const double lr = g[2 * Pe + q], lf = g[3 * Pe + q];
-      s_lR[q] = (T)lr;
-      s_lRlo[q] = (T)(lr - (double)(T)lr);
-      s_lF[q] = (T)lf;
-      s_lFlo[q] = (T)(lf - (double)(T)lf);
-    }
-  }
-  __syncthreads();
-
-  const Grp<G> gr;
-  const int gib = threadIdx.x / G;
-  T* my_F = s_grp + (size_t)gib * (2 * Pp + Pn);
-  T* my_R = my_F + Pp;
-  T* my_MU = my_R + Pp;
-
-  T mxF[NQ], mxR[NQ];
-  OnlineLse<T> lr[NQ], lf[NQ], lmu[kNPV];
-#pragma unroll
-  for (int k = 0; k < NQ; ++k) {
-    mxF[k] = neg_inf<T>();
-    mxR[k] = neg_inf<T>();
-    lr[k].init();
-    lf[k].init();
-  }
-#pragma unroll
-  for (int j = 0; j < kNPV; ++j) lmu[j].init();
-
-  const int gstride = gridDim.x * GPB;
-  for (int it = blockIdx.x * GPB + gib; it < a.nitems; it += gstride) {
-    const int4 item = a.items[it];
-    const int v = item.x, i0 = item.y, i1 = item.z, h = item.w;
-
-    // ---- segmented max over in-edges: M'[q] = max_e VR'[s_e][q] - dE[e][q]
-    T acc[NQ];
-#pragma unroll
-    for (int k = 0; k < NQ; ++k) acc[k] = neg_inf<T>();
-    for (int base = i0; base < i1; base += G) {
-      const int nb = min(G, i1 - base);
-      const int my_s = gr.lig < nb ? __ldg(a.src_of + base + gr.lig) : 0;
-      int j = 0;
-      for (; j + 4 <= nb; j += 4) {
-        VT vr[4][NQV], de[4][NQV];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int s = __shfl_sync(gr.mask, my_s, j + u, G);
-          const VT* rv = reinterpret_cast<const VT*>(a.vr_in + (size_t)s * Pp);
-          const VT* re = reinterpret_cast<const VT*>(a.dE + (size_t)(base + j + u) * Pp);
-#pragma unroll
-          for (int k = 0; k < NQV; ++k) {
-            const int qv = gr.lig + G * k;
-            if (qv * W < Pp) {
-              vr[u][k] = __ldg(rv + qv);
-              de[u][k] = __ldcs(re + qv);
-            } else {
-              vr[u][k] = vzero<T>();
-              de[u][k] = vzero<T>();
-            }
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int k = 0; k < NQV; ++k)
-#pragma unroll
-            for (int w = 0; w < W; ++w)
-              acc[k * W + w] = fmax(acc[k * W + w], lane_of<T>(vr[u][k], w) - lane_of<T>(de[u][k], w));
-      }
-      for (; j < nb; ++j) {
-        const int s = __shfl_sync(gr.mask, my_s, j, G);
-        const VT* rv = reinterpret_cast<const VT*>(a.vr_in + (size_t)s * Pp);
-        const VT* re = reinterpret_cast<const VT*>(a.dE + (size_t)(base + j) * Pp);
-#pragma unroll
-        for (int k = 0; k < NQV; ++k) {
-          const int qv = gr.lig + G * k;
-          if (qv * W < Pp) {
-            VT x = __ldg(rv + qv), y = __ldcs(re + qv);
-#pragma unroll
-            for (int w = 0; w < W; ++w)
-              acc[k * W + w] = fmax(acc[k * W + w], lane_of<T>(x, w) - lane_of<T>(y, w));
-          }
-        }
-      }
-    }
-
-    // ---- heavy vertex: publish this chunk; the last chunk to arrive combines
-    if (h >= 0) {
-      const int c = (i0 - __ldg(a.d_off + v)) / a.chunk;
-      T* prow = a.partial + (size_t)(__ldg(a.hbase + h) + c) * Pp;
-#pragma unroll
-      for (int k = 0; k < NQV; ++k) {
-        const int qv = gr.lig + G * k;
-        if (qv * W < Pp) {
-          VT x;
-#pragma unroll
-          for (int w = 0; w < W; ++w) lane_of<T>(x, w) = acc[k * W + w];
-          reinterpret_cast<VT*>(prow)[qv] = x;
-        }
-      }
-      __threadfence();
-      __syncwarp(gr.mask);
-      unsigned old = 0;
-      if (gr.lig == 0) old = atomicAdd(a.hcounter + h, 1u);
-      old = __shfl_sync(gr.mask, old, 0, G);
-      const int cnt = __ldg(a.hcount + h);
-      if ((int)old != cnt - 1) continue;  // another chunk finishes this vertex
-      __threadfence();
-      const T* p0 = a.partial + (size_t)__ldg(a.hbase + h) * Pp;
-      for (int r = 0; r < cnt; ++r) {
-        const VT* pr = reinterpret_cast<const VT*>(p0 + (size_t)r * Pp);
-#pragma unroll
-        for (int k = 0; k < NQV; ++k) {
-          const int qv = gr.lig + G * k;
-          if (qv * W < Pp) {
-            VT x = __ldcg(pr + qv);
-#pragma unroll
-            for (int w = 0; w < W; ++w) acc[k * W + w] = fmax(acc[k * W + w], lane_of<T>(x, w));
-          }
-        }
-      }
-      if (gr.lig == 0) a.hcounter[h] = 0u;  // every chunk arrived: reset for the next launch
-    }
-
-    // ---- vertex epilogue: FMax, RMax, MU_raw, next VF', VR'
-    const int indeg = __ldg(a.d_off + v + 1) - __ldg(a.d_off + v);
-    const int outdeg = __ldg(a.s_off + v + 1) - __ldg(a.s_off + v);
-    const size_t vrow = (size_t)v * Pp;
-    VT bv[NQV];
-#pragma unroll
-    for (int k = 0; k < NQV; ++k) {
-      const int qv = gr.lig + G * k;
-      VT vfv = vzero<T>(), emv = vzero<T>();
-      bv[k] = vzero<T>();
-      if (qv * W < Pp) {
-        vfv = reinterpret_cast<const VT*>(a.vf + vrow)[qv];
-        emv = __ldg(reinterpret_cast<const VT*>(a.dEmin + vrow) + qv);
-        bv[k] = __ldg(reinterpret_cast<const VT*>(a.B + vrow) + qv);
-      }
-#pragma unroll
-      for (int w = 0; w < W; ++w) {
-        const int q = qv * W + w;
-        if (q < Pe) {
-          T F = s_fillF[q];
-          if (indeg > 0) F = fmax(F, (acc[k * W + w] - s_lF[q]) - s_lFlo[q]);
-          T R = s_fillR[q];
-          if (outdeg > 0)
-            R = fmax(R, ((lane_of<T>(vfv, w) - lane_of<T>(emv, w)) - s_lR[q]) - s_lRlo[q]);
-          my_F[q] = F;
-          my_R[q] = R;
-        }
-      }
-    }
-    __syncwarp(gr.mask);
-#pragma unroll
-    for (int j = 0; j < kNPV; ++j) {
-      const int p = gr.lig + G * j;
-      if (p < Pn) {
-        T mu = -__ldg(a.CV + (size_t)v * Pn + p);
-        for (int t = s_inoff[p]; t < s_inoff[p + 1]; ++t) mu += my_F[s_inq[t]];
-        for (int t = s_outoff[p]; t < s_outoff[p + 1]; ++t) mu += my_R[s_outq[t]];
-        my_MU[p] = mu;
-        lmu[j].add(mu);
-        if (a.last) a.mu_raw[(size_t)v * Pn + p] = (double)mu;
-      }
-    }
-    __syncwarp(gr.mask);
-    if (!a.last) {
-#pragma unroll
-      for (int k = 0; k < NQV; ++k) {
-        const int qv = gr.lig + G * k;
-        VT nf = vzero<T>(), nr = vzero<T>();
-#pragma unroll
-        for (int w = 0; w < W; ++w) {
-          const int q = qv * W + w;
-          if (q < Pe) {
-            const T f = my_MU[s_pdst[q]] - my_F[q];
-            const T r = my_MU[s_psrc[q]] - my_R[q];
-            lane_of<T>(nf, w) = f;
-            lane_of<T>(nr, w) = r;
-            mxF[k * W + w] = fmax(mxF[k * W + w], f);
-            mxR[k * W + w] = fmax(mxR[k * W + w], r);
-            const T b = lane_of<T>(bv[k], w);
-            lr[k * W + w].add(f + b);
-            lf[k * W + w].add(r + b);
-          }
-        }
-        if (qv * W < Pp) {
-          reinterpret_cast<VT*>(a.vf + vrow)[qv] = nf;
-          reinterpret_cast<VT*>(a.vr_out + vrow)[qv] = nr;
-        }
-      }
-    }
-    __syncwarp(gr.mask);
-  }
-
-  // ---- block partials: mVF, mVR (max), lR, lF, S (lse)
-  const StatSpec spec{2 * Pe, 2 * Pe + Pn};
-  const int slots = spec.slots();
-  double* red = s_red + (size_t)(threadIdx.x >> 5) * slots;
-#pragma unroll
-  for (int k = 0; k < NQV; ++k)
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      const int q = (gr.lig + G * k) * W + w;
-      const double f = warp_group_max<G>((double)mxF[k * W + w]);
-      const double r = warp_group_max<G>((double)mxR[k * W + w]);
-      double m1 = lr[k * W + w].mval(), s1 = lr[k * W + w].sval();
-      double m2 = lf[k * W + w].mval(), s2 = lf[k * W + w].sval();
-      warp_group_lse<G>(m1, s1);
-      warp_group_lse<G>(m2, s2);
-      if (gr.gw == 0 && q < Pe) {
-        red[q] = f;
-        red[Pe + q] = r;
-        red[spec.nmax + 2 * q] = m1;
-        red[spec.nmax + 2 * q + 1] = s1;
-        red[spec.nmax + 2 * (Pe + q)] = m2;
-        red[spec.nmax + 2 * (Pe + q) + 1] = s2;
-      }
-    }
-#pragma unroll
-  for (int j = 0; j < kNPV; ++j) {
-    const int p = gr.lig + G * j;
-    double m = lmu[j].mval(), s = lmu[j].sval();
-    warp_group_lse<G>(m, s);
-    if (gr.gw == 0 && p < Pn) {
-      red[spec.nmax + 2 * (2 * Pe + p)] = m;
-      red[spec.nmax + 2 * (2 * Pe + p) + 1] = s;
-    }
-  }
-  __syncthreads();
-  block_partials_out(s_red, kWarps, spec, a.bpart);
-}
-
 // ----------------------------------------------------------- cdist (SIMT)
-// Difference form sqrt(sum_k (x_k - y_k)^2), as ac.hxx:33-56, in T.
-template <typename T>
+// Difference form sqrt(sum_k (x_k - y_k)^2), as ac.hxx:33-56, computed in T
+// from features stored as F (the caller's FP64 arrays, or the data graph's
+// FP32 copy for the mixed path, so that no FP64->FP32 conversion -- which runs
+// at the FP64 rate on GB300 -- happens per pair).
+template <typename T, typename F>
 __global__ void __launch_bounds__(256)
-cdist_v_kernel(const CdistVArgs<T> a) {
+cdist_v_kernel(const CdistVArgs<T, F> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int Pn = a.Pn, Kv = a.Kv;
-  double* s_pv = reinterpret_cast<double*>(smem);
-  double* s_red = s_pv + ((Pn * Kv + 1) & ~1);
-  for (int t = threadIdx.x; t < Pn * Kv; t += blockDim.x) s_pv[t] = a.pv[t];
+  T* s_pv = reinterpret_cast<T*>(smem);
+  double* s_red = reinterpret_cast<double*>(smem + carve_bytes((size_t)Pn * Kv, sizeof(T)));
+  for (int t = threadIdx.x; t < Pn * Kv; t += blockDim.x) s_pv[t] = (T)a.pv[t];
   __syncthreads();
   const int R = 256 / Pn;  // vertices per block step
   const int p = threadIdx.x % Pn, rl = threadIdx.x / Pn;
@@ -478,15 +198,15 @@ cdist_v_kernel(const CdistVArgs<T> a) {
   ln.init();
   if (rl < R) {
     for (long long v = (long long)blockIdx.x * R + rl; v < a.Dn; v += (long long)gridDim.x * R) {
-      const double* x = a.dv + (size_t)v * Kv;
-      const double* y = s_pv + p * Kv;
+      const F* x = a.dv + (size_t)v * a.kstride;
+      const T* y = s_pv + p * Kv;
       T acc = T(0);
       for (int k = 0; k < Kv; ++k) {
-        const T d = (T)y[k] - (T)__ldg(x + k);
+        const T d = y[k] - (T)__ldg(x + k);
         acc += d * d;
       }
       const T dist = sqrt(acc);
-      a.dV[(size_t)v * Pn + p] = dist;
+      a.dV[(size_t)v * a.Pnp + p] = dist;
       const double dd = (double)dist;
       mx = fmax(mx, -dd);
       lp.add(dd);
@@ -494,8 +214,7 @@ cdist_v_kernel(const CdistVArgs<T> a) {
     }
   }
   // per-p block reduction over the R rows, in row order
-  const int slots = 5 * Pn;  // nmax = Pn, nlse = 2 Pn
-  double* red = s_red;       // [R][5]
+  double* red = s_red;  // [R][Pn][5]
   if (rl < R) {
     red[(rl * Pn + p) * 5 + 0] = mx;
     red[(rl * Pn + p) * 5 + 1] = lp.m;
@@ -504,7 +223,6 @@ cdist_v_kernel(const CdistVArgs<T> a) {
     red[(rl * Pn + p) * 5 + 4] = ln.s;
   }
   __syncthreads();
-  (void)slots;
   for (int pp = threadIdx.x; pp < Pn; pp += blockDim.x) {
     double m = -CUDART_INF, am = -CUDART_INF, as = 0.0, bm = -CUDART_INF, bs = 0.0;
     for (int r = 0; r < R; ++r) {
@@ -522,14 +240,14 @@ cdist_v_kernel(const CdistVArgs<T> a) {
   }
 }
 
-template <typename T>
+template <typename T, typename F>
 __global__ void __launch_bounds__(256)
-cdist_e_kernel(const CdistEArgs<T> a) {
+cdist_e_kernel(const CdistEArgs<T, F> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int Pe = a.Pe, Pp = a.Pp, Ke = a.Ke;
-  double* s_pe = reinterpret_cast<double*>(smem);
-  double* s_red = s_pe + ((Pe * Ke + 1) & ~1);
-  for (int t = threadIdx.x; t < Pe * Ke; t += blockDim.x) s_pe[t] = a.pe[t];
+  T* s_pe = reinterpret_cast<T*>(smem);
+  double* s_red = reinterpret_cast<double*>(smem + carve_bytes((size_t)Pe * Ke, sizeof(T)));
+  for (int t = threadIdx.x; t < Pe * Ke; t += blockDim.x) s_pe[t] = (T)a.pe[t];
   __syncthreads();
   const int R = 256 / Pp;
   const int q = threadIdx.x % Pp, rl = threadIdx.x / Pp;
@@ -541,11 +259,11 @@ cdist_e_kernel(const CdistEArgs<T> a) {
       T dist = T(0);
       if (q < Pe) {
         const int e = __ldg(a.eid + i);
-        const double* x = a.ef + (size_t)e * Ke;
-        const double* y = s_pe + q * Ke;
+        const F* x = a.ef + (size_t)(a.gather ? e : i) * a.kstride;
+        const T* y = s_pe + q * Ke;
         T acc = T(0);
         for (int k = 0; k < Ke; ++k) {
-          const T d = (T)y[k] - (T)__ldg(x + k);
+          const T d = y[k] - (T)__ldg(x + k);
           acc += d * d;
         }
         dist = sqrt(acc);
@@ -568,87 +286,49 @@ cdist_e_kernel(const CdistEArgs<T> a) {
   }
 }
 
+// dst[i][k] = (float)src[row ? row[i] : i][k], zero padding to kstride.
+__global__ void convert_rows_kernel(const double* __restrict__ src, const int* __restrict__ row,
+                                    long long n, int K, float* __restrict__ dst, int kstride) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * kstride) return;
+  const long long i = t / kstride;
+  const int k = (int)(t % kstride);
+  float x = 0.f;
+  if (k < K) x = __double2float_rn(src[(size_t)(row ? row[i] : i) * K + k]);
+  dst[t] = x;
+}
+
 // ------------------------------------------------------ static row passes
-template <typename T, int G, int NQV>
+// HEAVY = false: every work item; a chunk of a heavy vertex writes its partial
+// (min, lse m, lse s, quirk max) rows and stops.  HEAVY = true: one group per
+// heavy vertex combines its partial rows in chunk order and writes the outputs.
+template <typename T, int G, int NQV, bool HEAVY>
 __global__ void __launch_bounds__(kThreads)
 row_pass_kernel(const RowPassArgs<T> a) {
   using VT = typename Vec<T>::type;
   constexpr int W = Vec<T>::W;
   constexpr int NQ = NQV * W;
   constexpr int GPB = kThreads / G;
-  const int Pe = a.Pe, Pp = a.Pp;
+  const int Pp = a.Pp;
   const Grp<G> gr;
   const int gib = threadIdx.x / G;
   const int gstride = gridDim.x * GPB;
-  for (int it = blockIdx.x * GPB + gib; it < a.nitems; it += gstride) {
-    const int4 item = a.items[it];
-    const int v = item.x, i0 = item.y, i1 = item.z, h = item.w;
+  const int nwork = HEAVY ? a.nheavy : a.nitems;
+  for (int it = blockIdx.x * GPB + gib; it < nwork; it += gstride) {
     T mn[NQ], bx[NQ];
-    OnlineLse<T> ls[NQ];
+    double lm[NQ], lsum[NQ];
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
       mn[k] = pos_inf<T>();
       bx[k] = neg_inf<T>();
-      ls[k].init();
+      lm[k] = -CUDART_INF;
+      lsum[k] = 0.0;
     }
-    for (int j = i0; j < i1; ++j) {
-      const int r = a.src_mode ? __ldg(a.row_of + j) : j;
-      const long long e = __ldg(a.eid_of_row + r);
-      const VT* row = reinterpret_cast<const VT*>(a.dE + (size_t)r * Pp);
-#pragma unroll
-      for (int k = 0; k < NQV; ++k) {
-        const int qv = gr.lig + G * k;
-        if (qv * W < Pp) {
-          const VT x = __ldg(row + qv);
-#pragma unroll
-          for (int w = 0; w < W; ++w) {
-            const int q = qv * W + w;
-            const T d = lane_of<T>(x, w);
-            const T buf = ((long long)q * a.De + e < a.lim) ? -d : T(0);
-            bx[k * W + w] = fmax(bx[k * W + w], buf);
-            if (a.src_mode) {
-              mn[k * W + w] = fmin(mn[k * W + w], d);
-              ls[k * W + w].add(-d);
-            }
-          }
-        }
-      }
-    }
-    if (h >= 0) {
-      const int c = (i0 - __ldg(a.off + v)) / a.chunk;
-      T* prow = a.partial + (size_t)(__ldg(a.hbase + h) + c) * 4 * Pp;
-#pragma unroll
-      for (int k = 0; k < NQV; ++k)
-#pragma unroll
-        for (int w = 0; w < W; ++w) {
-          const int q = (gr.lig + G * k) * W + w;
-          if (q < Pp) {
-            prow[q] = mn[k * W + w];
-            prow[Pp + q] = (T)ls[k * W + w].mval();
-            prow[2 * Pp + q] = (T)ls[k * W + w].sval();
-            prow[3 * Pp + q] = bx[k * W + w];
-          }
-        }
-      __threadfence();
-      __syncwarp(gr.mask);
-      unsigned old = 0;
-      if (gr.lig == 0) old = atomicAdd(a.hcounter + h, 1u);
-      old = __shfl_sync(gr.mask, old, 0, G);
-      const int cnt = __ldg(a.hcount + h);
-      if ((int)old != cnt - 1) continue;
-      __threadfence();
-      const T* p0 = a.partial + (size_t)__ldg(a.hbase + h) * 4 * Pp;
-#pragma unroll
-      for (int k = 0; k < NQ; ++k) {
-        mn[k] = pos_inf<T>();
-        bx[k] = neg_inf<T>();
-      }
-      double lm[NQ], lsum[NQ];
-#pragma unroll
-      for (int k = 0; k < NQ; ++k) {
-        lm[k] = -CUDART_INF;
-        lsum[k] = 0.0;
-      }
+    int v;
+    if constexpr (HEAVY) {
+      v = __ldg(a.hvert + it);
+      const T* p0 = a.partial + (size_t)__ldg(a.hbase + it) * 4 * Pp;
+      const int cnt = __ldg(a.hcount + it);
       for (int r = 0; r < cnt; ++r) {
         const T* pr = p0 + (size_t)r * 4 * Pp;
 #pragma unroll
@@ -664,12 +344,57 @@ row_pass_kernel(const RowPassArgs<T> a) {
             }
           }
       }
-      if (gr.lig == 0) a.hcounter[h] = 0u;
+    } else {
+      const int4 item = a.items[it];
+      v = item.x;
+      const int i0 = item.y, i1 = item.z, h = item.w;
+      OnlineLse<T> ls[NQ];
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) ls[k].init();
+      for (int j = i0; j < i1; ++j) {
+        const int r = a.src_mode ? __ldg(a.row_of + j) : j;
+        const long long e = __ldg(a.eid_of_row + r);
+        const VT* row = reinterpret_cast<const VT*>(a.dE + (size_t)r * Pp);
+#pragma unroll
+        for (int k = 0; k < NQV; ++k) {
+          const int qv = gr.lig + G * k;
+          if (qv * W < Pp) {
+            const VT x = __ldg(row + qv);
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+              const int q = qv * W + w;
+              const T d = lane_of<T>(x, w);
+              const T buf = ((long long)q * a.De + e < a.lim) ? -d : T(0);
+              bx[k * W + w] = fmax(bx[k * W + w], buf);
+              if (a.src_mode) {
+                mn[k * W + w] = fmin(mn[k * W + w], d);
+                ls[k * W + w].add(-d);
+              }
+            }
+          }
+        }
+      }
 #pragma unroll
       for (int k = 0; k < NQ; ++k) {
-        ls[k].init();
-        ls[k].m = (T)lm[k];
-        ls[k].s = (T)lsum[k];
+        lm[k] = ls[k].mval();
+        lsum[k] = ls[k].sval();
+      }
+      if (h >= 0) {
+        const int c = (i0 - __ldg(a.off + v)) / a.chunk;
+        T* prow = a.partial + (size_t)(__ldg(a.hbase + h) + c) * 4 * Pp;
+#pragma unroll
+        for (int k = 0; k < NQV; ++k)
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            const int q = (gr.lig + G * k) * W + w;
+            if (q < Pp) {
+              prow[q] = mn[k * W + w];
+              prow[Pp + q] = (T)lm[k * W + w];
+              prow[2 * Pp + q] = (T)lsum[k * W + w];
+              prow[3 * Pp + q] = bx[k * W + w];
+            }
+          }
+        continue;
       }
     }
     const size_t vrow = (size_t)v * Pp;
@@ -682,7 +407,7 @@ row_pass_kernel(const RowPassArgs<T> a) {
           a.out_buf[vrow + q] = bx[k * W + w];
           if (a.src_mode) {
             a.out_min[vrow + q] = mn[k * W + w];
-            const double m = ls[k * W + w].mval(), s = ls[k * W + w].sval();
+            const double m = lm[k * W + w], s = lsum[k * W + w];
             a.out_lse[vrow + q] = (m > -CUDART_INF && s > 0.0) ? (T)(m + log(s)) : neg_inf<T>();
           }
         }
@@ -748,8 +473,8 @@ init_vertex_kernel(const InitArgs<T> a) {
   const int gstride = gridDim.x * GPB;
   for (int v = blockIdx.x * GPB + gib; v < a.Dn; v += gstride) {
     for (int p = gr.lig; p < Pn; p += G) {
-      const double dv = (double)a.CV[(size_t)v * Pn + p];
-      a.CV[(size_t)v * Pn + p] = (T)(dv - s_lse1[p]);
+      const double dv = (double)a.CV[(size_t)v * a.Pnp + p];
+      a.CV[(size_t)v * a.Pnp + p] = (T)(dv - s_lse1[p]);
       my_MU[p] = (T)(-dv - s_lse2[p]);
     }
     __syncwarp(gr.mask);
@@ -805,21 +530,13 @@ init_vertex_kernel(const InitArgs<T> a) {
       }
     }
   __syncthreads();
-  block_partials_out(s_red, kWarps, spec, a.bpart);
+  block_partials_out(s_red, kWarps, spec, a.bpart, gridDim.x, blockIdx.x);
 }
 
 __global__ void mu_output_kernel(double* __restrict__ mu, const double* __restrict__ S,
                                  long long n, int Pn) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) mu[i] -= S[i % Pn];
-}
-
-template <typename T>
-size_t iter_smem(GroupShape gs, int pn, int pe, int pp) {
-  const int GPB = kThreads / gs.G;
-  return carve_bytes(pattern_ints(pn, pe), sizeof(int)) + 6 * carve_bytes(pe, sizeof(T)) +
-         carve_bytes((size_t)GPB * (2 * pp + pn), sizeof(T)) +
-         carve_bytes((size_t)kWarps * (6 * pe + 2 * pn), sizeof(double));
 }
 
 template <typename T>
@@ -855,57 +572,20 @@ GroupShape choose_shape(int elem_bytes, int pp, int pn) {
   return gs;
 }
 
-template <typename T>
-size_t iter_smem_bytes(GroupShape gs, int pn, int pe, int pp) {
-  return iter_smem<T>(gs, pn, pe, pp);
-}
-
-#define ACG_ITER_CASE(G_, N_)                                                           \
-  if (gs.G == G_ && gs.NQV == N_) {                                                     \
-    const size_t sm = iter_smem<T>(gs, a.Pn, a.Pe, a.Pp);                               \
-    if (sm > 48 * 1024)                                                                 \
-      cudaFuncSetAttribute(iter_kernel<T, G_, N_>,                                      \
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);       \
-    iter_kernel<T, G_, N_><<<blocks, kThreads, sm, s>>>(a);                             \
-    ACG_LAUNCH_CHECK();                                                                 \
-    return ACG_OK;                                                                      \
-  }
-
-template <typename T>
-acg_status launch_iter(const IterArgs<T>& a, GroupShape gs, int blocks, cudaStream_t s) {
-  ACG_SHAPES(ACG_ITER_CASE)
-  return set_error(ACG_ERR_UNSUPPORTED, "no iteration kernel for G=%d NQV=%d", gs.G, gs.NQV);
-}
-
-#define ACG_OCC_CASE(G_, N_)                                                            \
-  if (gs.G == G_ && gs.NQV == N_) {                                                     \
-    int nb = 0;                                                                         \
-    const size_t sm = iter_smem<T>(gs, pn, pe, pp);                                     \
-    if (sm > 48 * 1024)                                                                 \
-      cudaFuncSetAttribute(iter_kernel<T, G_, N_>,                                      \
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);       \
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, iter_kernel<T, G_, N_>,      \
-                                                      kThreads, sm) != cudaSuccess)     \
-      nb = 1;                                                                           \
-    return (nb < 1 ? 1 : nb);                                                           \
-  }
-
-template <typename T>
-int iter_max_blocks(GroupShape gs, int pn, int pe, int pp) {
-  ACG_SHAPES(ACG_OCC_CASE)
-  return 1;
-}
-
 #define ACG_ROW_CASE(G_, N_)                                                            \
   if (gs.G == G_ && gs.NQV == N_) {                                                     \
-    row_pass_kernel<T, G_, N_><<<blocks, kThreads, 0, s>>>(a);                          \
+    if (heavy)                                                                          \
+      row_pass_kernel<T, G_, N_, true><<<blocks, kThreads, 0, s>>>(a);                  \
+    else                                                                                \
+      row_pass_kernel<T, G_, N_, false><<<blocks, kThreads, 0, s>>>(a);                 \
     ACG_LAUNCH_CHECK();                                                                 \
     return ACG_OK;                                                                      \
   }
 
 template <typename T>
-acg_status launch_row_pass(const RowPassArgs<T>& a, GroupShape gs, int blocks, cudaStream_t s) {
-  if (a.nitems == 0) return ACG_OK;
+acg_status launch_row_pass(const RowPassArgs<T>& a, GroupShape gs, int blocks, bool heavy,
+                           cudaStream_t s) {
+  if ((heavy ? a.nheavy : a.nitems) == 0) return ACG_OK;
   ACG_SHAPES(ACG_ROW_CASE)
   return set_error(ACG_ERR_UNSUPPORTED, "no row-pass kernel for G=%d NQV=%d", gs.G, gs.NQV);
 }
@@ -936,26 +616,33 @@ acg_status launch_finalize(const double* bpart, int nblocks, StatSpec spec, doub
   return ACG_OK;
 }
 
-template <typename T>
-acg_status launch_cdist_v(const CdistVArgs<T>& a, int blocks, cudaStream_t s) {
+template <typename T, typename F>
+acg_status launch_cdist_v(const CdistVArgs<T, F>& a, int blocks, cudaStream_t s) {
   const int R = 256 / a.Pn;
-  const size_t sm = sizeof(double) * (((size_t)a.Pn * a.Kv + 1) & ~size_t(1)) +
-                    sizeof(double) * (size_t)R * a.Pn * 5;
+  const size_t sm = carve_bytes((size_t)a.Pn * a.Kv, sizeof(T)) + sizeof(double) * (size_t)R * a.Pn * 5;
   if (sm > 48 * 1024)
-    cudaFuncSetAttribute(cdist_v_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  cdist_v_kernel<T><<<blocks, 256, sm, s>>>(a);
+    cudaFuncSetAttribute(cdist_v_kernel<T, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cdist_v_kernel<T, F><<<blocks, 256, sm, s>>>(a);
   ACG_LAUNCH_CHECK();
   return ACG_OK;
 }
 
-template <typename T>
-acg_status launch_cdist_e(const CdistEArgs<T>& a, int blocks, cudaStream_t s) {
+template <typename T, typename F>
+acg_status launch_cdist_e(const CdistEArgs<T, F>& a, int blocks, cudaStream_t s) {
   const int R = 256 / a.Pp;
-  const size_t sm = sizeof(double) * (((size_t)a.Pe * a.Ke + 1) & ~size_t(1)) +
-                    sizeof(double) * (size_t)R * a.Pp * 2;
+  const size_t sm = carve_bytes((size_t)a.Pe * a.Ke, sizeof(T)) + sizeof(double) * (size_t)R * a.Pp * 2;
   if (sm > 48 * 1024)
-    cudaFuncSetAttribute(cdist_e_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  cdist_e_kernel<T><<<blocks, 256, sm, s>>>(a);
+    cudaFuncSetAttribute(cdist_e_kernel<T, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cdist_e_kernel<T, F><<<blocks, 256, sm, s>>>(a);
+  ACG_LAUNCH_CHECK();
+  return ACG_OK;
+}
+
+acg_status launch_convert_rows(const double* src, const int* row, long long n, int K, float* dst,
+                               int kstride, cudaStream_t s) {
+  const long long tot = n * kstride;
+  if (tot == 0) return ACG_OK;
+  convert_rows_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(src, row, n, K, dst, kstride);
   ACG_LAUNCH_CHECK();
   return ACG_OK;
 }
@@ -968,19 +655,13 @@ acg_status launch_mu_output(double* mu, const double* S, long long Dn, int Pn, c
   return ACG_OK;
 }
 
-template acg_status launch_iter<double>(const IterArgs<double>&, GroupShape, int, cudaStream_t);
-template acg_status launch_iter<float>(const IterArgs<float>&, GroupShape, int, cudaStream_t);
-template int iter_max_blocks<double>(GroupShape, int, int, int);
-template int iter_max_blocks<float>(GroupShape, int, int, int);
-template size_t iter_smem_bytes<double>(GroupShape, int, int, int);
-template size_t iter_smem_bytes<float>(GroupShape, int, int, int);
-template acg_status launch_row_pass<double>(const RowPassArgs<double>&, GroupShape, int, cudaStream_t);
-template acg_status launch_row_pass<float>(const RowPassArgs<float>&, GroupShape, int, cudaStream_t);
+template acg_status launch_row_pass<double>(const RowPassArgs<double>&, GroupShape, int, bool, cudaStream_t);
+template acg_status launch_row_pass<float>(const RowPassArgs<float>&, GroupShape, int, bool, cudaStream_t);
 template acg_status launch_init_vertex<double>(const InitArgs<double>&, GroupShape, int, cudaStream_t);
 template acg_status launch_init_vertex<float>(const InitArgs<float>&, GroupShape, int, cudaStream_t);
-template acg_status launch_cdist_v<double>(const CdistVArgs<double>&, int, cudaStream_t);
-template acg_status launch_cdist_v<float>(const CdistVArgs<float>&, int, cudaStream_t);
-template acg_status launch_cdist_e<double>(const CdistEArgs<double>&, int, cudaStream_t);
-template acg_status launch_cdist_e<float>(const CdistEArgs<float>&, int, cudaStream_t);
+template acg_status launch_cdist_v<double, double>(const CdistVArgs<double, double>&, int, cudaStream_t);
+template acg_status launch_cdist_v<float, float>(const CdistVArgs<float, float>&, int, cudaStream_t);
+template acg_status launch_cdist_e<double, double>(const CdistEArgs<double, double>&, int, cudaStream_t);
+template acg_status launch_cdist_e<float, float>(const CdistEArgs<float, float>&, int, cudaStream_t);
 
 }  // namespace acg

@@ -25,34 +25,6 @@ struct StatSpec {
   __host__ __device__ int outs() const { return nmax + nlse; }
 };
 
-// Arguments of one BP iteration (the fused edge + vertex pass).
-template <typename T>
-struct IterArgs {
-  const int4* items;
-  int nitems;
-  const int* src_of;    // [De] source vertex at each dst-CSR position
-  const int* d_off;     // [Dn+1] dst-CSR offsets
-  const int* s_off;     // [Dn+1] src-CSR offsets
-  const T* dE;          // [De][Pp] distances in dst-CSR order
-  const T* vr_in;       // [Dn][Pp] unshifted VR of the previous iteration
-  T* vr_out;            // [Dn][Pp] unshifted VR of this iteration
-  T* vf;                // [Dn][Pp] unshifted VF (read, then overwritten)
-  const T* dEmin;       // [Dn][Pp] min over out-edges of dE (static)
-  const T* B;           // [Dn][Pp] log sum over out-edges of exp(-dE) (static)
-  const T* CV;          // [Dn][Pn] normalised vertex cost
-  T* partial;           // [npartial][Pp] chunk maxima of heavy vertices
-  const int* hbase;
-  const int* hcount;
-  unsigned* hcounter;
-  int chunk;
-  const double* glob_in;  // [mVF|mVR|lR|lF|S] of the previous iteration
-  double* bpart;          // block partials of this iteration
-  double* mu_raw;         // [Dn][Pn] unnormalised mu (last iteration only)
-  const int* pat;         // pattern incidence
-  int Dn, Pn, Pe, Pp;
-  int last;
-};
-
 // Launch configuration chosen per (value type, Pp, Pn).
 struct GroupShape {
   int G;    // lanes per vertex
@@ -60,41 +32,41 @@ struct GroupShape {
 };
 GroupShape choose_shape(int elem_bytes, int pp, int pn);
 
-template <typename T>
-acg_status launch_iter(const IterArgs<T>& a, GroupShape gs, int blocks, cudaStream_t s);
-template <typename T>
-int iter_max_blocks(GroupShape gs, int pn, int pe, int pp);
-template <typename T>
-size_t iter_smem_bytes(GroupShape gs, int pn, int pe, int pp);
-
 acg_status launch_finalize(const double* bpart, int nblocks, StatSpec spec, double* out,
                            cudaStream_t s);
 
 // ---- initialisation kernels
-template <typename T>
+// F: element type of the stored features (double: the caller's arrays;
+// float: the data graph's FP32 copy used by the mixed path).
+template <typename T, typename F>
 struct CdistVArgs {
-  const double* dv;  // [Dn][Kv]
+  const F* dv;       // [Dn][kstride]
   const double* pv;  // [Pn][Kv]
-  T* dV;             // [Dn][Pn] raw distances (normalised in place by init_vertex)
+  T* dV;             // [Dn][Pnp] raw distances (normalised in place by init_vertex)
   double* bpart;     // stats: max(-dV) (Pn), LSE(dV) (Pn), LSE(-dV) (Pn)
-  int Dn, Pn, Kv;
+  int Dn, Pn, Kv, kstride, Pnp;
 };
-template <typename T>
-acg_status launch_cdist_v(const CdistVArgs<T>& a, int blocks, cudaStream_t s);
+template <typename T, typename F>
+acg_status launch_cdist_v(const CdistVArgs<T, F>& a, int blocks, cudaStream_t s);
 
-template <typename T>
+template <typename T, typename F>
 struct CdistEArgs {
-  const double* ef;   // [De][Ke] original edge order
+  const F* ef;        // features: gather ? [De][kstride] original order : dst-CSR order
   const int* eid;     // [De] original edge id at each dst-CSR position
   const double* pe;   // [Pe][Ke]
   T* dE;              // [De][Pp] out, dst-CSR order
   double* bpart;      // stats: LSE over covered elements of -dE (Pe)
   long long De;
-  int Pe, Pp, Ke;
+  int Pe, Pp, Ke, kstride;
+  int gather;         // 1: row = eid[i]; 0: row = i
   long long lim;      // Pn * Dn: flat positions below it hold -dE in the quirk buffer
 };
-template <typename T>
-acg_status launch_cdist_e(const CdistEArgs<T>& a, int blocks, cudaStream_t s);
+template <typename T, typename F>
+acg_status launch_cdist_e(const CdistEArgs<T, F>& a, int blocks, cudaStream_t s);
+
+// dst[i][k] = (float)src[row ? row[i] : i][k] for k < K, zero up to kstride.
+acg_status launch_convert_rows(const double* src, const int* row, long long n, int K, float* dst,
+                               int kstride, cudaStream_t s);
 
 // Static per-vertex reductions over a CSR of dE rows.
 //   src mode: dEmin, B = LSE(-dE), Rbuf = max of the quirk buffer, over out-edges
@@ -109,7 +81,8 @@ struct RowPassArgs {
   T* partial;         // [npartial][4][Pp]
   const int* hbase;
   const int* hcount;
-  unsigned* hcounter;
+  const int* hvert;
+  int nheavy;
   int chunk;
   const int* off;     // CSR offsets (for chunk index)
   T* out_min;         // src: dEmin
@@ -121,13 +94,14 @@ struct RowPassArgs {
   int src_mode;
 };
 template <typename T>
-acg_status launch_row_pass(const RowPassArgs<T>& a, GroupShape gs, int blocks, cudaStream_t s);
+acg_status launch_row_pass(const RowPassArgs<T>& a, GroupShape gs, int blocks, bool heavy,
+                           cudaStream_t s);
 
 template <typename T>
 struct InitArgs {
   const int* d_off;
   const int* s_off;
-  T* CV;               // [Dn][Pn]: raw dV in, normalised cost out
+  T* CV;               // [Dn][Pnp]: raw dV in, normalised cost out
   const T* Rbuf;       // [Dn][Pp]
   const T* Fbuf;       // [Dn][Pp]
   const T* B;          // [Dn][Pp]
@@ -139,7 +113,7 @@ struct InitArgs {
   const int* pat;
   long long De;
   long long lim;
-  int Dn, Pn, Pe, Pp;
+  int Dn, Pn, Pe, Pp, Pnp;
 };
 template <typename T>
 acg_status launch_init_vertex(const InitArgs<T>& a, GroupShape gs, int blocks, cudaStream_t s);

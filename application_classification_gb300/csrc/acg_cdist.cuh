@@ -1,0 +1,32 @@
+// acg_cdist.cuh -- register-blocked SIMT cost matrices (acg_cdist.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "acg_internal.h"
+
+namespace acg {
+
+constexpr int kCdistEdge = 0;    // stats: LSE of -d over the covered quirk elements
+constexpr int kCdistVertex = 1;  // stats: max(-d), LSE(d), LSE(-d)
+
+// out[r][q] = || x[row(r)] - y[q] || for r < nrows, q < P; out[r][q] = 0 for
+// P <= q < Pp.  row(r) = row ? row[r] : r.
+template <typename T, typename F>
+struct CdistRbArgs {
+  const F* x;          // data features, row stride kstride
+  const int* row;      // optional row index per output row
+  const int* eid;      // edge mode: original edge id per output row (quirk test)
+  const double* y;     // [P][K] pattern features
+  T* out;              // [nrows][ostride]
+  double* bpart;       // block partials (StatSpec{0,P} edge, {P,2P} vertex)
+  long long nrows;
+  long long De;
+  long long lim;       // Pn * Dn
+  int K, kstride, P, Pp, ostride;
+};
+
+template <typename T, typename F>
+acg_status launch_cdist_rb(const CdistRbArgs<T, F>& a, int mode, int blocks, cudaStream_t s);
+
+}  // namespace acg

@@ -301,7 +301,8 @@ __global__ void item_fill_kernel(const int* __restrict__ off, int n, int chunk,
                                  const uint32_t* __restrict__ item_off,
                                  const uint32_t* __restrict__ hidx,
                                  const uint32_t* __restrict__ hrow, int4* __restrict__ items,
-                                 int* __restrict__ hbase, int* __restrict__ hcount) {
+                                 int* __restrict__ hbase, int* __restrict__ hcount,
+                                 int* __restrict__ hvert) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
   const int i0 = off[v], i1 = off[v + 1];
@@ -311,6 +312,7 @@ __global__ void item_fill_kernel(const int* __restrict__ off, int n, int chunk,
   if (h >= 0) {
     hbase[h] = (int)hrow[v];
     hcount[h] = c;
+    hvert[h] = v;
   }
   const uint32_t base = item_off[v];
   for (int j = 0; j < c; ++j) {
@@ -331,7 +333,7 @@ acg_status build_items(const Csr& csr, int chunk, Items* out, std::vector<DevBuf
     ACG_TRY(dev_alloc(owned, 16, (void**)&out->items, s));
     ACG_TRY(dev_alloc(owned, 16, (void**)&out->hbase, s));
     ACG_TRY(dev_alloc(owned, 16, (void**)&out->hcount, s));
-    ACG_TRY(dev_alloc(owned, 16, (void**)&out->hcounter, s));
+    ACG_TRY(dev_alloc(owned, 16, (void**)&out->hvert, s));
     return ACG_OK;
   }
   const size_t nn = (size_t)n + 1;  // one extra slot so the scan yields totals
@@ -355,9 +357,10 @@ acg_status build_items(const Csr& csr, int chunk, Items* out, std::vector<DevBuf
   ACG_TRY(dev_alloc(owned, sizeof(int4) * (size_t)out->nitems, (void**)&out->items, s));
   ACG_TRY(dev_alloc(owned, sizeof(int) * (size_t)out->nheavy, (void**)&out->hbase, s));
   ACG_TRY(dev_alloc(owned, sizeof(int) * (size_t)out->nheavy, (void**)&out->hcount, s));
-  ACG_TRY(dev_alloc(owned, sizeof(unsigned) * (size_t)out->nheavy, (void**)&out->hcounter, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * (size_t)out->nheavy, (void**)&out->hvert, s));
   item_fill_kernel<<<ceil_div(n, 256), 256, 0, s>>>(csr.off, n, chunk, nch, heavy, hch,
-                                                    out->items, out->hbase, out->hcount);
+                                                    out->items, out->hbase, out->hcount,
+                                                    out->hvert);
   ACG_LAUNCH_CHECK();
   cudaFreeAsync(tmp, s);
   return ACG_OK;

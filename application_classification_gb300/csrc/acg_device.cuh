@@ -66,6 +66,9 @@ struct OnlineLse<double> {
       s += exp(x - m);
     }
   }
+  // add x = hi + lo (lo tiny next to hi)
+  __device__ __forceinline__ void add2(double hi, double lo) { add(hi + lo); }
+  __device__ __forceinline__ void add_fast(double x) { add(x); }
   __device__ __forceinline__ double mval() const { return m; }
   __device__ __forceinline__ double sval() const { return s; }
 };
@@ -96,6 +99,32 @@ struct OnlineLse<float> {
       kahan(expf(x - m));
     }
   }
+  // add x = hi + lo (lo tiny next to hi): exp(hi + lo - m) = exp(hi - m)(1 + lo)
+  // to first order, so the low part of a compensated value is not lost
+  __device__ __forceinline__ void add2(float hi, float lo) {
+    if (!(hi > -CUDART_INF_F)) return;
+    if (hi > m) {
+      float sc = expf(m - hi);
+      s *= sc;
+      c *= sc;
+      m = hi;
+      kahan(1.f + lo);
+    } else {
+      kahan(expf(hi - m) * (1.f + lo));
+    }
+  }
+  // Branch-free variant with the fast exponential, for the hot per-vertex
+  // statistics: m' = max(m, x); s = s e^(m - m') + e^(x - m').  Terms near the
+  // running maximum dominate the sum and carry ~1e-7 relative error.
+  __device__ __forceinline__ void add_fast(float x) {
+    if (!(x > -CUDART_INF_F)) return;
+    const float mn = fmaxf(m, x);
+    const float sc = __expf(m - mn);  // m = -inf -> 0
+    s *= sc;
+    c *= sc;
+    kahan(__expf(x - mn));
+    m = mn;
+  }
   __device__ __forceinline__ double mval() const { return (double)m; }
   __device__ __forceinline__ double sval() const { return (double)s - (double)c; }
 };
@@ -124,6 +153,68 @@ struct LseD {
   __device__ __forceinline__ double value() const {
     return (m > -CUDART_INF && s > 0.0) ? m + log(s) : -CUDART_INF;
   }
+};
+
+__device__ __forceinline__ void lse_merge(double& m, double& s, double m2, double s2) {
+  LseD a{m, s};
+  a.merge(m2, s2);
+  m = a.m;
+  s = a.s;
+}
+
+// Per-block statistics written as partials [slot][column]: `nmax` maxima, then
+// `nlse` log-sum-exps as (m, s) pairs.  red[w * slots + slot] holds warp w's
+// value; warps are combined in order, so the result does not depend on timing.
+__device__ __forceinline__ void write_block_partials(const double* red, int nwarps, int nmax,
+                                                     int nlse, double* bpart, int ncols,
+                                                     int col) {
+  const int slots = nmax + 2 * nlse;
+  for (int j = threadIdx.x; j < nmax + nlse; j += blockDim.x) {
+    if (j < nmax) {
+      double m = -CUDART_INF;
+      for (int w = 0; w < nwarps; ++w) m = fmax(m, red[w * slots + j]);
+      bpart[(size_t)j * ncols + col] = m;
+    } else {
+      const int sm = nmax + 2 * (j - nmax);
+      double m = -CUDART_INF, s = 0.0;
+      for (int w = 0; w < nwarps; ++w) lse_merge(m, s, red[w * slots + sm], red[w * slots + sm + 1]);
+      bpart[(size_t)sm * ncols + col] = m;
+      bpart[(size_t)(sm + 1) * ncols + col] = s;
+    }
+  }
+}
+
+// Compensated running sum for FP32 (TwoSum: hi + lo carries the exact sum of
+// the added terms to within one rounding); plain sum for FP64.
+template <typename T>
+struct CSum;
+template <>
+struct CSum<float> {
+  float hi, lo;
+  __device__ __forceinline__ void init(float x) {
+    hi = x;
+    lo = 0.f;
+  }
+  __device__ __forceinline__ void add(float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    lo += (hi - (s - bp)) + (x - bp);
+    hi = s;
+  }
+  __device__ __forceinline__ float value() const { return hi + lo; }
+  // (hi + lo) - y with a single final rounding of the small part
+  __device__ __forceinline__ float minus(float y) const { return (hi - y) + lo; }
+  __device__ __forceinline__ double dvalue() const { return (double)hi + (double)lo; }
+};
+template <>
+struct CSum<double> {
+  double hi;
+  double lo = 0.0;  // always zero: FP64 needs no compensation here
+  __device__ __forceinline__ void init(double x) { hi = x; }
+  __device__ __forceinline__ void add(double x) { hi += x; }
+  __device__ __forceinline__ double value() const { return hi; }
+  __device__ __forceinline__ double minus(double y) const { return hi - y; }
+  __device__ __forceinline__ double dvalue() const { return hi; }
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {

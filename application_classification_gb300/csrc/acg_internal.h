@@ -30,8 +30,8 @@ struct Csr {
 
 // Work items of one CSR: item = {vertex, first position, end position, heavy
 // vertex index or -1}.  A vertex with more than `chunk` edges is split into
-// ceil(deg / chunk) items that each reduce into a partial row; the last one to
-// finish combines the partial rows (no waiting, see the kernels).
+// ceil(deg / chunk) items that each reduce into a partial row; a second launch
+// combines each heavy vertex's rows (no waiting, no atomics).
 struct Items {
   int4* items = nullptr;   // [nitems]
   int nitems = 0;
@@ -40,7 +40,7 @@ struct Items {
   int npartial = 0;        // partial rows = total chunks of heavy vertices
   int* hbase = nullptr;    // [nheavy] first partial row of heavy vertex h
   int* hcount = nullptr;   // [nheavy] number of chunks of heavy vertex h
-  unsigned* hcounter = nullptr;  // [nheavy] arrival counters, zero between launches
+  int* hvert = nullptr;    // [nheavy] vertex id of heavy vertex h
 };
 
 // ---- primitives (acg_csr.cu)

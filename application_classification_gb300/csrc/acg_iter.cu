@@ -1,0 +1,567 @@
+// acg_iter.cu -- one BP iteration as two kernels (see acg_bp.cu's header for
+// the algebra).
+//
+// Phase A, edge_max_kernel -- the segmented (max, -) reduction over the
+// destination-sorted CSR:  M'[v][q] = max_{e in in(v)} VR'[s_e][q] - dE[e][q].
+//   One warp per work item (a light vertex's in-edges, or one chunk of a heavy
+//   vertex's).  The 32 lanes are (edge slot, 16-byte column) pairs: NPOW lanes
+//   cover one [Pp] row, S = 32 / NPOW in-edges are loaded per instruction and
+//   kU instructions are issued back to back, so each warp keeps S * kU pairs of
+//   (streamed dE row, gathered VR' row) in flight.  Each warp walks a
+//   contiguous item range of near-equal cost (load steps plus a per-item
+//   overhead), computed on the host.  A chunk writes a partial row;
+//   heavy_combine_kernel takes the max of a heavy vertex's partial rows.
+//
+// Phase B, vertex_update_kernel -- everything per vertex, streamed with
+//   coalesced 16-byte accesses: FMax, RMax, MU_raw (compensated sum), the next
+//   VF', VR', and per-column statistics.  One thread per (vertex, 16-byte
+//   column) for the q-side and per (vertex, pattern vertex) for MU; a block
+//   walks fixed tiles of consecutive vertices and every thread owns fixed
+//   columns, so statistics are accumulated in registers in a fixed order and
+//   results are bit-reproducible.  No kernel waits on another block.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "acg_device.cuh"
+#include "acg_iter.cuh"
+
+namespace acg {
+
+namespace {
+
+constexpr int kAT = 256;       // threads per block, phase A
+constexpr int kU = 4;          // edge steps issued back to back
+constexpr int kBT = 256;       // threads per block, phase B
+
+template <typename T>
+struct VecT;
+template <>
+struct VecT<double> {
+  using type = double2;
+  static constexpr int W = 2;
+};
+template <>
+struct VecT<float> {
+  using type = float4;
+  static constexpr int W = 4;
+};
+template <typename T>
+__device__ __forceinline__ T vg(const typename VecT<T>::type& v, int w) {
+  return reinterpret_cast<const T*>(&v)[w];
+}
+template <typename T>
+__device__ __forceinline__ void vs(typename VecT<T>::type& v, int w, T x) {
+  reinterpret_cast<T*>(&v)[w] = x;
+}
+template <typename T>
+__device__ __forceinline__ typename VecT<T>::type vfill(T x) {
+  typename VecT<T>::type r;
+#pragma unroll
+  for (int w = 0; w < VecT<T>::W; ++w) vs<T>(r, w, x);
+  return r;
+}
+
+__host__ __device__ inline size_t a16(size_t b) { return (b + 15) & ~size_t(15); }
+
+// ------------------------------------------------------------------ phase A
+template <typename T, int NPOW, int NQV>
+__global__ void __launch_bounds__(kAT)
+edge_max_kernel(const EdgeMaxArgs<T> a) {
+  using VT = typename VecT<T>::type;
+  constexpr int W = VecT<T>::W;
+  constexpr int S = 32 / NPOW;
+  constexpr int NQ = NQV * W;
+  constexpr int STEP = S * kU;
+  const int Pp = a.Pp;
+  const int lane = threadIdx.x & 31;
+  const int slot = lane / NPOW, qc = lane % NPOW;
+  const int gw = (blockIdx.x * kAT + threadIdx.x) >> 5;
+  const int it_end = __ldg(a.wsplit + gw + 1);
+  int it = __ldg(a.wsplit + gw);
+  if (it >= it_end) return;
+
+  // Software pipeline over the warp's steps (kU in-edges per slot per step,
+  // crossing item boundaries): the source indices of step k+1 are loaded while
+  // the gathered rows of step k are in flight.
+  int4 item = __ldg(a.items + it);
+  int4 item_next = it + 1 < it_end ? __ldg(a.items + it + 1) : make_int4(0, 0, 0, -1);
+  int base = item.y;
+  int sidx[kU];
+#pragma unroll
+  for (int u = 0; u < kU; ++u) {
+    const int e = base + slot + S * u;
+    sidx[u] = e < item.z ? __ldg(a.src_of + e) : 0;
+  }
+  T acc[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) acc[k] = neg_inf<T>();
+  for (;;) {
+    // rows of this step
+    VT x[kU][NQV], y[kU][NQV];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int e = base + slot + S * u;
+      const bool ok = e < item.z;
+#pragma unroll
+      for (int k = 0; k < NQV; ++k) {
+        const int qv = qc + NPOW * k;
+        if (ok && qv * W < Pp) {
+          x[u][k] = __ldg(reinterpret_cast<const VT*>(a.vr_in + (size_t)sidx[u] * Pp) + qv);
+          y[u][k] = __ldcs(reinterpret_cast<const VT*>(a.dE + (size_t)e * Pp) + qv);
+        } else {
+          x[u][k] = vfill<T>(neg_inf<T>());
+          y[u][k] = vfill<T>(T(0));
+        }
+      }
+    }
+    // next step's position, and its source indices (in flight with the rows)
+    const bool item_done = base + STEP >= item.z;
+    int nbase = base + STEP, nend = item.z;
+    bool more = true;
+    if (item_done) {
+      more = it + 1 < it_end;
+      nbase = item_next.y;
+      nend = item_next.z;
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int e = nbase + slot + S * u;
+      sidx[u] = (more && e < nend) ? __ldg(a.src_of + e) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u)
+#pragma unroll
+      for (int k = 0; k < NQV; ++k)
+#pragma unroll
+        for (int w = 0; w < W; ++w)
+          acc[k * W + w] = fmax(acc[k * W + w], vg<T>(x[u][k], w) - vg<T>(y[u][k], w));
+    if (item_done) {
+#pragma unroll
+      for (int o = NPOW; o < 32; o <<= 1)
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) acc[k] = fmax(acc[k], __shfl_xor_sync(0xffffffffu, acc[k], o));
+      if (slot == 0) {
+        T* row = item.w >= 0 ? a.partial + (size_t)item.w * Pp : a.M + (size_t)item.x * Pp;
+#pragma unroll
+        for (int k = 0; k < NQV; ++k) {
+          const int qv = qc + NPOW * k;
+          if (qv * W < Pp) {
+            VT o;
+#pragma unroll
+            for (int w = 0; w < W; ++w) vs<T>(o, w, acc[k * W + w]);
+            reinterpret_cast<VT*>(row)[qv] = o;
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) acc[k] = neg_inf<T>();
+      if (!more) break;
+      ++it;
+      item = item_next;
+      item_next = it + 1 < it_end ? __ldg(a.items + it + 1) : make_int4(0, 0, 0, -1);
+    }
+    base = nbase;
+  }
+}
+
+// Max over each heavy vertex's partial rows: one warp per heavy vertex.
+template <typename T>
+__global__ void __launch_bounds__(256)
+heavy_combine_kernel(const T* __restrict__ partial, const int* __restrict__ hbase,
+                     const int* __restrict__ hcount, const int* __restrict__ hvert, int nheavy,
+                     int Pp, T* __restrict__ M) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= nheavy) return;
+  const T* p0 = partial + (size_t)hbase[warp] * Pp;
+  const int cnt = hcount[warp];
+  T* row = M + (size_t)hvert[warp] * Pp;
+  for (int q = lane; q < Pp; q += 32) {
+    T m = neg_inf<T>();
+    int r = 0;
+    for (; r + 4 <= cnt; r += 4) {
+      const T a0 = p0[(size_t)r * Pp + q], a1 = p0[(size_t)(r + 1) * Pp + q];
+      const T a2 = p0[(size_t)(r + 2) * Pp + q], a3 = p0[(size_t)(r + 3) * Pp + q];
+      m = fmax(m, fmax(fmax(a0, a1), fmax(a2, a3)));
+    }
+    for (; r < cnt; ++r) m = fmax(m, p0[(size_t)r * Pp + q]);
+    row[q] = m;
+  }
+}
+
+// ------------------------------------------------------------------ phase B
+struct UpdSmem {
+  size_t pat, fill, lq, F, R, MU, red, stage, sM, sVF, sEM, sB, sCV, sOff, stage_bytes, total;
+  __host__ __device__ UpdSmem(int V, int Pn, int Pe, int Pp, int Pnp, int sz) {
+    size_t o = 0;
+    pat = o; o += a16(sizeof(int) * (size_t)(4 * Pe + 2 * (Pn + 1)));
+    fill = o; o += a16((size_t)2 * Pp * sz);  // fillF, fillR (padded to Pp)
+    lq = o; o += a16((size_t)4 * Pp * sz);    // lF, lFlo, lR, lRlo (padded to Pp)
+    F = o; o += a16((size_t)V * Pp * sz);
+    R = o; o += a16((size_t)V * Pp * sz);
+    MU = o; o += a16((size_t)V * 2 * Pn * sz);  // hi, lo
+    red = o; o += a16(sizeof(double) * (size_t)kBT * 6);
+    // one stage: the tile's M, VF, dEmin, B rows, CV rows, in-degree offsets
+    size_t so = 0;
+    sM = so; so += a16((size_t)V * Pp * sz);
+    sVF = so; so += a16((size_t)V * Pp * sz);
+    sEM = so; so += a16((size_t)V * Pp * sz);
+    sB = so; so += a16((size_t)V * Pp * sz);
+    sCV = so; so += a16((size_t)V * Pnp * sz);
+    sOff = so; so += a16(sizeof(int) * (size_t)(V + 1));
+    stage_bytes = so;
+    stage = o; o += 2 * so;
+    total = o;
+  }
+};
+
+__device__ __forceinline__ unsigned sm_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void cp16(void* sdst, const void* gsrc) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sm_u32(sdst)), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp4(void* sdst, const void* gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sm_u32(sdst)), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+template <typename T>
+__global__ void __launch_bounds__(kBT, 2)
+vertex_update_kernel(const VertexUpdArgs<T> a) {
+  using VT = typename VecT<T>::type;
+  constexpr int W = VecT<T>::W;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int Pe = a.Pe, Pn = a.Pn, Pp = a.Pp, Pnp = a.Pnp, Dn = a.Dn;
+  const int nvec = Pp / W;
+  const int V = kBT / nvec;  // vertices per tile
+  const UpdSmem L(V, Pn, Pe, Pp, Pnp, sizeof(T));
+  int* s_pat = reinterpret_cast<int*>(smem + L.pat);
+  T* s_fillF = reinterpret_cast<T*>(smem + L.fill);
+  T* s_fillR = s_fillF + Pp;
+  T* s_lF = reinterpret_cast<T*>(smem + L.lq);
+  T* s_lFlo = s_lF + Pp;
+  T* s_lR = s_lFlo + Pp;
+  T* s_lRlo = s_lR + Pp;
+  T* s_F = reinterpret_cast<T*>(smem + L.F);
+  T* s_R = reinterpret_cast<T*>(smem + L.R);
+  T* s_MU = reinterpret_cast<T*>(smem + L.MU);  // [V][Pn] hi then [V][Pn] lo
+  T* s_MUlo = s_MU + (size_t)V * Pn;
+  double* s_red = reinterpret_cast<double*>(smem + L.red);
+  const int* s_psrc = s_pat;
+  const int* s_pdst = s_pat + Pe;
+  const int* s_inoff = s_pat + 2 * Pe;
+  const int* s_inq = s_inoff + Pn + 1;
+  const int* s_outoff = s_inq + Pe;
+  const int* s_outq = s_outoff + Pn + 1;
+  const int tid = threadIdx.x;
+
+  for (int t = tid; t < 4 * Pe + 2 * (Pn + 1); t += kBT) s_pat[t] = a.pat[t];
+  __syncthreads();
+  {
+    const double* g = a.glob_in;  // mVF | mVR | lR | lF | S
+    for (int q = tid; q < Pp; q += kBT) {
+      if (q >= Pe) {
+        s_fillF[q] = s_fillR[q] = s_lF[q] = s_lFlo[q] = s_lR[q] = s_lRlo[q] = T(0);
+        continue;
+      }
+      const double cR = g[4 * Pe + s_psrc[q]], cF = g[4 * Pe + s_pdst[q]];
+      s_fillF[q] = (T)(g[Pe + q] - cR);
+      s_fillR[q] = (T)(g[q] - cF);
+      const double lr = g[2 * Pe + q], lf = g[3 * Pe + q];
+      s_lR[q] = (T)lr;
+      s_lRlo[q] = (T)(lr - (double)(T)lr);
+      s_lF[q] = (T)lf;
+      s_lFlo[q] = (T)(lf - (double)(T)lf);
+    }
+  }
+  __syncthreads();
+
+  // fixed columns: q-vector qv (vertex j0 of the tile), pattern vertex pc.
+  // Everything a thread indexes in shared memory is fixed across tiles, so the
+  // pointers and the pattern endpoints of its columns are set up once.
+  const int qv = tid % nvec, j0 = tid / nvec;
+  const bool qact = j0 < V;
+  const int pc = tid % Pn, jp0 = tid / Pn, prows = kBT / Pn;
+  T* const myF = s_F + j0 * Pp + qv * W;
+  T* const myR = s_R + j0 * Pp + qv * W;
+  const T* const myMU = s_MU + j0 * Pn;
+  const T* const myMUlo = s_MUlo + j0 * Pn;
+  const int qoff = j0 * Pp + qv * W;  // offset in a [V][Pp] stage block
+  int pdst[W], psrc[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    const int q = qv * W + w;
+    pdst[w] = q < Pe ? s_pdst[q] : 0;
+    psrc[w] = q < Pe ? s_psrc[q] : 0;
+  }
+  const int in0 = s_inoff[pc], in1 = s_inoff[pc + 1];
+  const int out0 = s_outoff[pc], out1 = s_outoff[pc + 1];
+  T mxF[W], mxR[W];
+  OnlineLse<T> lr[W], lf[W], lmu;
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    mxF[w] = neg_inf<T>();
+    mxR[w] = neg_inf<T>();
+    lr[w].init();
+    lf[w].init();
+  }
+  lmu.init();
+
+  const int ntiles = (Dn + V - 1) / V;
+  const int cvec = Pnp / W;
+  // Stage a tile's rows into shared memory with asynchronous 16-byte copies
+  // (its vertices are consecutive, so every row block is contiguous).
+  auto issue = [&](int tile, int k) {
+    if (tile >= ntiles) return;
+    unsigned char* st = smem + L.stage + (size_t)(k & 1) * L.stage_bytes;
+    const int v0 = tile * V;
+    const int nv = min(V, Dn - v0);
+    const T* gM = a.M + (size_t)v0 * Pp;
+    const T* gVF = a.vf + (size_t)v0 * Pp;
+    const T* gEM = a.dEmin + (size_t)v0 * Pp;
+    const T* gB = a.B + (size_t)v0 * Pp;
+    T* sM = reinterpret_cast<T*>(st + L.sM);
+    T* sVF = reinterpret_cast<T*>(st + L.sVF);
+    T* sEM = reinterpret_cast<T*>(st + L.sEM);
+    T* sB = reinterpret_cast<T*>(st + L.sB);
+    for (int c = tid * W; c < nv * Pp; c += kBT * W) {
+      cp16(sM + c, gM + c);
+      cp16(sVF + c, gVF + c);
+      cp16(sEM + c, gEM + c);
+      cp16(sB + c, gB + c);
+    }
+    const T* gCV = a.CV + (size_t)v0 * Pnp;
+    T* sCV = reinterpret_cast<T*>(st + L.sCV);
+    for (int c = tid * W; c < nv * Pnp; c += kBT * W) cp16(sCV + c, gCV + c);
+    int* sOff = reinterpret_cast<int*>(st + L.sOff);
+    for (int j = tid; j <= nv; j += kBT) cp4(sOff + j, a.d_off + v0 + j);
+  };
+  (void)cvec;
+  issue(blockIdx.x, 0);
+  cp_commit();
+  int k = 0;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++k) {
+    issue(tile + gridDim.x, k + 1);  // next tile's copies fly while this one computes
+    cp_commit();
+    cp_wait1();
+    __syncthreads();
+    const unsigned char* st = smem + L.stage + (size_t)(k & 1) * L.stage_bytes;
+    const T* sCV = reinterpret_cast<const T*>(st + L.sCV);
+    const int* sOff = reinterpret_cast<const int*>(st + L.sOff);
+    const int v0 = tile * V;
+    const int v = v0 + j0;
+    const bool vok = qact && v < Dn;
+    VT bv = vfill<T>(T(0));
+    if (vok) {
+      const bool has_in = sOff[j0 + 1] > sOff[j0];
+      const VT mv = has_in ? *reinterpret_cast<const VT*>(reinterpret_cast<const T*>(st + L.sM) + qoff)
+                           : vfill<T>(neg_inf<T>());
+      const VT vfv = *reinterpret_cast<const VT*>(reinterpret_cast<const T*>(st + L.sVF) + qoff);
+      const VT emv = *reinterpret_cast<const VT*>(reinterpret_cast<const T*>(st + L.sEM) + qoff);
+      bv = *reinterpret_cast<const VT*>(reinterpret_cast<const T*>(st + L.sB) + qoff);
+      // per-q constants of the thread's columns (16-byte shared loads)
+      const VT fF = *reinterpret_cast<const VT*>(s_fillF + qv * W);
+      const VT fR = *reinterpret_cast<const VT*>(s_fillR + qv * W);
+      const VT cF = *reinterpret_cast<const VT*>(s_lF + qv * W);
+      const VT cFl = *reinterpret_cast<const VT*>(s_lFlo + qv * W);
+      const VT cR = *reinterpret_cast<const VT*>(s_lR + qv * W);
+      const VT cRl = *reinterpret_cast<const VT*>(s_lRlo + qv * W);
+      VT fo, ro;
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        // no in-edges: M = -inf; no out-edges: dEmin = +inf; the fill wins
+        vs<T>(fo, w, fmax(vg<T>(fF, w), (vg<T>(mv, w) - vg<T>(cF, w)) - vg<T>(cFl, w)));
+        vs<T>(ro, w, fmax(vg<T>(fR, w), ((vg<T>(vfv, w) - vg<T>(emv, w)) - vg<T>(cR, w)) - vg<T>(cRl, w)));
+      }
+      *reinterpret_cast<VT*>(myF) = fo;
+      *reinterpret_cast<VT*>(myR) = ro;
+    }
+    __syncthreads();
+    // MU_raw = -CV + sum F + sum R, compensated (|terms| reach 50..100)
+    for (int j = jp0; j < V && jp0 < prows; j += prows) {
+      const int vv = v0 + j;
+      if (vv >= Dn) break;
+      const T* rowF = s_F + j * Pp;
+      const T* rowR = s_R + j * Pp;
+      CSum<T> mu;
+      mu.init(-sCV[j * Pnp + pc]);
+      for (int t = in0; t < in1; ++t) mu.add(rowF[s_inq[t]]);
+      for (int t = out0; t < out1; ++t) mu.add(rowR[s_outq[t]]);
+      s_MU[j * Pn + pc] = mu.hi;
+      if constexpr (sizeof(T) == 4) s_MUlo[j * Pn + pc] = mu.lo;
+      lmu.add2(mu.hi, mu.lo);
+      if (a.last) a.mu_raw[(size_t)vv * Pn + pc] = mu.dvalue();
+    }
+    __syncthreads();
+    if (!a.last && vok) {
+      const VT fo = *reinterpret_cast<const VT*>(myF);
+      const VT ro = *reinterpret_cast<const VT*>(myR);
+      VT nf, nr;
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        T f, r;
+        if constexpr (sizeof(T) == 4) {
+          f = (myMU[pdst[w]] - vg<T>(fo, w)) + myMUlo[pdst[w]];
+          r = (myMU[psrc[w]] - vg<T>(ro, w)) + myMUlo[psrc[w]];
+        } else {
+          f = myMU[pdst[w]] - vg<T>(fo, w);
+          r = myMU[psrc[w]] - vg<T>(ro, w);
+        }
+        if (qv * W + w < Pe) {
+          mxF[w] = fmax(mxF[w], f);
+          mxR[w] = fmax(mxR[w], r);
+          const T b = vg<T>(bv, w);
+          lr[w].add_fast(f + b);
+          lf[w].add_fast(r + b);
+        } else {
+          f = T(0);
+          r = T(0);
+        }
+        vs<T>(nf, w, f);
+        vs<T>(nr, w, r);
+      }
+      const size_t go = (size_t)v * Pp + (size_t)qv * W;
+      *reinterpret_cast<VT*>(a.vf + go) = nf;
+      *reinterpret_cast<VT*>(a.vr_out + go) = nr;
+    }
+    __syncthreads();  // the tile's smem rows and this stage are free
+  }
+  cp_wait0();
+
+  // ---- block partials: mVF, mVR (max), lR, lF, S (lse); rows combined in order
+  const int nmax = 2 * Pe;
+  const int ncols = gridDim.x, col = blockIdx.x;
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    __syncthreads();
+    double* e = s_red + (size_t)tid * 6;
+    e[0] = (double)mxF[w];
+    e[1] = (double)mxR[w];
+    e[2] = lr[w].mval();
+    e[3] = lr[w].sval();
+    e[4] = lf[w].mval();
+    e[5] = lf[w].sval();
+    __syncthreads();
+    for (int c = tid; c < nvec; c += kBT) {
+      const int q = c * W + w;
+      if (q >= Pe) continue;
+      double f = -CUDART_INF, r = -CUDART_INF, m1 = -CUDART_INF, s1 = 0, m2 = -CUDART_INF, s2 = 0;
+      for (int row = 0; row < V; ++row) {
+        const double* x = s_red + (size_t)(row * nvec + c) * 6;
+        f = fmax(f, x[0]);
+        r = fmax(r, x[1]);
+        lse_merge(m1, s1, x[2], x[3]);
+        lse_merge(m2, s2, x[4], x[5]);
+      }
+      a.bpart[(size_t)q * ncols + col] = f;
+      a.bpart[(size_t)(Pe + q) * ncols + col] = r;
+      a.bpart[(size_t)(nmax + 2 * q) * ncols + col] = m1;
+      a.bpart[(size_t)(nmax + 2 * q + 1) * ncols + col] = s1;
+      a.bpart[(size_t)(nmax + 2 * (Pe + q)) * ncols + col] = m2;
+      a.bpart[(size_t)(nmax + 2 * (Pe + q) + 1) * ncols + col] = s2;
+    }
+  }
+  __syncthreads();
+  s_red[tid * 2] = lmu.mval();
+  s_red[tid * 2 + 1] = lmu.sval();
+  __syncthreads();
+  for (int p = tid; p < Pn; p += kBT) {
+    double m = -CUDART_INF, s = 0;
+    for (int row = 0; row < prows; ++row)
+      lse_merge(m, s, s_red[(row * Pn + p) * 2], s_red[(row * Pn + p) * 2 + 1]);
+    a.bpart[(size_t)(nmax + 2 * (2 * Pe + p)) * ncols + col] = m;
+    a.bpart[(size_t)(nmax + 2 * (2 * Pe + p) + 1) * ncols + col] = s;
+  }
+}
+
+#define ACG_EDGE_SHAPES(X) \
+  X(1, 1) X(2, 1) X(4, 1) X(8, 1) X(16, 1) X(32, 1) X(32, 2) X(32, 4)
+
+}  // namespace
+
+int edge_step(WarpShape ws) { return (32 / ws.npow) * kU; }
+
+WarpShape choose_warp_shape(int elem_bytes, int pp) {
+  const int W = 16 / elem_bytes;
+  const int nvec = (pp + W - 1) / W;
+  WarpShape ws{32, 1};
+  if (nvec <= 32) {
+    int np = 1;
+    while (np < nvec) np <<= 1;
+    ws.npow = np;
+    ws.nqv = 1;
+  } else {
+    ws.npow = 32;
+    ws.nqv = nvec <= 64 ? 2 : 4;
+  }
+  return ws;
+}
+
+#define ACG_EDGE_LAUNCH(NP_, NQ_)                                           \
+  if (ws.npow == NP_ && ws.nqv == NQ_) {                                    \
+    edge_max_kernel<T, NP_, NQ_><<<blocks, kAT, 0, s>>>(a);                 \
+    ACG_LAUNCH_CHECK();                                                     \
+    return ACG_OK;                                                          \
+  }
+
+template <typename T>
+acg_status launch_edge_max(const EdgeMaxArgs<T>& a, WarpShape ws, int blocks, cudaStream_t s) {
+  if (a.nitems == 0) return ACG_OK;
+  ACG_EDGE_SHAPES(ACG_EDGE_LAUNCH)
+  return set_error(ACG_ERR_UNSUPPORTED, "no edge kernel for npow=%d nqv=%d", ws.npow, ws.nqv);
+}
+
+template <typename T>
+acg_status launch_heavy_combine(const T* partial, const int* hbase, const int* hcount,
+                                const int* hvert, int nheavy, int Pp, T* M, cudaStream_t s) {
+  if (nheavy == 0) return ACG_OK;
+  heavy_combine_kernel<T><<<ceil_div(nheavy, 8), 256, 0, s>>>(partial, hbase, hcount, hvert,
+                                                               nheavy, Pp, M);
+  ACG_LAUNCH_CHECK();
+  return ACG_OK;
+}
+
+template <typename T>
+size_t vertex_update_smem(int pn, int pe, int pp) {
+  const int nvec = pp / VecT<T>::W;
+  const int pnp = (pn + VecT<T>::W - 1) / VecT<T>::W * VecT<T>::W;
+  return UpdSmem(kBT / nvec, pn, pe, pp, pnp, sizeof(T)).total;
+}
+
+template <typename T>
+acg_status launch_vertex_update(const VertexUpdArgs<T>& a, int blocks, cudaStream_t s) {
+  const size_t sm = vertex_update_smem<T>(a.Pn, a.Pe, a.Pp);
+  if (sm > 48 * 1024)
+    ACG_CUDA_TRY(cudaFuncSetAttribute(vertex_update_kernel<T>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  vertex_update_kernel<T><<<blocks, kBT, sm, s>>>(a);
+  ACG_LAUNCH_CHECK();
+  return ACG_OK;
+}
+
+template <typename T>
+int vertex_update_blocks_per_sm(int pn, int pe, int pp) {
+  const size_t sm = vertex_update_smem<T>(pn, pe, pp);
+  if (sm > 48 * 1024)
+    cudaFuncSetAttribute(vertex_update_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int nb = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, vertex_update_kernel<T>, kBT, sm) !=
+      cudaSuccess)
+    nb = 1;
+  return nb < 1 ? 1 : nb;
+}
+
+template acg_status launch_edge_max<double>(const EdgeMaxArgs<double>&, WarpShape, int, cudaStream_t);
+template acg_status launch_edge_max<float>(const EdgeMaxArgs<float>&, WarpShape, int, cudaStream_t);
+template acg_status launch_heavy_combine<double>(const double*, const int*, const int*, const int*, int, int, double*, cudaStream_t);
+template acg_status launch_heavy_combine<float>(const float*, const int*, const int*, const int*, int, int, float*, cudaStream_t);
+template acg_status launch_vertex_update<double>(const VertexUpdArgs<double>&, int, cudaStream_t);
+template acg_status launch_vertex_update<float>(const VertexUpdArgs<float>&, int, cudaStream_t);
+template int vertex_update_blocks_per_sm<double>(int, int, int);
+template int vertex_update_blocks_per_sm<float>(int, int, int);
+
+}  // namespace acg

@@ -32,8 +32,13 @@ def test_rmat18_fp64_vs_mixed(cuda, rmat18):
     assert np.isfinite(mu64).all() and np.isfinite(mu32).all()
     assert _colsum_err(mu64) < 1e-10
     assert _colsum_err(mu32) < 1e-6
-    assert np.abs(mu32 - mu64).max() <= 1e-4
-    assert (mu32.argmax(1) == mu64.argmax(1)).mean() > 0.999999
+    err = np.abs(mu32 - mu64).max()
+    assert err <= 1e-4
+    # identical per-vertex argmax, except where the FP64 top two are closer than
+    # the mixed path can resolve (2 x its max error): ties at that precision
+    srt = np.sort(mu64, axis=1)
+    tie = (srt[:, -1] - srt[:, -2]) <= 2 * err
+    assert ((mu32.argmax(1) == mu64.argmax(1)) | tie).all()
     # the planted vertices are the best match of each pattern vertex
     assert all(int(mu64[:, i].argmax()) == int(truth[i]) for i in range(p.num_nodes))
 
