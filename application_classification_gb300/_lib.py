@@ -106,6 +106,7 @@ SIGNATURES: dict[str, tuple] = {
     "acg_match": (i32, [vp, vp, vp]),
     "acg_plan_stats": (i32, [vp, _P(Stats)]),
     "acg_match_graphs": (i32, [_P(Graph), _P(Graph), _P(Options), vp, vp]),
+    "acg_initial_mu_noalloc": (i32, [vp, u64, u64, vp, u64, vp, vp]),
     "acg_status_string": (C.c_char_p, [i32]),
     "acg_last_error": (C.c_char_p, []),
     "acg_version": (C.c_char_p, []),

@@ -135,6 +135,24 @@ acg_status acg_match_graphs(const acg_graph* data, const acg_graph* pattern,
                             const acg_options* opt, double* mu_out,
                             void* stream);
 
+/* ---------------- no-allocation entry point ---------------------------- */
+/* The match's initial mu, before any BP iteration:
+ *   mu_out[v][p] = -d(v,p) - log sum_v' exp(-d(v',p)),  d = || x_v - y_p ||_2,
+ * i.e. the [num_nodes][pattern_nodes] output acg_match gives with
+ * num_iters = 0, computed without allocating any memory.  No counterpart in
+ * the reference: it exists for callers that cannot allocate device memory at
+ * the point of the call (inside stream capture, under a fixed memory budget,
+ * or embedded behind another framework's allocator).  Its scratch is one
+ * file-scope device array of about 1.5 MB that every GPU loading the library
+ * keeps until exit.  Limits: 1..128 pattern vertices, feature dimension
+ * 1..32 (else ACG_ERR_UNSUPPORTED).  The first call on each device looks the
+ * array's address up (make it before any stream capture).  All calls share the
+ * array: calls whose work overlaps on the GPU race and must be serialised.
+ * Inputs and output are caller-owned device memory (FP64, row-major). */
+acg_status acg_initial_mu_noalloc(const double* data_node_feats, uint64_t num_nodes,
+                                  uint64_t feat_dim, const double* pattern_node_feats,
+                                  uint64_t pattern_nodes, double* mu_out, void* stream);
+
 /* ---------------- errors ----------------------------------------------- */
 const char* acg_status_string(acg_status s);
 /* Message of the last failing call on this host thread ("" if none). */
