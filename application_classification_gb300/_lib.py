@@ -77,8 +77,10 @@ class Stats(C.Structure):
         ("ms_init", C.c_double),
         ("ms_iters", C.c_double),
         ("bytes_iters", C.c_double),
-        ("bytes_per_edge_pass", C.c_double),
-        ("ms_iter_kernels", C.c_double),
+        ("bytes_edge_phase", C.c_double),
+        ("bytes_vertex_phase", C.c_double),
+        ("ms_edge_phase", C.c_double),
+        ("ms_vertex_phase", C.c_double),
         ("launches", i64),
         ("num_iters", i64),
     ]

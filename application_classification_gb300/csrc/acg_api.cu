@@ -95,6 +95,7 @@ struct acg_plan {
   void* dEmin = nullptr;
   void* B = nullptr;
   void* CV = nullptr;
+  void* CVlo = nullptr;  // mixed precision: low part of CV
   void* Rbuf = nullptr;
   void* Fbuf = nullptr;
   void* M = nullptr;          // [Dn][Pp] edge-phase maxima
@@ -103,7 +104,7 @@ struct acg_plan {
   double* bpart = nullptr;
   double* gv = nullptr;      // [3 Pn]
   double* ge = nullptr;      // [Pe]
-  double* gi[2] = {nullptr, nullptr};  // [4 Pe + Pn]
+  double* gi[2] = {nullptr, nullptr};  // [glob_doubles(Pn, Pe)]
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   int kernel_timing = 0;
   std::vector<cudaEvent_t> kev;  // [2 * iters] around each iteration kernel
@@ -145,13 +146,15 @@ __global__ void compose_kernel(const int* __restrict__ seid, const int* __restri
   if (j < m) pos[j] = inv[seid[j]];
 }
 
-__global__ void mu_from_cv_kernel(double* __restrict__ mu, const void* __restrict__ cv, int fp64,
+__global__ void mu_from_cv_kernel(double* __restrict__ mu, const void* __restrict__ cv,
+                                  const float* __restrict__ cvlo, int fp64,
                                   const double* __restrict__ gv, long long n, int Pn, int Pnp) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int p = (int)(i % Pn);
   const long long ci = (i / Pn) * Pnp + p;
-  const double c = fp64 ? ((const double*)cv)[ci] : (double)((const float*)cv)[ci];
+  const double c = fp64 ? ((const double*)cv)[ci]
+                        : (double)((const float*)cv)[ci] + (double)cvlo[ci];
   // CV holds dV - LSE(dV); MU0 = -dV - LSE(-dV)
   mu[i] = -(c + gv[Pn + p]) - gv[2 * Pn + p];
 }
@@ -313,18 +316,20 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
   }
   // ---- init vertex pass
   {
-    InitArgs<T> a{D->dcsr.off, D->scsr.off, (T*)P->CV, (const T*)P->Rbuf, (const T*)P->Fbuf,
-                  (const T*)P->B, (T*)P->vf, (T*)P->vr[0], P->gv, P->ge, P->bpart, P->pat,
-                  De, lim, Dn, Pn, Pe, Pp, P->Pnp};
+    InitArgs<T> a{D->dcsr.off, D->scsr.off, (T*)P->CV, (T*)P->CVlo, (const T*)P->Rbuf,
+                  (const T*)P->Fbuf, (const T*)P->B, (const T*)P->dEmin, (T*)P->vf,
+                  (T*)P->vr[0], P->gv, P->ge, P->bpart, P->pat, De, lim, Dn, Pn, Pe, Pp, P->Pnp};
     ACG_TRY(launch_init_vertex<T>(a, P->gs, P->init_blocks, s));
-    ACG_CUDA_TRY(cudaMemsetAsync(P->gi[0] + 4 * Pe, 0, sizeof(double) * Pn, s));
+    // S = 0 (MU0 is normalised) and shifts 0 for the first pass
+    ACG_CUDA_TRY(cudaMemsetAsync(P->gi[0] + 4 * Pe, 0,
+                                 sizeof(double) * (glob_doubles(Pn, Pe) - 4 * Pe), s));
     ACG_TRY(launch_finalize(P->bpart, P->init_blocks, StatSpec{2 * Pe, 2 * Pe}, P->gi[0], s));
     P->launches += 2;
   }
   cudaEventRecord(P->ev[2], s);
   // ---- BP iterations (main.cu:160-245): edge phase, heavy combine, vertex phase
   for (int t = 1; t <= P->iters; ++t) {
-    if (P->kernel_timing) cudaEventRecord(P->kev[2 * (t - 1)], s);
+    if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1)], s);
     if (Pe > 0) {
       EdgeMaxArgs<T> ea{P->witems, P->nwitems, P->wsplit, D->dcsr.other,
                         (const T*)P->dE, (const T*)P->vr[(t - 1) & 1], (T*)P->M,
@@ -334,13 +339,14 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
                                       P->th_vert, P->th_n, Pp, (T*)P->M, s));
       P->launches += 1 + (P->th_n > 0);
     }
-    if (P->kernel_timing) cudaEventRecord(P->kev[2 * (t - 1) + 1], s);
+    if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1) + 1], s);
     VertexUpdArgs<T> va{D->dcsr.off, (const T*)P->M, (T*)P->vf, (T*)P->vr[t & 1],
                         (const T*)P->dEmin, (const T*)P->B, (const T*)P->CV,
-                        P->gi[(t - 1) & 1], P->bpart, mu_out, P->pat,
-                        Dn, Pn, Pe, Pp, P->Pnp, t == P->iters};
+                        (const T*)P->CVlo, P->gi[(t - 1) & 1], P->gi[t & 1], P->bpart,
+                        mu_out, P->pat, Dn, Pn, Pe, Pp, P->Pnp, t == 1, t == P->iters};
     ACG_TRY(launch_vertex_update<T>(va, P->vert_blocks, s));
     ACG_TRY(launch_finalize(P->bpart, P->vert_blocks, StatSpec{2 * Pe, 2 * Pe + Pn}, P->gi[t & 1], s));
+    if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1) + 2], s);
     P->launches += 2;
   }
   cudaEventRecord(P->ev[3], s);
@@ -350,7 +356,8 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
   } else {
     const long long n = (long long)Dn * Pn;
     if (n > 0) {
-      mu_from_cv_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(mu_out, P->CV, P->prec == ACG_PREC_FP64, P->gv, n, Pn, P->Pnp);
+      mu_from_cv_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+          mu_out, P->CV, (const float*)P->CVlo, P->prec == ACG_PREC_FP64, P->gv, n, Pn, P->Pnp);
       ACG_LAUNCH_CHECK();
     }
   }
@@ -583,6 +590,7 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
   alloc(vrow, &P->Rbuf);
   alloc(vrow, &P->Fbuf);
   alloc((size_t)Dn * P->Pnp * eb, &P->CV);
+  if (P->prec == ACG_PREC_MIXED) alloc((size_t)Dn * P->Pnp * eb, &P->CVlo);
   alloc(vrow, &P->M);
   alloc((size_t)std::max(1, P->th_npartial) * Pp * eb, &P->part_iter);
   alloc((size_t)std::max(1, std::max(P->ditems.npartial, P->sitems.npartial)) * 4 * Pp * eb, &P->part_row);
@@ -592,14 +600,14 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
   alloc(sizeof(double) * bp, (void**)&P->bpart);
   alloc(sizeof(double) * 3 * Pn, (void**)&P->gv);
   alloc(sizeof(double) * std::max(1, Pe), (void**)&P->ge);
-  alloc(sizeof(double) * (4 * Pe + Pn), (void**)&P->gi[0]);
-  alloc(sizeof(double) * (4 * Pe + Pn), (void**)&P->gi[1]);
+  alloc(sizeof(double) * glob_doubles(Pn, Pe), (void**)&P->gi[0]);
+  alloc(sizeof(double) * glob_doubles(Pn, Pe), (void**)&P->gi[1]);
   if (st != ACG_OK) return fail(st);
   for (auto& e : P->ev)
     if (cudaEventCreate(&e) != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "cudaEventCreate failed"));
   P->kernel_timing = o.kernel_timing;
   if (P->kernel_timing) {
-    P->kev.assign(2 * (size_t)P->iters, nullptr);
+    P->kev.assign(3 * (size_t)P->iters, nullptr);
     for (auto& e : P->kev)
       if (cudaEventCreate(&e) != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "cudaEventCreate failed"));
   }
@@ -651,24 +659,27 @@ acg_status acg_plan_stats(acg_plan* P, acg_stats* out) {
   out->ms_total = t04;
   const double eb = elem_bytes(P->prec);
   const double Dn = P->data->Dn, De = P->data->De, Pe = P->Pe, Pn = P->Pn;
-  // Algorithmic bytes of one fused iteration launch (unpadded Pe): per in-edge
-  // its dE row and source index; per vertex the gathered VR row once, the
-  // VF/dEmin/B and CV reads, the VF/VR writes, CSR offsets and the work item.
-  const double edge = De * (Pe * eb + 4.0);
-  const double vert = Dn * (Pe * eb + 3 * Pe * eb + Pn * eb + 2 * Pe * eb + 8.0) +
-                      (double)P->ditems.nitems * 16.0;
-  out->bytes_per_edge_pass = edge + vert;
-  out->bytes_iters = out->bytes_per_edge_pass * P->iters;
+  // Algorithmic bytes (unpadded Pe).  Edge phase: per in-edge its dE row and
+  // source index; each source's Z row read once; each M row written once; the
+  // work items.  Vertex phase: M, Y, dEmin, B and CV (with its low part in
+  // mixed precision) read, Y and Z written, the in-degree offsets.
+  const double cvb = P->prec == ACG_PREC_MIXED ? 2.0 * eb : eb;
+  out->bytes_edge_phase = De * (Pe * eb + 4.0) + 2.0 * Dn * Pe * eb + (double)P->nwitems * 16.0;
+  out->bytes_vertex_phase = Dn * (4.0 * Pe * eb + Pn * cvb + 2.0 * Pe * eb + 4.0);
+  out->bytes_iters = (out->bytes_edge_phase + out->bytes_vertex_phase) * P->iters;
   out->launches = P->launches;
   out->num_iters = P->iters;
   if (P->kernel_timing) {
-    double sum = 0;
+    double se = 0, sv = 0;
     for (int t = 0; t < P->iters; ++t) {
-      float ms = 0;
-      cudaEventElapsedTime(&ms, P->kev[2 * t], P->kev[2 * t + 1]);
-      sum += ms;
+      float a = 0, b = 0;
+      cudaEventElapsedTime(&a, P->kev[3 * t], P->kev[3 * t + 1]);
+      cudaEventElapsedTime(&b, P->kev[3 * t + 1], P->kev[3 * t + 2]);
+      se += a;
+      sv += b;
     }
-    out->ms_iter_kernels = sum;
+    out->ms_edge_phase = se;
+    out->ms_vertex_phase = sv;
   }
   return ACG_OK;
 }

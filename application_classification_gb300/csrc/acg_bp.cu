@@ -434,7 +434,7 @@ init_vertex_kernel(const InitArgs<T> a) {
   double* s_vfmax0 = cv.take<double>(Pe);
   double* s_vrmax0 = cv.take<double>(Pe);
   double* s_lbuf = cv.take<double>(Pe);
-  T* s_grp = cv.take<T>((size_t)GPB * Pn);
+  double* s_grp = cv.take<double>((size_t)GPB * Pn);
   double* s_red = cv.take<double>((size_t)kWarps * 6 * Pe);
   const int* s_psrc = s_pat;
   const int* s_pdst = s_pat + Pe;
@@ -460,7 +460,7 @@ init_vertex_kernel(const InitArgs<T> a) {
   __syncthreads();
   const Grp<G> gr;
   const int gib = threadIdx.x / G;
-  T* my_MU = s_grp + (size_t)gib * Pn;
+  double* my_MU = s_grp + (size_t)gib * Pn;
   T mxF[NQ], mxR[NQ];
   OnlineLse<T> lr[NQ], lf[NQ];
 #pragma unroll
@@ -474,8 +474,11 @@ init_vertex_kernel(const InitArgs<T> a) {
   for (int v = blockIdx.x * GPB + gib; v < a.Dn; v += gstride) {
     for (int p = gr.lig; p < Pn; p += G) {
       const double dv = (double)a.CV[(size_t)v * a.Pnp + p];
-      a.CV[(size_t)v * a.Pnp + p] = (T)(dv - s_lse1[p]);
-      my_MU[p] = (T)(-dv - s_lse2[p]);
+      const double c = dv - s_lse1[p];
+      const T ch = (T)c;
+      a.CV[(size_t)v * a.Pnp + p] = ch;
+      if constexpr (sizeof(T) == 4) a.CVlo[(size_t)v * a.Pnp + p] = (T)(c - (double)ch);
+      my_MU[p] = -dv - s_lse2[p];
     }
     __syncwarp(gr.mask);
     const int indeg = a.d_off[v + 1] - a.d_off[v];
@@ -487,20 +490,22 @@ init_vertex_kernel(const InitArgs<T> a) {
       for (int w = 0; w < W; ++w) {
         const int q = (gr.lig + G * k) * W + w;
         if (q < Pp) {
-          T f = T(0), r = T(0);
+          T y = T(0), r = T(0);
           if (q < Pe) {
             double R0 = s_vfmax0[q], F0 = s_vrmax0[q];
             if (outdeg > 0) R0 = fmax(R0, (double)a.Rbuf[vrow + q] - s_lbuf[q]);
             if (indeg > 0) F0 = fmax(F0, (double)a.Fbuf[vrow + q] - s_lbuf[q]);
-            f = (T)((double)my_MU[s_pdst[q]] - F0);
-            r = (T)((double)my_MU[s_psrc[q]] - R0);
+            const double fd = my_MU[s_pdst[q]] - F0;
+            const T f = (T)fd;
+            r = (T)(my_MU[s_psrc[q]] - R0);
+            y = (T)(fd - (double)a.dEmin[vrow + q]);  // no out-edges: -inf
             const T b = a.B[vrow + q];
             mxF[k * W + w] = fmax(mxF[k * W + w], f);
             mxR[k * W + w] = fmax(mxR[k * W + w], r);
             lr[k * W + w].add(f + b);
             lf[k * W + w].add(r + b);
           }
-          a.vf[vrow + q] = f;
+          a.vf[vrow + q] = y;
           a.vr[vrow + q] = r;
         }
       }
@@ -543,7 +548,7 @@ template <typename T>
 size_t init_smem(GroupShape gs, int pn, int pe) {
   const int GPB = kThreads / gs.G;
   return carve_bytes(pattern_ints(pn, pe), sizeof(int)) + 2 * carve_bytes(pn, sizeof(double)) +
-         3 * carve_bytes(pe, sizeof(double)) + carve_bytes((size_t)GPB * pn, sizeof(T)) +
+         3 * carve_bytes(pe, sizeof(double)) + carve_bytes((size_t)GPB * pn, sizeof(double)) +
          carve_bytes((size_t)kWarps * 6 * pe, sizeof(double));
 }
 

@@ -102,11 +102,13 @@ struct InitArgs {
   const int* d_off;
   const int* s_off;
   T* CV;               // [Dn][Pnp]: raw dV in, normalised cost out
+  T* CVlo;             // [Dn][Pnp] out: low part of the cost (FP32 only, else null)
   const T* Rbuf;       // [Dn][Pp]
   const T* Fbuf;       // [Dn][Pp]
   const T* B;          // [Dn][Pp]
-  T* vf;               // [Dn][Pp] out: VF of iteration 1
-  T* vr;               // [Dn][Pp] out: VR of iteration 1
+  const T* dEmin;      // [Dn][Pp]
+  T* vf;               // [Dn][Pp] out: Y = VF - dEmin of iteration 1 (shift 0)
+  T* vr;               // [Dn][Pp] out: Z = VR of iteration 1 (shift 0)
   const double* gv;    // [maxneg(Pn) | lse_pos(Pn) | lse_neg(Pn)]
   const double* ge;    // [Pe] LSE over covered quirk elements
   double* bpart;       // stats: mVF, mVR (max), lR, lF (lse)

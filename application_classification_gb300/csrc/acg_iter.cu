@@ -192,23 +192,24 @@ heavy_combine_kernel(const T* __restrict__ partial, const int* __restrict__ hbas
 
 // ------------------------------------------------------------------ phase B
 struct UpdSmem {
-  size_t pat, fill, lq, F, R, MU, red, stage, sM, sVF, sEM, sB, sCV, sOff, stage_bytes, total;
+  size_t pat, fill, lq, F, R, MU, red, stage, sM, sVF, sEM, sB, sCV, sCVl, sOff, stage_bytes, total;
   __host__ __device__ UpdSmem(int V, int Pn, int Pe, int Pp, int Pnp, int sz) {
     size_t o = 0;
     pat = o; o += a16(sizeof(int) * (size_t)(4 * Pe + 2 * (Pn + 1)));
     fill = o; o += a16((size_t)2 * Pp * sz);  // fillF, fillR (padded to Pp)
-    lq = o; o += a16((size_t)4 * Pp * sz);    // lF, lFlo, lR, lRlo (padded to Pp)
+    lq = o; o += a16((size_t)8 * Pp * sz);    // dF, dR, cR', cF' as hi/lo pairs (padded to Pp)
     F = o; o += a16((size_t)V * Pp * sz);
     R = o; o += a16((size_t)V * Pp * sz);
     MU = o; o += a16((size_t)V * 2 * Pn * sz);  // hi, lo
     red = o; o += a16(sizeof(double) * (size_t)kBT * 6);
-    // one stage: the tile's M, VF, dEmin, B rows, CV rows, in-degree offsets
+    // one stage: the tile's M, Y, dEmin, B rows, CV (hi, lo) rows, in-degree offsets
     size_t so = 0;
     sM = so; so += a16((size_t)V * Pp * sz);
     sVF = so; so += a16((size_t)V * Pp * sz);
     sEM = so; so += a16((size_t)V * Pp * sz);
     sB = so; so += a16((size_t)V * Pp * sz);
     sCV = so; so += a16((size_t)V * Pnp * sz);
+    sCVl = so; so += sz == 4 ? a16((size_t)V * Pnp * sz) : 0;
     sOff = so; so += a16(sizeof(int) * (size_t)(V + 1));
     stage_bytes = so;
     stage = o; o += 2 * so;
@@ -242,10 +243,14 @@ vertex_update_kernel(const VertexUpdArgs<T> a) {
   int* s_pat = reinterpret_cast<int*>(smem + L.pat);
   T* s_fillF = reinterpret_cast<T*>(smem + L.fill);
   T* s_fillR = s_fillF + Pp;
-  T* s_lF = reinterpret_cast<T*>(smem + L.lq);
-  T* s_lFlo = s_lF + Pp;
-  T* s_lR = s_lFlo + Pp;
-  T* s_lRlo = s_lR + Pp;
+  T* s_dF = reinterpret_cast<T*>(smem + L.lq);  // hi, lo of each constant
+  T* s_dFlo = s_dF + Pp;
+  T* s_dR = s_dFlo + Pp;
+  T* s_dRlo = s_dR + Pp;
+  T* s_cR = s_dRlo + Pp;
+  T* s_cRlo = s_cR + Pp;
+  T* s_cF = s_cRlo + Pp;
+  T* s_cFlo = s_cF + Pp;
   T* s_F = reinterpret_cast<T*>(smem + L.F);
   T* s_R = reinterpret_cast<T*>(smem + L.R);
   T* s_MU = reinterpret_cast<T*>(smem + L.MU);  // [V][Pn] hi then [V][Pn] lo
@@ -262,20 +267,48 @@ vertex_update_kernel(const VertexUpdArgs<T> a) {
   for (int t = tid; t < 4 * Pe + 2 * (Pn + 1); t += kBT) s_pat[t] = a.pat[t];
   __syncthreads();
   {
-    const double* g = a.glob_in;  // mVF | mVR | lR | lF | S
+    // Shifted storage: Y = VF' - dEmin - cR and Z = VR' - cF with per-q FP64
+    // shifts, so that the entries that can win a max are small numbers and an
+    // FP32 store keeps their low bits.  With dR = lR - cR, dF = lF - cF
+    // (statistics of the previous pass, in that pass's shifts):
+    //   RMax = max(fillR, Y - dR)       FMax = max(fillF, max_e(Z[s_e] - dE) - dF)
+    // New shifts for this pass's stores: lR, lF of the pass before the previous
+    // one (the iteration has period two, so that value tracks lR, lF closely);
+    // the first pass uses the previous pass's own.  Any finite shift is exact.
+    const double* g = a.glob_in;
+    const int x0 = 4 * Pe + Pn;
+    auto split = [](double x, T* hi, T* lo, int q) {
+      const T h = (T)x;
+      hi[q] = h;
+      lo[q] = (T)(x - (double)h);
+    };
     for (int q = tid; q < Pp; q += kBT) {
       if (q >= Pe) {
-        s_fillF[q] = s_fillR[q] = s_lF[q] = s_lFlo[q] = s_lR[q] = s_lRlo[q] = T(0);
+        s_fillF[q] = s_fillR[q] = T(0);
+        s_dF[q] = s_dFlo[q] = s_dR[q] = s_dRlo[q] = T(0);
+        s_cR[q] = s_cRlo[q] = s_cF[q] = s_cFlo[q] = T(0);
         continue;
       }
-      const double cR = g[4 * Pe + s_psrc[q]], cF = g[4 * Pe + s_pdst[q]];
-      s_fillF[q] = (T)(g[Pe + q] - cR);
-      s_fillR[q] = (T)(g[q] - cF);
-      const double lr = g[2 * Pe + q], lf = g[3 * Pe + q];
-      s_lR[q] = (T)lr;
-      s_lRlo[q] = (T)(lr - (double)(T)lr);
-      s_lF[q] = (T)lf;
-      s_lFlo[q] = (T)(lf - (double)(T)lf);
+      const double cRu = g[x0 + q], cFu = g[x0 + Pe + q];
+      const double dR = g[2 * Pe + q], dF = g[3 * Pe + q];
+      s_fillR[q] = (T)(g[q] + cRu - g[4 * Pe + s_pdst[q]]);
+      s_fillF[q] = (T)(g[Pe + q] + cFu - g[4 * Pe + s_psrc[q]]);
+      split(dR, s_dR, s_dRlo, q);
+      split(dF, s_dF, s_dFlo, q);
+      const double lRp = cRu + dR, lFp = cFu + dF;
+      double cRn = a.first ? lRp : g[x0 + 2 * Pe + q];
+      double cFn = a.first ? lFp : g[x0 + 3 * Pe + q];
+      if (!isfinite(cRn)) cRn = 0.0;
+      if (!isfinite(cFn)) cFn = 0.0;
+      split(cRn, s_cR, s_cRlo, q);
+      split(cFn, s_cF, s_cFlo, q);
+      if (blockIdx.x == 0) {
+        double* o = a.glob_out;
+        o[x0 + q] = (double)s_cR[q] + (double)s_cRlo[q];
+        o[x0 + Pe + q] = (double)s_cF[q] + (double)s_cFlo[q];
+        o[x0 + 2 * Pe + q] = lRp;
+        o[x0 + 3 * Pe + q] = lFp;
+      }
     }
   }
   __syncthreads();
@@ -337,6 +370,11 @@ vertex_update_kernel(const VertexUpdArgs<T> a) {
     const T* gCV = a.CV + (size_t)v0 * Pnp;
     T* sCV = reinterpret_cast<T*>(st + L.sCV);
     for (int c = tid * W; c < nv * Pnp; c += kBT * W) cp16(sCV + c, gCV + c);
+    if constexpr (sizeof(T) == 4) {
+      const T* gCVl = a.CVlo + (size_t)v0 * Pnp;
+      T* sCVl = reinterpret_cast<T*>(st + L.sCVl);
+      for (int c = tid * W; c < nv * Pnp; c += kBT * W) cp16(sCVl + c, gCVl + c);
+    }
     int* sOff = reinterpret_cast<int*>(st + L.sOff);
     for (int j = tid; j <= nv; j += kBT) cp4(sOff + j, a.d_off + v0 + j);
   };
@@ -355,33 +393,33 @@ vertex_update_kernel(const VertexUpdArgs<T> a) {
     const int v0 = tile * V;
     const int v = v0 + j0;
     const bool vok = qact && v < Dn;
-    VT bv = vfill<T>(T(0));
+    VT bv = vfill<T>(T(0)), emv = vfill<T>(T(0));
     if (vok) {
       const bool has_in = sOff[j0 + 1] > sOff[j0];
       const VT mv = has_in ? *reinterpret_cast<const VT*>(reinterpret_cast<const T*>(st + L.sM) + qoff)
                            : vfill<T>(neg_inf<T>());
-      const VT vfv = *reinterpret_cast<const VT*>(reinterpret_cast<const T*>(st + L.sVF) + qoff);
-      const VT emv = *reinterpret_cast<const VT*>(reinterpret_cast<const T*>(st + L.sEM) + qoff);
+      const VT yv = *reinterpret_cast<const VT*>(reinterpret_cast<const T*>(st + L.sVF) + qoff);
+      emv = *reinterpret_cast<const VT*>(reinterpret_cast<const T*>(st + L.sEM) + qoff);
       bv = *reinterpret_cast<const VT*>(reinterpret_cast<const T*>(st + L.sB) + qoff);
       // per-q constants of the thread's columns (16-byte shared loads)
       const VT fF = *reinterpret_cast<const VT*>(s_fillF + qv * W);
       const VT fR = *reinterpret_cast<const VT*>(s_fillR + qv * W);
-      const VT cF = *reinterpret_cast<const VT*>(s_lF + qv * W);
-      const VT cFl = *reinterpret_cast<const VT*>(s_lFlo + qv * W);
-      const VT cR = *reinterpret_cast<const VT*>(s_lR + qv * W);
-      const VT cRl = *reinterpret_cast<const VT*>(s_lRlo + qv * W);
+      const VT dF = *reinterpret_cast<const VT*>(s_dF + qv * W);
+      const VT dFl = *reinterpret_cast<const VT*>(s_dFlo + qv * W);
+      const VT dR = *reinterpret_cast<const VT*>(s_dR + qv * W);
+      const VT dRl = *reinterpret_cast<const VT*>(s_dRlo + qv * W);
       VT fo, ro;
 #pragma unroll
       for (int w = 0; w < W; ++w) {
-        // no in-edges: M = -inf; no out-edges: dEmin = +inf; the fill wins
-        vs<T>(fo, w, fmax(vg<T>(fF, w), (vg<T>(mv, w) - vg<T>(cF, w)) - vg<T>(cFl, w)));
-        vs<T>(ro, w, fmax(vg<T>(fR, w), ((vg<T>(vfv, w) - vg<T>(emv, w)) - vg<T>(cR, w)) - vg<T>(cRl, w)));
+        // no in-edges: M = -inf; no out-edges: Y = -inf; the fill wins
+        vs<T>(fo, w, fmax(vg<T>(fF, w), (vg<T>(mv, w) - vg<T>(dF, w)) - vg<T>(dFl, w)));
+        vs<T>(ro, w, fmax(vg<T>(fR, w), (vg<T>(yv, w) - vg<T>(dR, w)) - vg<T>(dRl, w)));
       }
       *reinterpret_cast<VT*>(myF) = fo;
       *reinterpret_cast<VT*>(myR) = ro;
     }
     __syncthreads();
-    // MU_raw = -CV + sum F + sum R, compensated (|terms| reach 50..100)
+    // MU_raw = -CV + sum F + sum R, compensated (CV carries a low part)
     for (int j = jp0; j < V && jp0 < prows; j += prows) {
       const int vv = v0 + j;
       if (vv >= Dn) break;
@@ -389,6 +427,8 @@ vertex_update_kernel(const VertexUpdArgs<T> a) {
       const T* rowR = s_R + j * Pp;
       CSum<T> mu;
       mu.init(-sCV[j * Pnp + pc]);
+      if constexpr (sizeof(T) == 4)
+        mu.lo = -reinterpret_cast<const T*>(st + L.sCVl)[j * Pnp + pc];
       for (int t = in0; t < in1; ++t) mu.add(rowF[s_inq[t]]);
       for (int t = out0; t < out1; ++t) mu.add(rowR[s_outq[t]]);
       s_MU[j * Pn + pc] = mu.hi;
@@ -400,28 +440,37 @@ vertex_update_kernel(const VertexUpdArgs<T> a) {
     if (!a.last && vok) {
       const VT fo = *reinterpret_cast<const VT*>(myF);
       const VT ro = *reinterpret_cast<const VT*>(myR);
+      const VT cR = *reinterpret_cast<const VT*>(s_cR + qv * W);
+      const VT cF = *reinterpret_cast<const VT*>(s_cF + qv * W);
       VT nf, nr;
 #pragma unroll
       for (int w = 0; w < W; ++w) {
+        // f = VF' - cR, r = VR' - cF; the shift is taken off the compensated
+        // MU_raw first (for the entries that matter the two are close, so the
+        // difference is exact) and the small message after
         T f, r;
         if constexpr (sizeof(T) == 4) {
-          f = (myMU[pdst[w]] - vg<T>(fo, w)) + myMUlo[pdst[w]];
-          r = (myMU[psrc[w]] - vg<T>(ro, w)) + myMUlo[psrc[w]];
+          const VT cRl = *reinterpret_cast<const VT*>(s_cRlo + qv * W);
+          const VT cFl = *reinterpret_cast<const VT*>(s_cFlo + qv * W);
+          f = ((myMU[pdst[w]] - vg<T>(cR, w)) - vg<T>(fo, w)) + (myMUlo[pdst[w]] - vg<T>(cRl, w));
+          r = ((myMU[psrc[w]] - vg<T>(cF, w)) - vg<T>(ro, w)) + (myMUlo[psrc[w]] - vg<T>(cFl, w));
         } else {
-          f = myMU[pdst[w]] - vg<T>(fo, w);
-          r = myMU[psrc[w]] - vg<T>(ro, w);
+          f = (myMU[pdst[w]] - vg<T>(cR, w)) - vg<T>(fo, w);
+          r = (myMU[psrc[w]] - vg<T>(cF, w)) - vg<T>(ro, w);
         }
+        T y;
         if (qv * W + w < Pe) {
           mxF[w] = fmax(mxF[w], f);
           mxR[w] = fmax(mxR[w], r);
           const T b = vg<T>(bv, w);
           lr[w].add_fast(f + b);
           lf[w].add_fast(r + b);
+          y = f - vg<T>(emv, w);  // no out-edges: dEmin = +inf, Y = -inf
         } else {
-          f = T(0);
+          y = T(0);
           r = T(0);
         }
-        vs<T>(nf, w, f);
+        vs<T>(nf, w, y);
         vs<T>(nr, w, r);
       }
       const size_t go = (size_t)v * Pp + (size_t)qv * W;

@@ -23,21 +23,30 @@ struct EdgeMaxArgs {
   int Pp;
 };
 
+// Column statistics of one iteration (FP64), double-buffered across iterations:
+//   [0,Pe) max_v VF'-cR | [Pe,2Pe) max_v VR'-cF | [2Pe,3Pe) dR = LSE_v(VF'-cR+B)
+//   | [3Pe,4Pe) dF = LSE_v(VR'-cF+B) | [4Pe,4Pe+Pn) S = LSE_v MU_raw
+//   | then from 4Pe+Pn: cR, cF (the shifts the stored Y, Z carry), and the
+//   absolute lR, lF of the iteration before (the next shifts).
+inline int glob_doubles(int pn, int pe) { return 8 * pe + pn; }
+
 template <typename T>
 struct VertexUpdArgs {
   const int* d_off;    // [Dn+1] (in-degree: empty rows of M are -inf)
-  const T* M;          // [Dn][Pp]
-  T* vf;               // [Dn][Pp] read then overwritten
-  T* vr_out;           // [Dn][Pp]
+  const T* M;          // [Dn][Pp] max over in-edges of Z[src] - dE
+  T* vf;               // [Dn][Pp] Y = VF' - dEmin - cR: read then overwritten
+  T* vr_out;           // [Dn][Pp] Z = VR' - cF
   const T* dEmin;      // [Dn][Pp]
   const T* B;          // [Dn][Pp]
   const T* CV;         // [Dn][Pnp]
+  const T* CVlo;       // [Dn][Pnp] low parts (FP32 only, else null)
   const double* glob_in;
+  double* glob_out;    // this iteration's shifts (block 0; the rest by stat_finalize)
   double* bpart;       // [slot][gridDim.x]
   double* mu_raw;      // [Dn][Pn] (last iteration)
   const int* pat;
   int Dn, Pn, Pe, Pp, Pnp;
-  int last;
+  int first, last;
 };
 
 struct WarpShape {

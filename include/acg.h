@@ -71,8 +71,8 @@ typedef struct acg_options {
   int32_t precision;  /* acg_precision */
   int32_t num_iters;  /* BP iterations; < 0 means pattern num_nodes, which is
                          what the reference runs (main.cu:160) */
-  int32_t kernel_timing; /* nonzero: bracket every iteration-kernel launch with
-                            CUDA events (acg_stats.ms_iter_kernels) */
+  int32_t kernel_timing; /* nonzero: bracket each iteration's edge and vertex
+                            phases with CUDA events (acg_stats.ms_*_phase) */
   int32_t reserved[5];
 } acg_options;
 
@@ -91,9 +91,13 @@ typedef struct acg_stats {
   double ms_init;
   double ms_iters;
   double bytes_iters;     /* algorithmic bytes of all iterations */
-  double bytes_per_edge_pass; /* algorithmic bytes of one iteration-kernel launch */
-  double ms_iter_kernels; /* summed duration of the iteration-kernel launches
-                             (only with acg_options.kernel_timing, else 0) */
+  double bytes_edge_phase;   /* algorithmic bytes of one edge phase: dE rows and
+                                source indices of every in-edge, each source row
+                                and each output row once */
+  double bytes_vertex_phase; /* algorithmic bytes of one vertex phase */
+  double ms_edge_phase;   /* edge phases summed over the iterations (only with
+                             acg_options.kernel_timing, else 0) */
+  double ms_vertex_phase; /* vertex phases (kernel + statistics), summed */
   int64_t launches;       /* kernels launched by the last acg_match */
   int64_t num_iters;
 } acg_stats;
