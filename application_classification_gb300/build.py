@@ -51,7 +51,7 @@ def _compile(src: Path, verbose: bool) -> Path:
     obj = BUILD / (src.name + ".o")
     if src.suffix == ".cu":
         cmd = [
-            _nvcc(), ARCH, "-lineinfo", "-O3", "-std=c++17", "-c", str(src), "-o", str(obj),
+            _nvcc(), ARCH, "-lineinfo", "-O3", "-std=c++20", "-c", str(src), "-o", str(obj),
             "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", "--expt-relaxed-constexpr",
             "-I", str(INCLUDE), "-I", str(CSRC),
         ]

@@ -83,6 +83,7 @@ struct acg_plan {
   int4* witems = nullptr;
   int nwitems = 0, wchunk = 0;
   int edge_blocks = 1, vert_blocks = 1;
+  int maxdeg = 0;  // max over pattern vertices of in- plus out-degree
   int* wsplit = nullptr;     // [edge warps + 1] item range of each edge-phase warp
   int* th_base = nullptr;    // [nheavy] first partial row
   int* th_count = nullptr;   // [nheavy] chunks
@@ -343,7 +344,8 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
     VertexUpdArgs<T> va{D->dcsr.off, (const T*)P->M, (T*)P->vf, (T*)P->vr[t & 1],
                         (const T*)P->dEmin, (const T*)P->B, (const T*)P->CV,
                         (const T*)P->CVlo, P->gi[(t - 1) & 1], P->gi[t & 1], P->bpart,
-                        mu_out, P->pat, Dn, Pn, Pe, Pp, P->Pnp, t == 1, t == P->iters};
+                        mu_out, P->pat, Dn, Pn, Pe, Pp, P->Pnp, P->maxdeg, t == 1,
+                        t == P->iters};
     ACG_TRY(launch_vertex_update<T>(va, P->vert_blocks, s));
     ACG_TRY(launch_finalize(P->bpart, P->vert_blocks, StatSpec{2 * Pe, 2 * Pe + Pn}, P->gi[t & 1], s));
     if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1) + 2], s);
@@ -562,18 +564,22 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
   if (st != ACG_OK) return fail(st);
 
   P->ws = choose_warp_shape(eb, Pp);
-  // edge phase: 6 blocks of 8 warps per SM (40 registers per thread)
-  P->edge_blocks = D->num_sms * 6;
+  // edge phase: one wave of resident blocks (8 warps each)
+  P->edge_blocks = D->num_sms * (eb == 8 ? edge_max_blocks_per_sm<double>(P->ws)
+                                         : edge_max_blocks_per_sm<float>(P->ws));
   st = build_edge_items(P.get(), P->edge_blocks * 8, s);
   if (st != ACG_OK) return fail(st);
   P->gs = choose_shape(eb, Pp, Pn);
   const int GPB = 256 / P->gs.G;
   const int nsm = D->num_sms;
   {
-    const int bps = eb == 8 ? vertex_update_blocks_per_sm<double>(Pn, Pe, Pp)
-                            : vertex_update_blocks_per_sm<float>(Pn, Pe, Pp);
-    const int V = 256 / (Pp / (16 / eb));
-    P->vert_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), V), nsm * bps));
+    const int* io = pat.data() + 2 * Pe;  // in_off, then in_q, then out_off
+    const int* oo = io + Pn + 1 + Pe;
+    int md = 0;
+    for (int p = 0; p < Pn; ++p) md = std::max(md, io[p + 1] - io[p] + oo[p + 1] - oo[p]);
+    P->maxdeg = md;
+    P->vert_blocks = eb == 8 ? vertex_update_blocks<double>(Pn, Pe, Pp, P->Pnp, md, nsm, Dn)
+                             : vertex_update_blocks<float>(Pn, Pe, Pp, P->Pnp, md, nsm, Dn);
   }
   P->row_blocks = std::max(1, std::min(ceil_div(std::max(1, std::max(P->ditems.nitems, P->sitems.nitems)), GPB), nsm * 4));
   P->init_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), GPB), nsm * 4));
@@ -592,6 +598,10 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
   alloc((size_t)Dn * P->Pnp * eb, &P->CV);
   if (P->prec == ACG_PREC_MIXED) alloc((size_t)Dn * P->Pnp * eb, &P->CVlo);
   alloc(vrow, &P->M);
+  // rows of vertices without in-edges are never written by the edge phase
+  if (st == ACG_OK)
+    st = eb == 8 ? launch_fill_neg_inf<double>((double*)P->M, (size_t)Dn * Pp, s)
+                 : launch_fill_neg_inf<float>((float*)P->M, (size_t)Dn * Pp, s);
   alloc((size_t)std::max(1, P->th_npartial) * Pp * eb, &P->part_iter);
   alloc((size_t)std::max(1, std::max(P->ditems.npartial, P->sitems.npartial)) * 4 * Pp * eb, &P->part_row);
   const size_t bp = std::max({(size_t)(6 * Pe + 2 * Pn) * P->vert_blocks,

@@ -21,7 +21,9 @@
 //   results are bit-reproducible.  No kernel waits on another block.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <limits>
 
 #include "acg_device.cuh"
 #include "acg_iter.cuh"
@@ -65,8 +67,11 @@ __device__ __forceinline__ typename VecT<T>::type vfill(T x) {
 __host__ __device__ inline size_t a16(size_t b) { return (b + 15) & ~size_t(15); }
 
 // ------------------------------------------------------------------ phase A
+#ifndef ACG_EDGE_MIN_BLOCKS
+#define ACG_EDGE_MIN_BLOCKS 1
+#endif
 template <typename T, int NPOW, int NQV>
-__global__ void __launch_bounds__(kAT)
+__global__ void __launch_bounds__(kAT, ACG_EDGE_MIN_BLOCKS)
 edge_max_kernel(const EdgeMaxArgs<T> a) {
   using VT = typename VecT<T>::type;
   constexpr int W = VecT<T>::W;
@@ -527,6 +532,308 @@ vertex_update_kernel(const VertexUpdArgs<T> a) {
   }
 }
 
+
+// ------------------------------------------------------ phase B, warp form
+// Patterns with Pp <= 64 and Pn <= 64.  Lane l owns the QPL contiguous edge
+// columns q = l * QPL + k and the pattern vertices p = l + 32 j (j < PPL); the
+// per-q constants and statistics of its columns live in registers.  Each warp
+// walks a contiguous range of vertices; their rows are staged into a per-warp
+// double-buffered ring (kVps vertices per stage) with cp.async, so a warp never
+// waits on another.  Per vertex: F, R from the staged M, Y; the compensated
+// MU_raw[p] from a per-warp shared copy of F|R through precomputed incidence
+// indices (in-edges of p ascending, then out-edges ascending -- the order of
+// the tile form); the new Y, Z from MU_raw[dst_q], MU_raw[src_q].  Vertices
+// without in-edges have M rows of -inf (set once, never written by phase A).
+constexpr int kVps = 4;  // vertices per stage
+constexpr int kVw = kBT / 32;
+
+template <typename T, int QPL, int PPL>
+struct VwSmem {
+  size_t pat, inc, ring, fr, mu, total, stage, warp_ring, oM, oY, oE, oB, oC, oCl, fr_n, mu_n;
+  __host__ __device__ VwSmem(int Pn, int Pe, int Pp, int Pnp, int maxdeg) {
+    const size_t sz = sizeof(T);
+    size_t o = 0;
+    pat = o; o += a16(sizeof(int) * (size_t)(4 * Pe + 2 * (Pn + 1)));
+    inc = o; o += a16(sizeof(int) * (size_t)PPL * maxdeg * 32);
+    size_t so = 0;  // one stage; row sizes are 16-byte multiples
+    oM = so; so += (size_t)kVps * Pp * sz;
+    oY = so; so += (size_t)kVps * Pp * sz;
+    oE = so; so += (size_t)kVps * Pp * sz;
+    oB = so; so += (size_t)kVps * Pp * sz;
+    oC = so; so += (size_t)kVps * Pnp * sz;
+    oCl = so; so += sz == 4 ? (size_t)kVps * Pnp * sz : 0;
+    stage = so;
+    warp_ring = 2 * so;
+    const size_t red = sizeof(double) * (size_t)kVw * (6 * Pe + 2 * Pn);  // aliases the rings
+    ring = o; o += a16(red > kVw * warp_ring ? red : kVw * warp_ring);
+    fr_n = 2 * 32 * QPL + 4;  // F | R | zeros
+    fr = o; o += a16((size_t)kVw * fr_n * sz);
+    mu_n = 2 * 32 * PPL;      // MU_raw hi | lo
+    mu = o; o += a16((size_t)kVw * mu_n * sz);
+    total = o;
+  }
+};
+
+template <typename T, int N>
+__device__ __forceinline__ void lds_n(const T* p, T (&x)[N]) {
+  if constexpr (N == 2 && sizeof(T) == 4) {
+    const float2 v = *reinterpret_cast<const float2*>(p);
+    x[0] = v.x;
+    x[1] = v.y;
+  } else if constexpr (N == 2 && sizeof(T) == 8) {
+    const double2 v = *reinterpret_cast<const double2*>(p);
+    x[0] = v.x;
+    x[1] = v.y;
+  } else {
+#pragma unroll
+    for (int k = 0; k < N; ++k) x[k] = p[k];
+  }
+}
+template <typename T, int N>
+__device__ __forceinline__ void st_n(T* p, const T (&x)[N]) {
+  if constexpr (N == 2 && sizeof(T) == 4) {
+    *reinterpret_cast<float2*>(p) = make_float2(x[0], x[1]);
+  } else if constexpr (N == 2 && sizeof(T) == 8) {
+    *reinterpret_cast<double2*>(p) = make_double2(x[0], x[1]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < N; ++k) p[k] = x[k];
+  }
+}
+
+template <typename T, int QPL, int PPL>
+__global__ void __launch_bounds__(kBT)
+vertex_warp_kernel(const VertexUpdArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int Pe = a.Pe, Pn = a.Pn, Pp = a.Pp, Pnp = a.Pnp, Dn = a.Dn, maxdeg = a.maxdeg;
+  const VwSmem<T, QPL, PPL> L(Pn, Pe, Pp, Pnp, maxdeg);
+  const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
+  int* s_pat = reinterpret_cast<int*>(smem + L.pat);
+  int* s_inc = reinterpret_cast<int*>(smem + L.inc);
+  for (int t = tid; t < 4 * Pe + 2 * (Pn + 1); t += kBT) s_pat[t] = a.pat[t];
+  __syncthreads();
+  const int* s_psrc = s_pat;
+  const int* s_pdst = s_pat + Pe;
+  const int* s_inoff = s_pat + 2 * Pe;
+  const int* s_inq = s_inoff + Pn + 1;
+  const int* s_outoff = s_inq + Pe;
+  const int* s_outq = s_outoff + Pn + 1;
+  constexpr int kZero = 2 * 32 * QPL;
+  // incidence index of lane l, pattern vertex p = l + 32 j, round t, at
+  // s_inc[(j * maxdeg + t) * 32 + l]: F[q] (dst_q = p), then R[q] (src_q = p),
+  // then a zero
+  for (int i = tid; i < PPL * maxdeg * 32; i += kBT) {
+    const int l = i & 31, t = (i >> 5) % maxdeg, j = (i >> 5) / maxdeg;
+    const int p = l + 32 * j;
+    int code = kZero;
+    if (p < Pn) {
+      const int nin = s_inoff[p + 1] - s_inoff[p];
+      const int nout = s_outoff[p + 1] - s_outoff[p];
+      if (t < nin)
+        code = s_inq[s_inoff[p] + t];
+      else if (t < nin + nout)
+        code = 32 * QPL + s_outq[s_outoff[p] + t - nin];
+    }
+    s_inc[i] = code;
+  }
+
+  // per-q constants of the lane's columns (see the tile form for the algebra)
+  const double* g = a.glob_in;
+  const int x0 = 4 * Pe + Pn;
+  const int qo = lane * QPL;
+  const bool qon = qo < Pp;
+  T fF[QPL], fR[QPL], dFh[QPL], dFl[QPL], dRh[QPL], dRl[QPL], cRh[QPL], cRl[QPL], cFh[QPL], cFl[QPL];
+  int qd[QPL], qs[QPL];
+#pragma unroll
+  for (int k = 0; k < QPL; ++k) {
+    const int q = qo + k;
+    fF[k] = fR[k] = dFh[k] = dFl[k] = dRh[k] = dRl[k] = cRh[k] = cRl[k] = cFh[k] = cFl[k] = T(0);
+    qd[k] = qs[k] = 0;
+    if (q < Pe) {
+      qd[k] = s_pdst[q];
+      qs[k] = s_psrc[q];
+      const double cRu = g[x0 + q], cFu = g[x0 + Pe + q];
+      const double dR = g[2 * Pe + q], dF = g[3 * Pe + q];
+      fR[k] = (T)(g[q] + cRu - g[4 * Pe + qd[k]]);
+      fF[k] = (T)(g[Pe + q] + cFu - g[4 * Pe + qs[k]]);
+      dRh[k] = (T)dR;
+      dRl[k] = (T)(dR - (double)dRh[k]);
+      dFh[k] = (T)dF;
+      dFl[k] = (T)(dF - (double)dFh[k]);
+      const double lRp = cRu + dR, lFp = cFu + dF;
+      double cRn = a.first ? lRp : g[x0 + 2 * Pe + q];
+      double cFn = a.first ? lFp : g[x0 + 3 * Pe + q];
+      if (!isfinite(cRn)) cRn = 0.0;
+      if (!isfinite(cFn)) cFn = 0.0;
+      cRh[k] = (T)cRn;
+      cRl[k] = (T)(cRn - (double)cRh[k]);
+      cFh[k] = (T)cFn;
+      cFl[k] = (T)(cFn - (double)cFh[k]);
+      if (blockIdx.x == 0 && wib == 0) {
+        double* o = a.glob_out;
+        o[x0 + q] = (double)cRh[k] + (double)cRl[k];
+        o[x0 + Pe + q] = (double)cFh[k] + (double)cFl[k];
+        o[x0 + 2 * Pe + q] = lRp;
+        o[x0 + 3 * Pe + q] = lFp;
+      }
+    }
+  }
+  T mxF[QPL], mxR[QPL];
+  OnlineLse<T> lr[QPL], lf[QPL], lmu[PPL];
+#pragma unroll
+  for (int k = 0; k < QPL; ++k) {
+    mxF[k] = mxR[k] = neg_inf<T>();
+    lr[k].init();
+    lf[k].init();
+  }
+#pragma unroll
+  for (int j = 0; j < PPL; ++j) lmu[j].init();
+  __syncthreads();  // s_inc complete
+
+  const long long nw = (long long)gridDim.x * kVw;
+  const long long gw = (long long)blockIdx.x * kVw + wib;
+  const int vb = (int)(gw * Dn / nw), ve = (int)((gw + 1) * Dn / nw);
+  unsigned char* ring = smem + L.ring + (size_t)wib * L.warp_ring;
+  T* sfr = reinterpret_cast<T*>(smem + L.fr) + (size_t)wib * L.fr_n;
+  T* smu = reinterpret_cast<T*>(smem + L.mu) + (size_t)wib * L.mu_n;
+  if (lane < 4) sfr[kZero + lane] = T(0);
+  const size_t rowb = (size_t)Pp * sizeof(T), crow = (size_t)Pnp * sizeof(T);
+  auto issue = [&](int v0, int buf) {
+    const int nv = min(kVps, ve - v0);
+    if (nv <= 0) return;
+    unsigned char* st = ring + (size_t)buf * L.stage;
+    const int n16 = (int)((size_t)nv * rowb / 16);
+    const size_t go = (size_t)v0 * rowb;
+    for (int c = lane; c < n16; c += 32) {
+      cp16(st + L.oM + c * 16, reinterpret_cast<const unsigned char*>(a.M) + go + c * 16);
+      cp16(st + L.oY + c * 16, reinterpret_cast<const unsigned char*>(a.vf) + go + c * 16);
+      cp16(st + L.oE + c * 16, reinterpret_cast<const unsigned char*>(a.dEmin) + go + c * 16);
+      cp16(st + L.oB + c * 16, reinterpret_cast<const unsigned char*>(a.B) + go + c * 16);
+    }
+    const int c16 = (int)((size_t)nv * crow / 16);
+    const size_t co = (size_t)v0 * crow;
+    for (int c = lane; c < c16; c += 32) {
+      cp16(st + L.oC + c * 16, reinterpret_cast<const unsigned char*>(a.CV) + co + c * 16);
+      if constexpr (sizeof(T) == 4)
+        cp16(st + L.oCl + c * 16, reinterpret_cast<const unsigned char*>(a.CVlo) + co + c * 16);
+    }
+  };
+  issue(vb, 0);
+  cp_commit();
+  int buf = 0;
+  for (int v0 = vb; v0 < ve; v0 += kVps, buf ^= 1) {
+    issue(v0 + kVps, buf ^ 1);  // the next stage flies while this one computes
+    cp_commit();
+    cp_wait1();
+    __syncwarp();
+    const unsigned char* st = ring + (size_t)buf * L.stage;
+    const int nv = min(kVps, ve - v0);
+    for (int jv = 0; jv < nv; ++jv) {
+      const int v = v0 + jv;
+      T F[QPL], R[QPL], em[QPL], b[QPL];
+      if (qon) {
+        T m[QPL], y[QPL];
+        lds_n<T, QPL>(reinterpret_cast<const T*>(st + L.oM) + jv * Pp + qo, m);
+        lds_n<T, QPL>(reinterpret_cast<const T*>(st + L.oY) + jv * Pp + qo, y);
+        lds_n<T, QPL>(reinterpret_cast<const T*>(st + L.oE) + jv * Pp + qo, em);
+        lds_n<T, QPL>(reinterpret_cast<const T*>(st + L.oB) + jv * Pp + qo, b);
+#pragma unroll
+        for (int k = 0; k < QPL; ++k) {
+          // no in-edges: M = -inf; no out-edges: Y = -inf; the fill wins
+          F[k] = fmax(fF[k], (m[k] - dFh[k]) - dFl[k]);
+          R[k] = fmax(fR[k], (y[k] - dRh[k]) - dRl[k]);
+        }
+        st_n<T, QPL>(sfr + qo, F);
+        st_n<T, QPL>(sfr + 32 * QPL + qo, R);
+      }
+      __syncwarp();
+      // MU_raw = -CV + sum F + sum R, compensated (CV carries a low part)
+      const T* sC = reinterpret_cast<const T*>(st + L.oC) + jv * Pnp;
+#pragma unroll
+      for (int j = 0; j < PPL; ++j) {
+        const int p = lane + 32 * j;
+        CSum<T> mu;
+        mu.init(p < Pn ? -sC[p] : T(0));
+        if constexpr (sizeof(T) == 4)
+          mu.lo = p < Pn ? -(reinterpret_cast<const T*>(st + L.oCl) + jv * Pnp)[p] : T(0);
+        const int* inc = s_inc + j * maxdeg * 32 + lane;
+        for (int t = 0; t < maxdeg; ++t) mu.add(sfr[inc[t * 32]]);
+        smu[p] = mu.hi;
+        if constexpr (sizeof(T) == 4) smu[32 * PPL + p] = mu.lo;
+        if (p < Pn) {
+          lmu[j].add2(mu.hi, mu.lo);
+          if (a.last) a.mu_raw[(size_t)v * Pn + p] = mu.dvalue();
+        }
+      }
+      __syncwarp();
+      if (!a.last && qon) {
+        T yo[QPL], zo[QPL];
+#pragma unroll
+        for (int k = 0; k < QPL; ++k) {
+          // f = VF' - cR, r = VR' - cF: the shift comes off the compensated
+          // MU_raw first, the small message after
+          T f, r;
+          if constexpr (sizeof(T) == 4) {
+            f = ((smu[qd[k]] - cRh[k]) - F[k]) + (smu[32 * PPL + qd[k]] - cRl[k]);
+            r = ((smu[qs[k]] - cFh[k]) - R[k]) + (smu[32 * PPL + qs[k]] - cFl[k]);
+          } else {
+            f = (smu[qd[k]] - cRh[k]) - F[k];
+            r = (smu[qs[k]] - cFh[k]) - R[k];
+          }
+          if (qo + k < Pe) {
+            mxF[k] = fmax(mxF[k], f);
+            mxR[k] = fmax(mxR[k], r);
+            lr[k].add_fast(f + b[k]);
+            lf[k].add_fast(r + b[k]);
+            yo[k] = f - em[k];  // no out-edges: dEmin = +inf, Y = -inf
+            zo[k] = r;
+          } else {
+            yo[k] = zo[k] = T(0);
+          }
+        }
+        st_n<T, QPL>(a.vf + (size_t)v * Pp + qo, yo);
+        st_n<T, QPL>(a.vr_out + (size_t)v * Pp + qo, zo);
+      }
+    }
+    __syncwarp();  // this stage's buffer is free for the stage after next
+  }
+  cp_wait0();
+  __syncthreads();  // the rings become the reduction area
+
+  const int nmax = 2 * Pe, nlse = 2 * Pe + Pn, slots = nmax + 2 * nlse;
+  double* red = reinterpret_cast<double*>(smem + L.ring);
+  double* r = red + (size_t)wib * slots;
+#pragma unroll
+  for (int k = 0; k < QPL; ++k) {
+    const int q = qo + k;
+    if (q < Pe) {
+      r[q] = (double)mxF[k];
+      r[Pe + q] = (double)mxR[k];
+      r[nmax + 2 * q] = lr[k].mval();
+      r[nmax + 2 * q + 1] = lr[k].sval();
+      r[nmax + 2 * (Pe + q)] = lf[k].mval();
+      r[nmax + 2 * (Pe + q) + 1] = lf[k].sval();
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < PPL; ++j) {
+    const int p = lane + 32 * j;
+    if (p < Pn) {
+      r[nmax + 2 * (2 * Pe + p)] = lmu[j].mval();
+      r[nmax + 2 * (2 * Pe + p) + 1] = lmu[j].sval();
+    }
+  }
+  __syncthreads();
+  write_block_partials(red, kVw, nmax, nlse, a.bpart, gridDim.x, blockIdx.x);
+}
+
+template <typename T>
+__global__ void fill_kernel(T* __restrict__ p, size_t n, T v) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
 #define ACG_EDGE_SHAPES(X) \
   X(1, 1) X(2, 1) X(4, 1) X(8, 1) X(16, 1) X(32, 1) X(32, 2) X(32, 4)
 
@@ -564,6 +871,20 @@ acg_status launch_edge_max(const EdgeMaxArgs<T>& a, WarpShape ws, int blocks, cu
   return set_error(ACG_ERR_UNSUPPORTED, "no edge kernel for npow=%d nqv=%d", ws.npow, ws.nqv);
 }
 
+#define ACG_EDGE_OCC(NP_, NQ_)                                                        \
+  if (ws.npow == NP_ && ws.nqv == NQ_) {                                             \
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, edge_max_kernel<T, NP_, NQ_>, \
+                                                      kAT, 0) != cudaSuccess)        \
+      nb = 1;                                                                        \
+  }
+
+template <typename T>
+int edge_max_blocks_per_sm(WarpShape ws) {
+  int nb = 1;
+  ACG_EDGE_SHAPES(ACG_EDGE_OCC)
+  return nb < 1 ? 1 : nb;
+}
+
 template <typename T>
 acg_status launch_heavy_combine(const T* partial, const int* hbase, const int* hcount,
                                 const int* hvert, int nheavy, int Pp, T* M, cudaStream_t s) {
@@ -581,13 +902,69 @@ size_t vertex_update_smem(int pn, int pe, int pp) {
   return UpdSmem(kBT / nvec, pn, pe, pp, pnp, sizeof(T)).total;
 }
 
+template <typename T, int QPL, int PPL>
+size_t vertex_warp_setup(int pn, int pe, int pp, int pnp, int maxdeg) {
+  const size_t sm = VwSmem<T, QPL, PPL>(pn, pe, pp, pnp, maxdeg).total;
+  if (sm > 48 * 1024)
+    cudaFuncSetAttribute(vertex_warp_kernel<T, QPL, PPL>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  return sm;
+}
+
+// Calls f.template operator()<QPL, PPL>() for the warp form's shape; false if
+// the pattern is too large for it.
+template <typename F>
+bool warp_form(int pn, int pp, F&& f) {
+  if (pp > 64 || pn > 64) return false;
+  if (pp <= 32 && pn <= 32) f.template operator()<1, 1>();
+  else if (pp <= 32) f.template operator()<1, 2>();
+  else if (pn <= 32) f.template operator()<2, 1>();
+  else f.template operator()<2, 2>();
+  return true;
+}
+
 template <typename T>
 acg_status launch_vertex_update(const VertexUpdArgs<T>& a, int blocks, cudaStream_t s) {
+  cudaError_t le = cudaSuccess;
+  const bool warp = warp_form(a.Pn, a.Pp, [&]<int QPL, int PPL>() {
+    const size_t sm = vertex_warp_setup<T, QPL, PPL>(a.Pn, a.Pe, a.Pp, a.Pnp, a.maxdeg);
+    vertex_warp_kernel<T, QPL, PPL><<<blocks, kBT, sm, s>>>(a);
+    le = cudaGetLastError();
+  });
+  if (warp) {
+    if (le != cudaSuccess)
+      return set_error(ACG_ERR_CUDA, "vertex_warp_kernel launch: %s", cudaGetErrorString(le));
+    return ACG_OK;
+  }
   const size_t sm = vertex_update_smem<T>(a.Pn, a.Pe, a.Pp);
   if (sm > 48 * 1024)
     ACG_CUDA_TRY(cudaFuncSetAttribute(vertex_update_kernel<T>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   vertex_update_kernel<T><<<blocks, kBT, sm, s>>>(a);
+  ACG_LAUNCH_CHECK();
+  return ACG_OK;
+}
+
+template <typename T>
+int vertex_update_blocks(int pn, int pe, int pp, int pnp, int maxdeg, int num_sms, int dn) {
+  int nb = 0;
+  const bool warp = warp_form(pn, pp, [&]<int QPL, int PPL>() {
+    const size_t sm = vertex_warp_setup<T, QPL, PPL>(pn, pe, pp, pnp, maxdeg);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, vertex_warp_kernel<T, QPL, PPL>, kBT,
+                                                      sm) != cudaSuccess)
+      nb = 1;
+  });
+  if (warp) return num_sms * (nb < 1 ? 1 : nb);
+  const int V = kBT / (pp / VecT<T>::W);
+  const long long tiles = (dn + V - 1) / V;
+  const long long b = (long long)num_sms * vertex_update_blocks_per_sm<T>(pn, pe, pp);
+  return (int)(tiles < 1 ? 1 : (tiles < b ? tiles : b));
+}
+
+template <typename T>
+acg_status launch_fill_neg_inf(T* p, size_t n, cudaStream_t s) {
+  if (n == 0) return ACG_OK;
+  fill_kernel<T><<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, s>>>(p, n, -std::numeric_limits<T>::infinity());
   ACG_LAUNCH_CHECK();
   return ACG_OK;
 }
@@ -610,6 +987,12 @@ template acg_status launch_heavy_combine<double>(const double*, const int*, cons
 template acg_status launch_heavy_combine<float>(const float*, const int*, const int*, const int*, int, int, float*, cudaStream_t);
 template acg_status launch_vertex_update<double>(const VertexUpdArgs<double>&, int, cudaStream_t);
 template acg_status launch_vertex_update<float>(const VertexUpdArgs<float>&, int, cudaStream_t);
+template int edge_max_blocks_per_sm<double>(WarpShape);
+template int edge_max_blocks_per_sm<float>(WarpShape);
+template int vertex_update_blocks<double>(int, int, int, int, int, int, int);
+template int vertex_update_blocks<float>(int, int, int, int, int, int, int);
+template acg_status launch_fill_neg_inf<double>(double*, size_t, cudaStream_t);
+template acg_status launch_fill_neg_inf<float>(float*, size_t, cudaStream_t);
 template int vertex_update_blocks_per_sm<double>(int, int, int);
 template int vertex_update_blocks_per_sm<float>(int, int, int);
 

@@ -46,6 +46,7 @@ struct VertexUpdArgs {
   double* mu_raw;      // [Dn][Pn] (last iteration)
   const int* pat;
   int Dn, Pn, Pe, Pp, Pnp;
+  int maxdeg;          // max over pattern vertices of in- plus out-degree
   int first, last;
 };
 
@@ -66,5 +67,16 @@ template <typename T>
 acg_status launch_vertex_update(const VertexUpdArgs<T>& a, int blocks, cudaStream_t s);
 template <typename T>
 int vertex_update_blocks_per_sm(int pn, int pe, int pp);
+// Grid of the vertex phase: the warp form (Pp <= 64, Pn <= 64) runs one wave
+// of resident blocks; the tile form one block per tile up to resident blocks.
+template <typename T>
+int vertex_update_blocks(int pn, int pe, int pp, int pnp, int maxdeg, int num_sms, int dn);
+// Set every element of p[0, n) to -inf (rows of vertices without in-edges).
+template <typename T>
+acg_status launch_fill_neg_inf(T* p, size_t n, cudaStream_t s);
+// Resident blocks per SM of the edge kernel for this shape (the grid is one
+// wave of them: the warp ranges are static, so every warp must be resident).
+template <typename T>
+int edge_max_blocks_per_sm(WarpShape ws);
 
 }  // namespace acg

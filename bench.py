@@ -52,13 +52,27 @@ WORKLOADS = {
 }
 
 
+def workload_info(name: str):
+    """(description, CPU-baseline sample) of a named workload."""
+    if name in WORKLOADS:
+        return WORKLOADS[name]
+    parts = name[4:].split("_") if name.startswith("rmat") else []
+    if len(parts) != 3 or not all(x.isdigit() for x in parts):
+        raise SystemExit(f"unknown workload {name!r}")
+    sc, pn, pe = (int(x) for x in parts)
+    return (f"RMAT scale {sc} (edge factor 16, a=.57 b=c=.19, dedup, no self-loops), planted "
+            f"pattern {pn} / {pe}, 13/17-dim N(0,1) features, seed {sc}",
+            f"rmat{min(sc, 14)}_{pn}_{pe}")
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="rmat22", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="rmat22",
+                    help="one of %s, or rmatS_P_E (RMAT scale S, pattern P/E)" % sorted(WORKLOADS))
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
@@ -177,7 +191,7 @@ def cpu_sample(workload: str, threads: int | None = None):
     from oracle import oracle
 
     full = _work_units(workload)
-    sample = WORKLOADS[workload][1]
+    sample = workload_info(workload)[1]
     d, p, _ = graph.workload(sample)
     nt = threads or os.cpu_count() or 1
     _, el_us = oracle.match(d, p, threads=nt, return_elapsed=True)
@@ -194,11 +208,15 @@ def _units(dn, de, pn, pe):
     return (de + dn) * max(pe, 1) * (pn + 1)
 
 
-_SHAPES = {"rmat22": (4194304, 67108864 * 0.945, 32, 64), "rmat18": (262144, 3939126, 16, 32),
+_SHAPES = {"rmat22": (4194304, 65242331, 32, 64), "rmat18": (262144, 3939126, 16, 32),
            "rmat20": (1048576, 16087353, 16, 32), "er1k": (1000, 20000, 10, 20)}
 
 
 def _work_units(workload):
+    if workload not in _SHAPES:
+        from application_classification_gb300 import graph
+        d, p, _ = graph.workload(workload)
+        _SHAPES[workload] = (d.num_nodes, d.num_edges, p.num_nodes, p.num_edges)
     dn, de, pn, pe = _SHAPES[workload]
     return _units(dn, de, pn, pe)
 
@@ -282,7 +300,7 @@ def run_ours(args, ws, rank, local):
         "warmup": args.warmup, "ms_per_step": round(ms_total / args.steps, 4),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
-        "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][0]}",
+        "config": {"workload": f"{args.workload}: {workload_info(args.workload)[0]}",
                    "data_vertices": d.num_nodes, "data_edges": d.num_edges,
                    "pattern_vertices": p.num_nodes, "pattern_edges": p.num_edges,
                    "precision": args.precision, "bp_iterations": int(st["num_iters"]),
@@ -390,7 +408,7 @@ def run_reference(args, ws, rank):
     from oracle import oracle
 
     full = _work_units(args.workload)
-    sample = WORKLOADS[args.workload][1]
+    sample = workload_info(args.workload)[1]
     d, p, _ = graph.workload(sample)
     nt = os.cpu_count() or 1
     units = _units(d.num_nodes, d.num_edges, p.num_nodes, p.num_edges)
@@ -411,7 +429,7 @@ def run_reference(args, ws, rank):
         "value": round(value, 1), "unit": "ms", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_sample, 2), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][0]}",
+        "config": {"workload": f"{args.workload}: {workload_info(args.workload)[0]}",
                    "precision": "fp64 (the reference computes in FP64)"},
         "cpu_baseline": {"value": round(value, 1), "unit": "ms", "cores": nt, "kind": "port",
                          "sample": f"{sample}: {d.num_nodes} vertices / {d.num_edges} edges, "

@@ -141,3 +141,21 @@ def test_quirk_full_coverage(cuda):
                     np.array([0, 1, 2], np.uint64), np.array([1, 2, 3], np.uint64))
     ref = oracle.match(d, p)
     assert np.abs(matcher.match(d, p) - ref).max() <= 1e-10 * max(1, np.abs(ref).max())
+
+
+# Pattern sizes that select each form of the vertex phase: the warp form with
+# one or two edge columns and one or two pattern vertices per lane, and the
+# tile form (more than 64 padded edge columns, or more than 64 pattern vertices).
+SHAPES = [(5, 7), (20, 40), (33, 32), (40, 45), (24, 100), (70, 80)]
+
+
+@pytest.mark.parametrize("pn,pe", SHAPES)
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_pattern_shapes_vs_oracle(cuda, prec, pn, pe):
+    d = graph.gen_rmat(11, 16, seed=pn + pe)
+    d, p, _, _ = graph.plant(d, pn, pe, 0.05, seed=pn)
+    ref = oracle.match(d, p)
+    mu = matcher.match(d, p, prec)
+    tol = FP64_REL * max(1.0, np.abs(ref).max()) if prec == "fp64" else MIXED_ABS
+    assert np.abs(mu - ref).max() <= tol
+    assert _argmax_same(mu, ref, tol=1e-9 if prec == "fp64" else 1e-5)
