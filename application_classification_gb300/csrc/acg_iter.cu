@@ -67,11 +67,8 @@ __device__ __forceinline__ typename VecT<T>::type vfill(T x) {
 __host__ __device__ inline size_t a16(size_t b) { return (b + 15) & ~size_t(15); }
 
 // ------------------------------------------------------------------ phase A
-#ifndef ACG_EDGE_MIN_BLOCKS
-#define ACG_EDGE_MIN_BLOCKS 1
-#endif
 template <typename T, int NPOW, int NQV>
-__global__ void __launch_bounds__(kAT, ACG_EDGE_MIN_BLOCKS)
+__global__ void __launch_bounds__(kAT)
 edge_max_kernel(const EdgeMaxArgs<T> a) {
   using VT = typename VecT<T>::type;
   constexpr int W = VecT<T>::W;
