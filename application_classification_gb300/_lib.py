@@ -67,7 +67,8 @@ class HostGraph(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("precision", i32), ("num_iters", i32), ("kernel_timing", i32),
-                ("reserved", i32 * 5)]
+                ("edge_blocks_per_sm", i32), ("vertex_blocks_per_sm", i32),
+                ("reserved", i32 * 3)]
 
 
 class Stats(C.Structure):

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <vector>
 
@@ -19,6 +20,7 @@
 #include "acg_device.cuh"
 #include "acg_internal.h"
 #include "acg_cdist.cuh"
+#include "acg_static.cuh"
 #include "acg_iter.cuh"
 
 using namespace acg;
@@ -74,21 +76,17 @@ struct acg_plan {
   const double* pv = nullptr;  // caller's pattern features (device)
   const double* pe = nullptr;
   int* pat = nullptr;          // pattern incidence (device)
-  Items ditems, sitems;      // work items of the static row passes
-  GroupShape gs{32, 1};      // group shape of the row-pass and init kernels
-  int row_blocks = 1, init_blocks = 1, cv_blocks = 1, ce_blocks = 1;
-  // work of the edge phase: items (vertices with in-edges, chunks of heavy
-  // vertices) and the heavy vertices whose chunk maxima are combined
-  WarpShape ws{32, 1};
-  int4* witems = nullptr;
-  int nwitems = 0, wchunk = 0;
-  int edge_blocks = 1, vert_blocks = 1;
+  GroupShape gs{32, 1};      // group shape of the init kernel
+  int init_blocks = 1, cv_blocks = 1, ce_blocks = 1;
+  bool init_warp = false;    // init pass in warp form (small patterns)
+  int qcov = 0, Pqc = 0;     // quirk-buffer columns holding -dE; their padded count
+  // warp work over the destination-sorted CSR (edge phase, and the quirk maxima
+  // over in-edges) and over the source-sorted CSR (static per-vertex reductions)
+  WarpShape ws{32, 1};       // edge phase and source-side pass (all Pp columns)
+  WarpShape qws{32, 1};      // destination-side quirk pass (Pqc columns)
+  WarpWork ew, sw;
+  int edge_blocks = 1, src_blocks = 1, vert_blocks = 1;
   int maxdeg = 0;  // max over pattern vertices of in- plus out-degree
-  int* wsplit = nullptr;     // [edge warps + 1] item range of each edge-phase warp
-  int* th_base = nullptr;    // [nheavy] first partial row
-  int* th_count = nullptr;   // [nheavy] chunks
-  int* th_vert = nullptr;    // [nheavy] vertex
-  int th_n = 0, th_npartial = 0;
   // work buffers (element type per precision)
   void* dE = nullptr;
   void* vf = nullptr;
@@ -97,11 +95,11 @@ struct acg_plan {
   void* B = nullptr;
   void* CV = nullptr;
   void* CVlo = nullptr;  // mixed precision: low part of CV
-  void* Rbuf = nullptr;
-  void* Fbuf = nullptr;
+  void* Rq = nullptr;         // [Dn][Pqc] quirk maxima over out-edges
+  void* Fq = nullptr;         // [Dn][Pqc] quirk maxima over in-edges
   void* M = nullptr;          // [Dn][Pp] edge-phase maxima
   void* part_iter = nullptr;
-  void* part_row = nullptr;
+  void* part_src = nullptr;   // [sw.npartial][3 Pp + Pqc] chunk rows of the source-side pass
   double* bpart = nullptr;
   double* gv = nullptr;      // [3 Pn]
   double* ge = nullptr;      // [Pe]
@@ -178,19 +176,15 @@ acg_status check_graph(const acg_graph* g, const char* what, bool need_feats) {
   return ACG_OK;
 }
 
-// Work items of the edge phase and their split over `nwarps` warps (host side,
-// from the dst-CSR offsets): every vertex with in-edges is an item; a vertex
-// whose in-edges would take a large share of one warp's work is split into
-// chunks whose maxima go to partial rows.  Item cost = load steps + overhead;
-// warp ranges are contiguous and of near-equal cost.
-acg_status build_edge_items(acg_plan* P, int nwarps, cudaStream_t s) {
-  acg_data* D = P->data;
-  const int n = D->Dn;
+}  // namespace
+
+acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* out,
+                           std::vector<DevBuf>* owned, cudaStream_t s) {
+  const int n = c.n;
   std::vector<int> off((size_t)n + 1);
-  ACG_CUDA_TRY(cudaMemcpyAsync(off.data(), D->dcsr.off, sizeof(int) * ((size_t)n + 1),
+  ACG_CUDA_TRY(cudaMemcpyAsync(off.data(), c.off, sizeof(int) * ((size_t)n + 1),
                                cudaMemcpyDeviceToHost, s));
   ACG_CUDA_TRY(cudaStreamSynchronize(s));
-  const int step = edge_step(P->ws);
   const double kOver = 3.0;  // per-item cost in steps (item load, combine, store)
   double total = 0;
   for (int v = 0; v < n; ++v) {
@@ -200,7 +194,6 @@ acg_status build_edge_items(acg_plan* P, int nwarps, cudaStream_t s) {
   const double per_warp = total / std::max(1, nwarps);
   const long long cs = std::max(4LL, (long long)(per_warp / 4));  // chunk, in steps
   const int chunk = (int)std::min<long long>(1LL << 24, cs * step);
-  P->wchunk = chunk;
   std::vector<int4> items;
   std::vector<double> cost;
   std::vector<int> hb, hc, hv;
@@ -211,16 +204,16 @@ acg_status build_edge_items(acg_plan* P, int nwarps, cudaStream_t s) {
     const int deg = off[v + 1] - off[v];
     if (deg == 0) continue;
     if (deg > chunk) {
-      const int c = (deg + chunk - 1) / chunk;
+      const int k = (deg + chunk - 1) / chunk;
       hb.push_back(npart);
-      hc.push_back(c);
+      hc.push_back(k);
       hv.push_back(v);
-      for (int j = 0; j < c; ++j) {
+      for (int j = 0; j < k; ++j) {
         const int a = off[v] + j * chunk, b = std::min(off[v + 1], a + chunk);
         items.push_back(make_int4(v, a, b, npart + j));
         cost.push_back((b - a + step - 1) / step + kOver);
       }
-      npart += c;
+      npart += k;
     } else {
       items.push_back(make_int4(v, off[v], off[v + 1], -1));
       cost.push_back((deg + step - 1) / step + kOver);
@@ -230,7 +223,7 @@ acg_status build_edge_items(acg_plan* P, int nwarps, cudaStream_t s) {
   split[0] = 0;
   {
     double acc = 0, target = 0;
-    for (double c : cost) target += c;
+    for (double x : cost) target += x;
     target /= std::max(1, nwarps);
     int w = 1;
     for (size_t i = 0; i < items.size() && w < nwarps; ++i) {
@@ -238,27 +231,33 @@ acg_status build_edge_items(acg_plan* P, int nwarps, cudaStream_t s) {
       while (w < nwarps && acc >= target * w) split[w++] = (int)i + 1;
     }
   }
-  P->nwitems = (int)items.size();
-  P->th_n = (int)hv.size();
-  P->th_npartial = npart;
-  ACG_TRY(dev_alloc(&P->owned, sizeof(int4) * items.size(), (void**)&P->witems, s));
-  ACG_TRY(dev_alloc(&P->owned, sizeof(int) * split.size(), (void**)&P->wsplit, s));
-  ACG_TRY(dev_alloc(&P->owned, sizeof(int) * hv.size(), (void**)&P->th_base, s));
-  ACG_TRY(dev_alloc(&P->owned, sizeof(int) * hv.size(), (void**)&P->th_count, s));
-  ACG_TRY(dev_alloc(&P->owned, sizeof(int) * hv.size(), (void**)&P->th_vert, s));
+  WarpWork& W = *out;
+  W = WarpWork{};
+  W.nitems = (int)items.size();
+  W.nwarps = nwarps;
+  W.chunk = chunk;
+  W.nheavy = (int)hv.size();
+  W.npartial = npart;
+  ACG_TRY(dev_alloc(owned, sizeof(int4) * std::max<size_t>(1, items.size()), (void**)&W.items, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * split.size(), (void**)&W.wsplit, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * std::max<size_t>(1, hv.size()), (void**)&W.hbase, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * std::max<size_t>(1, hv.size()), (void**)&W.hcount, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * std::max<size_t>(1, hv.size()), (void**)&W.hvert, s));
   if (!items.empty())
-    ACG_CUDA_TRY(cudaMemcpyAsync(P->witems, items.data(), sizeof(int4) * items.size(),
+    ACG_CUDA_TRY(cudaMemcpyAsync(W.items, items.data(), sizeof(int4) * items.size(),
                                  cudaMemcpyHostToDevice, s));
-  ACG_CUDA_TRY(cudaMemcpyAsync(P->wsplit, split.data(), sizeof(int) * split.size(),
+  ACG_CUDA_TRY(cudaMemcpyAsync(W.wsplit, split.data(), sizeof(int) * split.size(),
                                cudaMemcpyHostToDevice, s));
   if (!hv.empty()) {
-    ACG_CUDA_TRY(cudaMemcpyAsync(P->th_base, hb.data(), sizeof(int) * hb.size(), cudaMemcpyHostToDevice, s));
-    ACG_CUDA_TRY(cudaMemcpyAsync(P->th_count, hc.data(), sizeof(int) * hc.size(), cudaMemcpyHostToDevice, s));
-    ACG_CUDA_TRY(cudaMemcpyAsync(P->th_vert, hv.data(), sizeof(int) * hv.size(), cudaMemcpyHostToDevice, s));
+    ACG_CUDA_TRY(cudaMemcpyAsync(W.hbase, hb.data(), sizeof(int) * hb.size(), cudaMemcpyHostToDevice, s));
+    ACG_CUDA_TRY(cudaMemcpyAsync(W.hcount, hc.data(), sizeof(int) * hc.size(), cudaMemcpyHostToDevice, s));
+    ACG_CUDA_TRY(cudaMemcpyAsync(W.hvert, hv.data(), sizeof(int) * hv.size(), cudaMemcpyHostToDevice, s));
   }
   ACG_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die here
   return ACG_OK;
 }
+
+namespace {
 
 template <typename T>
 acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
@@ -272,55 +271,31 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
   // ---- cdist (ac.hxx:33-56 via main.cu:109-110) + column stats
   ACG_TRY(Cdist<T>::run(P, D, lim, s));
   cudaEventRecord(P->ev[1], s);
-  // ---- static per-vertex reductions
-  {
-    RowPassArgs<T> a{};
-    a.items = P->sitems.items;
-    a.nitems = P->sitems.nitems;
-    a.row_of = D->pos_in_dst;
-    a.eid_of_row = D->dcsr.eid;
-    a.dE = (const T*)P->dE;
-    a.partial = (T*)P->part_row;
-    a.hbase = P->sitems.hbase;
-    a.hcount = P->sitems.hcount;
-    a.hvert = P->sitems.hvert;
-    a.nheavy = P->sitems.nheavy;
-    a.chunk = P->sitems.chunk;
-    a.off = D->scsr.off;
-    a.out_min = (T*)P->dEmin;
-    a.out_lse = (T*)P->B;
-    a.out_buf = (T*)P->Rbuf;
-    a.De = De;
-    a.lim = lim;
-    a.Dn = Dn;
-    a.Pe = Pe;
-    a.Pp = Pp;
-    a.src_mode = 1;
-    ACG_TRY(launch_row_pass<T>(a, P->gs, P->row_blocks, false, s));
-    ACG_TRY(launch_row_pass<T>(a, P->gs, P->row_blocks, true, s));
-    a.items = P->ditems.items;
-    a.nitems = P->ditems.nitems;
-    a.row_of = nullptr;
-    a.hbase = P->ditems.hbase;
-    a.hcount = P->ditems.hcount;
-    a.hvert = P->ditems.hvert;
-    a.nheavy = P->ditems.nheavy;
-    a.chunk = P->ditems.chunk;
-    a.off = D->dcsr.off;
-    a.out_min = nullptr;
-    a.out_lse = nullptr;
-    a.out_buf = (T*)P->Fbuf;
-    a.src_mode = 0;
-    ACG_TRY(launch_row_pass<T>(a, P->gs, P->row_blocks, false, s));
-    ACG_TRY(launch_row_pass<T>(a, P->gs, P->row_blocks, true, s));
-    P->launches += 2 + (P->sitems.nheavy > 0) + (P->ditems.nheavy > 0);
+  // ---- static per-vertex reductions (acg_static.cu)
+  if (De > 0) {
+    SrcStatsArgs<T> sa{P->sw.items, P->sw.nitems, P->sw.wsplit, D->pos_in_dst, D->scsr.eid,
+                       (const T*)P->dE, (T*)P->dEmin, (T*)P->B, (T*)P->Rq,
+                       (T*)P->part_src, De, lim, Pp, P->Pqc, P->qcov};
+    ACG_TRY(launch_src_stats<T>(sa, P->ws, P->src_blocks, s));
+    ACG_TRY(launch_src_stats_combine<T>(sa, P->sw, s));
+    DstQuirkArgs<T> qa{P->ew.items, P->ew.nitems, P->ew.wsplit, D->dcsr.eid, (const T*)P->dE,
+                       (T*)P->Fq, (T*)P->part_iter, De, lim, Pp, P->Pqc, P->qcov};
+    ACG_TRY(launch_dst_quirk<T>(qa, P->qws, P->edge_blocks, s));
+    if (P->qcov > 0)
+      ACG_TRY(launch_heavy_combine<T>((const T*)P->part_iter, P->ew.hbase, P->ew.hcount,
+                                      P->ew.hvert, P->ew.nheavy, P->Pqc, (T*)P->Fq, s));
+    P->launches += 2 + (P->sw.nheavy > 0) + (P->qcov > 0 && P->ew.nheavy > 0);
   }
   // ---- init vertex pass
   {
-    InitArgs<T> a{D->dcsr.off, D->scsr.off, (T*)P->CV, (T*)P->CVlo, (const T*)P->Rbuf,
-                  (const T*)P->Fbuf, (const T*)P->B, (const T*)P->dEmin, (T*)P->vf,
-                  (T*)P->vr[0], P->gv, P->ge, P->bpart, P->pat, De, lim, Dn, Pn, Pe, Pp, P->Pnp};
-    ACG_TRY(launch_init_vertex<T>(a, P->gs, P->init_blocks, s));
+    InitArgs<T> a{D->dcsr.off, D->scsr.off, (T*)P->CV, (T*)P->CVlo, (const T*)P->Rq,
+                  (const T*)P->Fq, (const T*)P->B, (const T*)P->dEmin, (T*)P->vf,
+                  (T*)P->vr[0], P->gv, P->ge, P->bpart, P->pat, De, lim, Dn, Pn, Pe, Pp,
+                  P->Pnp, P->Pqc, P->qcov};
+    if (P->init_warp)
+      ACG_TRY(launch_init_warp<T>(a, P->init_blocks, s));
+    else
+      ACG_TRY(launch_init_vertex<T>(a, P->gs, P->init_blocks, s));
     // S = 0 (MU0 is normalised) and shifts 0 for the first pass
     ACG_CUDA_TRY(cudaMemsetAsync(P->gi[0] + 4 * Pe, 0,
                                  sizeof(double) * (glob_doubles(Pn, Pe) - 4 * Pe), s));
@@ -332,13 +307,13 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
   for (int t = 1; t <= P->iters; ++t) {
     if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1)], s);
     if (Pe > 0) {
-      EdgeMaxArgs<T> ea{P->witems, P->nwitems, P->wsplit, D->dcsr.other,
+      EdgeMaxArgs<T> ea{P->ew.items, P->ew.nitems, P->ew.wsplit, D->dcsr.other,
                         (const T*)P->dE, (const T*)P->vr[(t - 1) & 1], (T*)P->M,
                         (T*)P->part_iter, Pp};
       ACG_TRY(launch_edge_max<T>(ea, P->ws, P->edge_blocks, s));
-      ACG_TRY(launch_heavy_combine<T>((const T*)P->part_iter, P->th_base, P->th_count,
-                                      P->th_vert, P->th_n, Pp, (T*)P->M, s));
-      P->launches += 1 + (P->th_n > 0);
+      ACG_TRY(launch_heavy_combine<T>((const T*)P->part_iter, P->ew.hbase, P->ew.hcount,
+                                      P->ew.hvert, P->ew.nheavy, Pp, (T*)P->M, s));
+      P->launches += 1 + (P->ew.nheavy > 0);
     }
     if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1) + 1], s);
     VertexUpdArgs<T> va{D->dcsr.off, (const T*)P->M, (T*)P->vf, (T*)P->vr[t & 1],
@@ -559,16 +534,25 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
 
   if (P->prec == ACG_PREC_MIXED) st = ensure_f32(D, s);
   if (st != ACG_OK) return fail(st);
-  st = build_items(D->dcsr, kChunk, &P->ditems, &P->owned, s);
-  if (st == ACG_OK) st = build_items(D->scsr, kChunk, &P->sitems, &P->owned, s);
-  if (st != ACG_OK) return fail(st);
 
   P->ws = choose_warp_shape(eb, Pp);
   // edge phase: one wave of resident blocks (8 warps each)
-  P->edge_blocks = D->num_sms * (eb == 8 ? edge_max_blocks_per_sm<double>(P->ws)
-                                         : edge_max_blocks_per_sm<float>(P->ws));
-  st = build_edge_items(P.get(), P->edge_blocks * 8, s);
+  {
+    const int fit = eb == 8 ? edge_max_blocks_per_sm<double>(P->ws) : edge_max_blocks_per_sm<float>(P->ws);
+    P->edge_blocks = D->num_sms * (o.edge_blocks_per_sm > 0 ? std::min(fit, o.edge_blocks_per_sm) : fit);
+  }
+  st = build_warp_work(D->dcsr, P->edge_blocks * 8, edge_step(P->ws), &P->ew, &P->owned, s);
   if (st != ACG_OK) return fail(st);
+  // source-side static pass: one wave of resident blocks over the source CSR
+  {
+    const int fit = eb == 8 ? src_stats_blocks_per_sm<double>(P->ws) : src_stats_blocks_per_sm<float>(P->ws);
+    P->src_blocks = D->num_sms * (o.edge_blocks_per_sm > 0 ? std::min(fit, o.edge_blocks_per_sm) : fit);
+  }
+  st = build_warp_work(D->scsr, P->src_blocks * 8, edge_step(P->ws), &P->sw, &P->owned, s);
+  if (st != ACG_OK) return fail(st);
+  P->qcov = quirk_columns((long long)Pn * Dn, De, Pe);
+  P->Pqc = std::max(W, (P->qcov + W - 1) / W * W);
+  P->qws = choose_warp_shape(eb, P->Pqc);
   P->gs = choose_shape(eb, Pp, Pn);
   const int GPB = 256 / P->gs.G;
   const int nsm = D->num_sms;
@@ -580,9 +564,18 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
     P->maxdeg = md;
     P->vert_blocks = eb == 8 ? vertex_update_blocks<double>(Pn, Pe, Pp, P->Pnp, md, nsm, Dn)
                              : vertex_update_blocks<float>(Pn, Pe, Pp, P->Pnp, md, nsm, Dn);
+    if (o.vertex_blocks_per_sm > 0)
+      P->vert_blocks = std::min(P->vert_blocks, nsm * o.vertex_blocks_per_sm);
   }
-  P->row_blocks = std::max(1, std::min(ceil_div(std::max(1, std::max(P->ditems.nitems, P->sitems.nitems)), GPB), nsm * 4));
   P->init_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), GPB), nsm * 4));
+  {
+    const int ib = eb == 8 ? init_warp_blocks<double>(Pn, Pe, Pp, nsm)
+                           : init_warp_blocks<float>(Pn, Pe, Pp, nsm);
+    if (ib > 0) {
+      P->init_warp = true;
+      P->init_blocks = ib;
+    }
+  }
   P->cv_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), 64), nsm * 2));
   P->ce_blocks = std::max(1, std::min(ceil_div(std::max(1, De), 64), nsm * 2));
 
@@ -593,17 +586,33 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
   alloc(vrow, &P->vr[1]);
   alloc(vrow, &P->dEmin);
   alloc(vrow, &P->B);
-  alloc(vrow, &P->Rbuf);
-  alloc(vrow, &P->Fbuf);
+  alloc((size_t)Dn * P->Pqc * eb, &P->Rq);
+  alloc((size_t)Dn * P->Pqc * eb, &P->Fq);
   alloc((size_t)Dn * P->Pnp * eb, &P->CV);
   if (P->prec == ACG_PREC_MIXED) alloc((size_t)Dn * P->Pnp * eb, &P->CVlo);
   alloc(vrow, &P->M);
   // rows of vertices without in-edges are never written by the edge phase
   if (st == ACG_OK)
-    st = eb == 8 ? launch_fill_neg_inf<double>((double*)P->M, (size_t)Dn * Pp, s)
-                 : launch_fill_neg_inf<float>((float*)P->M, (size_t)Dn * Pp, s);
-  alloc((size_t)std::max(1, P->th_npartial) * Pp * eb, &P->part_iter);
-  alloc((size_t)std::max(1, std::max(P->ditems.npartial, P->sitems.npartial)) * 4 * Pp * eb, &P->part_row);
+    st = eb == 8 ? launch_fill<double>((double*)P->M, (size_t)Dn * Pp, -std::numeric_limits<double>::infinity(), s)
+                 : launch_fill<float>((float*)P->M, (size_t)Dn * Pp, -std::numeric_limits<float>::infinity(), s);
+  alloc((size_t)std::max(1, P->ew.npartial) * Pp * eb, &P->part_iter);
+  alloc((size_t)std::max(1, P->sw.npartial) * (3 * Pp + P->Pqc) * eb, &P->part_src);
+  // rows of vertices without out-edges (in-edges) are never written by the
+  // static passes: dEmin = +inf, B = -inf (and -inf quirk maxima, unused)
+  if (st == ACG_OK) {
+    const size_t nv = (size_t)Dn * Pp, nq = (size_t)Dn * P->Pqc;
+    if (eb == 8) {
+      st = launch_fill<double>((double*)P->dEmin, nv, std::numeric_limits<double>::infinity(), s);
+      if (st == ACG_OK) st = launch_fill<double>((double*)P->B, nv, -std::numeric_limits<double>::infinity(), s);
+      if (st == ACG_OK) st = launch_fill<double>((double*)P->Rq, nq, -std::numeric_limits<double>::infinity(), s);
+      if (st == ACG_OK) st = launch_fill<double>((double*)P->Fq, nq, -std::numeric_limits<double>::infinity(), s);
+    } else {
+      st = launch_fill<float>((float*)P->dEmin, nv, std::numeric_limits<float>::infinity(), s);
+      if (st == ACG_OK) st = launch_fill<float>((float*)P->B, nv, -std::numeric_limits<float>::infinity(), s);
+      if (st == ACG_OK) st = launch_fill<float>((float*)P->Rq, nq, -std::numeric_limits<float>::infinity(), s);
+      if (st == ACG_OK) st = launch_fill<float>((float*)P->Fq, nq, -std::numeric_limits<float>::infinity(), s);
+    }
+  }
   const size_t bp = std::max({(size_t)(6 * Pe + 2 * Pn) * P->vert_blocks,
                               (size_t)5 * Pn * P->cv_blocks, (size_t)2 * Pe * P->ce_blocks,
                               (size_t)6 * Pe * P->init_blocks});
@@ -674,7 +683,7 @@ acg_status acg_plan_stats(acg_plan* P, acg_stats* out) {
   // work items.  Vertex phase: M, Y, dEmin, B and CV (with its low part in
   // mixed precision) read, Y and Z written, the in-degree offsets.
   const double cvb = P->prec == ACG_PREC_MIXED ? 2.0 * eb : eb;
-  out->bytes_edge_phase = De * (Pe * eb + 4.0) + 2.0 * Dn * Pe * eb + (double)P->nwitems * 16.0;
+  out->bytes_edge_phase = De * (Pe * eb + 4.0) + 2.0 * Dn * Pe * eb + (double)P->ew.nitems * 16.0;
   out->bytes_vertex_phase = Dn * (4.0 * Pe * eb + Pn * cvb + 2.0 * Pe * eb + 4.0);
   out->bytes_iters = (out->bytes_edge_phase + out->bytes_vertex_phase) * P->iters;
   out->launches = P->launches;

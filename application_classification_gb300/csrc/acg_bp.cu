@@ -176,116 +176,6 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kNPV = 4;  // pattern vertices per lane: Pn <= 4 * G
 
-// ----------------------------------------------------------- cdist (SIMT)
-// Difference form sqrt(sum_k (x_k - y_k)^2), as ac.hxx:33-56, computed in T
-// from features stored as F (the caller's FP64 arrays, or the data graph's
-// FP32 copy for the mixed path, so that no FP64->FP32 conversion -- which runs
-// at the FP64 rate on GB300 -- happens per pair).
-template <typename T, typename F>
-__global__ void __launch_bounds__(256)
-cdist_v_kernel(const CdistVArgs<T, F> a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int Pn = a.Pn, Kv = a.Kv;
-  T* s_pv = reinterpret_cast<T*>(smem);
-  double* s_red = reinterpret_cast<double*>(smem + carve_bytes((size_t)Pn * Kv, sizeof(T)));
-  for (int t = threadIdx.x; t < Pn * Kv; t += blockDim.x) s_pv[t] = (T)a.pv[t];
-  __syncthreads();
-  const int R = 256 / Pn;  // vertices per block step
-  const int p = threadIdx.x % Pn, rl = threadIdx.x / Pn;
-  double mx = -CUDART_INF;
-  OnlineLse<double> lp, ln;
-  lp.init();
-  ln.init();
-  if (rl < R) {
-    for (long long v = (long long)blockIdx.x * R + rl; v < a.Dn; v += (long long)gridDim.x * R) {
-      const F* x = a.dv + (size_t)v * a.kstride;
-      const T* y = s_pv + p * Kv;
-      T acc = T(0);
-      for (int k = 0; k < Kv; ++k) {
-        const T d = y[k] - (T)__ldg(x + k);
-        acc += d * d;
-      }
-      const T dist = sqrt(acc);
-      a.dV[(size_t)v * a.Pnp + p] = dist;
-      const double dd = (double)dist;
-      mx = fmax(mx, -dd);
-      lp.add(dd);
-      ln.add(-dd);
-    }
-  }
-  // per-p block reduction over the R rows, in row order
-  double* red = s_red;  // [R][Pn][5]
-  if (rl < R) {
-    red[(rl * Pn + p) * 5 + 0] = mx;
-    red[(rl * Pn + p) * 5 + 1] = lp.m;
-    red[(rl * Pn + p) * 5 + 2] = lp.s;
-    red[(rl * Pn + p) * 5 + 3] = ln.m;
-    red[(rl * Pn + p) * 5 + 4] = ln.s;
-  }
-  __syncthreads();
-  for (int pp = threadIdx.x; pp < Pn; pp += blockDim.x) {
-    double m = -CUDART_INF, am = -CUDART_INF, as = 0.0, bm = -CUDART_INF, bs = 0.0;
-    for (int r = 0; r < R; ++r) {
-      const double* e = red + (r * Pn + pp) * 5;
-      m = fmax(m, e[0]);
-      lse_merge(am, as, e[1], e[2]);
-      lse_merge(bm, bs, e[3], e[4]);
-    }
-    const int nmax = Pn;
-    a.bpart[(size_t)pp * gridDim.x + blockIdx.x] = m;
-    a.bpart[(size_t)(nmax + 2 * pp) * gridDim.x + blockIdx.x] = am;
-    a.bpart[(size_t)(nmax + 2 * pp + 1) * gridDim.x + blockIdx.x] = as;
-    a.bpart[(size_t)(nmax + 2 * (Pn + pp)) * gridDim.x + blockIdx.x] = bm;
-    a.bpart[(size_t)(nmax + 2 * (Pn + pp) + 1) * gridDim.x + blockIdx.x] = bs;
-  }
-}
-
-template <typename T, typename F>
-__global__ void __launch_bounds__(256)
-cdist_e_kernel(const CdistEArgs<T, F> a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int Pe = a.Pe, Pp = a.Pp, Ke = a.Ke;
-  T* s_pe = reinterpret_cast<T*>(smem);
-  double* s_red = reinterpret_cast<double*>(smem + carve_bytes((size_t)Pe * Ke, sizeof(T)));
-  for (int t = threadIdx.x; t < Pe * Ke; t += blockDim.x) s_pe[t] = (T)a.pe[t];
-  __syncthreads();
-  const int R = 256 / Pp;
-  const int q = threadIdx.x % Pp, rl = threadIdx.x / Pp;
-  OnlineLse<double> lb;
-  lb.init();
-  if (rl < R) {
-    const long long qbase = (long long)q * a.De;
-    for (long long i = (long long)blockIdx.x * R + rl; i < a.De; i += (long long)gridDim.x * R) {
-      T dist = T(0);
-      if (q < Pe) {
-        const int e = __ldg(a.eid + i);
-        const F* x = a.ef + (size_t)(a.gather ? e : i) * a.kstride;
-        const T* y = s_pe + q * Ke;
-        T acc = T(0);
-        for (int k = 0; k < Ke; ++k) {
-          const T d = y[k] - (T)__ldg(x + k);
-          acc += d * d;
-        }
-        dist = sqrt(acc);
-        if (qbase + e < a.lim) lb.add(-(double)dist);
-      }
-      a.dE[(size_t)i * Pp + q] = dist;
-    }
-  }
-  double* red = s_red;  // [R][Pp][2]
-  if (rl < R) {
-    red[(rl * Pp + q) * 2 + 0] = lb.m;
-    red[(rl * Pp + q) * 2 + 1] = lb.s;
-  }
-  __syncthreads();
-  for (int qq = threadIdx.x; qq < Pe; qq += blockDim.x) {
-    double m = -CUDART_INF, s = 0.0;
-    for (int r = 0; r < R; ++r) lse_merge(m, s, red[(r * Pp + qq) * 2], red[(r * Pp + qq) * 2 + 1]);
-    a.bpart[(size_t)(2 * qq) * gridDim.x + blockIdx.x] = m;
-    a.bpart[(size_t)(2 * qq + 1) * gridDim.x + blockIdx.x] = s;
-  }
-}
-
 // dst[i][k] = (float)src[row ? row[i] : i][k], zero padding to kstride.
 __global__ void convert_rows_kernel(const double* __restrict__ src, const int* __restrict__ row,
                                     long long n, int K, float* __restrict__ dst, int kstride) {
@@ -296,123 +186,6 @@ __global__ void convert_rows_kernel(const double* __restrict__ src, const int* _
   float x = 0.f;
   if (k < K) x = __double2float_rn(src[(size_t)(row ? row[i] : i) * K + k]);
   dst[t] = x;
-}
-
-// ------------------------------------------------------ static row passes
-// HEAVY = false: every work item; a chunk of a heavy vertex writes its partial
-// (min, lse m, lse s, quirk max) rows and stops.  HEAVY = true: one group per
-// heavy vertex combines its partial rows in chunk order and writes the outputs.
-template <typename T, int G, int NQV, bool HEAVY>
-__global__ void __launch_bounds__(kThreads)
-row_pass_kernel(const RowPassArgs<T> a) {
-  using VT = typename Vec<T>::type;
-  constexpr int W = Vec<T>::W;
-  constexpr int NQ = NQV * W;
-  constexpr int GPB = kThreads / G;
-  const int Pp = a.Pp;
-  const Grp<G> gr;
-  const int gib = threadIdx.x / G;
-  const int gstride = gridDim.x * GPB;
-  const int nwork = HEAVY ? a.nheavy : a.nitems;
-  for (int it = blockIdx.x * GPB + gib; it < nwork; it += gstride) {
-    T mn[NQ], bx[NQ];
-    double lm[NQ], lsum[NQ];
-#pragma unroll
-    for (int k = 0; k < NQ; ++k) {
-      mn[k] = pos_inf<T>();
-      bx[k] = neg_inf<T>();
-      lm[k] = -CUDART_INF;
-      lsum[k] = 0.0;
-    }
-    int v;
-    if constexpr (HEAVY) {
-      v = __ldg(a.hvert + it);
-      const T* p0 = a.partial + (size_t)__ldg(a.hbase + it) * 4 * Pp;
-      const int cnt = __ldg(a.hcount + it);
-      for (int r = 0; r < cnt; ++r) {
-        const T* pr = p0 + (size_t)r * 4 * Pp;
-#pragma unroll
-        for (int k = 0; k < NQV; ++k)
-#pragma unroll
-          for (int w = 0; w < W; ++w) {
-            const int q = (gr.lig + G * k) * W + w;
-            if (q < Pp) {
-              mn[k * W + w] = fmin(mn[k * W + w], __ldcg(pr + q));
-              lse_merge(lm[k * W + w], lsum[k * W + w], (double)__ldcg(pr + Pp + q),
-                        (double)__ldcg(pr + 2 * Pp + q));
-              bx[k * W + w] = fmax(bx[k * W + w], __ldcg(pr + 3 * Pp + q));
-            }
-          }
-      }
-    } else {
-      const int4 item = a.items[it];
-      v = item.x;
-      const int i0 = item.y, i1 = item.z, h = item.w;
-      OnlineLse<T> ls[NQ];
-#pragma unroll
-      for (int k = 0; k < NQ; ++k) ls[k].init();
-      for (int j = i0; j < i1; ++j) {
-        const int r = a.src_mode ? __ldg(a.row_of + j) : j;
-        const long long e = __ldg(a.eid_of_row + r);
-        const VT* row = reinterpret_cast<const VT*>(a.dE + (size_t)r * Pp);
-#pragma unroll
-        for (int k = 0; k < NQV; ++k) {
-          const int qv = gr.lig + G * k;
-          if (qv * W < Pp) {
-            const VT x = __ldg(row + qv);
-#pragma unroll
-            for (int w = 0; w < W; ++w) {
-              const int q = qv * W + w;
-              const T d = lane_of<T>(x, w);
-              const T buf = ((long long)q * a.De + e < a.lim) ? -d : T(0);
-              bx[k * W + w] = fmax(bx[k * W + w], buf);
-              if (a.src_mode) {
-                mn[k * W + w] = fmin(mn[k * W + w], d);
-                ls[k * W + w].add(-d);
-              }
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < NQ; ++k) {
-        lm[k] = ls[k].mval();
-        lsum[k] = ls[k].sval();
-      }
-      if (h >= 0) {
-        const int c = (i0 - __ldg(a.off + v)) / a.chunk;
-        T* prow = a.partial + (size_t)(__ldg(a.hbase + h) + c) * 4 * Pp;
-#pragma unroll
-        for (int k = 0; k < NQV; ++k)
-#pragma unroll
-          for (int w = 0; w < W; ++w) {
-            const int q = (gr.lig + G * k) * W + w;
-            if (q < Pp) {
-              prow[q] = mn[k * W + w];
-              prow[Pp + q] = (T)lm[k * W + w];
-              prow[2 * Pp + q] = (T)lsum[k * W + w];
-              prow[3 * Pp + q] = bx[k * W + w];
-            }
-          }
-        continue;
-      }
-    }
-    const size_t vrow = (size_t)v * Pp;
-#pragma unroll
-    for (int k = 0; k < NQV; ++k)
-#pragma unroll
-      for (int w = 0; w < W; ++w) {
-        const int q = (gr.lig + G * k) * W + w;
-        if (q < Pp) {
-          a.out_buf[vrow + q] = bx[k * W + w];
-          if (a.src_mode) {
-            a.out_min[vrow + q] = mn[k * W + w];
-            const double m = lm[k * W + w], s = lsum[k * W + w];
-            a.out_lse[vrow + q] = (m > -CUDART_INF && s > 0.0) ? (T)(m + log(s)) : neg_inf<T>();
-          }
-        }
-      }
-  }
 }
 
 // ------------------------------------------------------ init vertex pass
@@ -493,8 +266,9 @@ init_vertex_kernel(const InitArgs<T> a) {
           T y = T(0), r = T(0);
           if (q < Pe) {
             double R0 = s_vfmax0[q], F0 = s_vrmax0[q];
-            if (outdeg > 0) R0 = fmax(R0, (double)a.Rbuf[vrow + q] - s_lbuf[q]);
-            if (indeg > 0) F0 = fmax(F0, (double)a.Fbuf[vrow + q] - s_lbuf[q]);
+            const size_t qrow = (size_t)v * a.Pqc + q;
+            if (outdeg > 0) R0 = fmax(R0, (q < a.qcov ? (double)a.Rq[qrow] : 0.0) - s_lbuf[q]);
+            if (indeg > 0) F0 = fmax(F0, (q < a.qcov ? (double)a.Fq[qrow] : 0.0) - s_lbuf[q]);
             const double fd = my_MU[s_pdst[q]] - F0;
             const T f = (T)fd;
             r = (T)(my_MU[s_psrc[q]] - R0);
@@ -577,24 +351,6 @@ GroupShape choose_shape(int elem_bytes, int pp, int pn) {
   return gs;
 }
 
-#define ACG_ROW_CASE(G_, N_)                                                            \
-  if (gs.G == G_ && gs.NQV == N_) {                                                     \
-    if (heavy)                                                                          \
-      row_pass_kernel<T, G_, N_, true><<<blocks, kThreads, 0, s>>>(a);                  \
-    else                                                                                \
-      row_pass_kernel<T, G_, N_, false><<<blocks, kThreads, 0, s>>>(a);                 \
-    ACG_LAUNCH_CHECK();                                                                 \
-    return ACG_OK;                                                                      \
-  }
-
-template <typename T>
-acg_status launch_row_pass(const RowPassArgs<T>& a, GroupShape gs, int blocks, bool heavy,
-                           cudaStream_t s) {
-  if ((heavy ? a.nheavy : a.nitems) == 0) return ACG_OK;
-  ACG_SHAPES(ACG_ROW_CASE)
-  return set_error(ACG_ERR_UNSUPPORTED, "no row-pass kernel for G=%d NQV=%d", gs.G, gs.NQV);
-}
-
 #define ACG_INIT_CASE(G_, N_)                                                           \
   if (gs.G == G_ && gs.NQV == N_) {                                                     \
     const size_t sm = init_smem<T>(gs, a.Pn, a.Pe);                                     \
@@ -621,28 +377,6 @@ acg_status launch_finalize(const double* bpart, int nblocks, StatSpec spec, doub
   return ACG_OK;
 }
 
-template <typename T, typename F>
-acg_status launch_cdist_v(const CdistVArgs<T, F>& a, int blocks, cudaStream_t s) {
-  const int R = 256 / a.Pn;
-  const size_t sm = carve_bytes((size_t)a.Pn * a.Kv, sizeof(T)) + sizeof(double) * (size_t)R * a.Pn * 5;
-  if (sm > 48 * 1024)
-    cudaFuncSetAttribute(cdist_v_kernel<T, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  cdist_v_kernel<T, F><<<blocks, 256, sm, s>>>(a);
-  ACG_LAUNCH_CHECK();
-  return ACG_OK;
-}
-
-template <typename T, typename F>
-acg_status launch_cdist_e(const CdistEArgs<T, F>& a, int blocks, cudaStream_t s) {
-  const int R = 256 / a.Pp;
-  const size_t sm = carve_bytes((size_t)a.Pe * a.Ke, sizeof(T)) + sizeof(double) * (size_t)R * a.Pp * 2;
-  if (sm > 48 * 1024)
-    cudaFuncSetAttribute(cdist_e_kernel<T, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  cdist_e_kernel<T, F><<<blocks, 256, sm, s>>>(a);
-  ACG_LAUNCH_CHECK();
-  return ACG_OK;
-}
-
 acg_status launch_convert_rows(const double* src, const int* row, long long n, int K, float* dst,
                                int kstride, cudaStream_t s) {
   const long long tot = n * kstride;
@@ -660,13 +394,7 @@ acg_status launch_mu_output(double* mu, const double* S, long long Dn, int Pn, c
   return ACG_OK;
 }
 
-template acg_status launch_row_pass<double>(const RowPassArgs<double>&, GroupShape, int, bool, cudaStream_t);
-template acg_status launch_row_pass<float>(const RowPassArgs<float>&, GroupShape, int, bool, cudaStream_t);
 template acg_status launch_init_vertex<double>(const InitArgs<double>&, GroupShape, int, cudaStream_t);
 template acg_status launch_init_vertex<float>(const InitArgs<float>&, GroupShape, int, cudaStream_t);
-template acg_status launch_cdist_v<double, double>(const CdistVArgs<double, double>&, int, cudaStream_t);
-template acg_status launch_cdist_v<float, float>(const CdistVArgs<float, float>&, int, cudaStream_t);
-template acg_status launch_cdist_e<double, double>(const CdistEArgs<double, double>&, int, cudaStream_t);
-template acg_status launch_cdist_e<float, float>(const CdistEArgs<float, float>&, int, cudaStream_t);
 
 }  // namespace acg

@@ -35,67 +35,9 @@ GroupShape choose_shape(int elem_bytes, int pp, int pn);
 acg_status launch_finalize(const double* bpart, int nblocks, StatSpec spec, double* out,
                            cudaStream_t s);
 
-// ---- initialisation kernels
-// F: element type of the stored features (double: the caller's arrays;
-// float: the data graph's FP32 copy used by the mixed path).
-template <typename T, typename F>
-struct CdistVArgs {
-  const F* dv;       // [Dn][kstride]
-  const double* pv;  // [Pn][Kv]
-  T* dV;             // [Dn][Pnp] raw distances (normalised in place by init_vertex)
-  double* bpart;     // stats: max(-dV) (Pn), LSE(dV) (Pn), LSE(-dV) (Pn)
-  int Dn, Pn, Kv, kstride, Pnp;
-};
-template <typename T, typename F>
-acg_status launch_cdist_v(const CdistVArgs<T, F>& a, int blocks, cudaStream_t s);
-
-template <typename T, typename F>
-struct CdistEArgs {
-  const F* ef;        // features: gather ? [De][kstride] original order : dst-CSR order
-  const int* eid;     // [De] original edge id at each dst-CSR position
-  const double* pe;   // [Pe][Ke]
-  T* dE;              // [De][Pp] out, dst-CSR order
-  double* bpart;      // stats: LSE over covered elements of -dE (Pe)
-  long long De;
-  int Pe, Pp, Ke, kstride;
-  int gather;         // 1: row = eid[i]; 0: row = i
-  long long lim;      // Pn * Dn: flat positions below it hold -dE in the quirk buffer
-};
-template <typename T, typename F>
-acg_status launch_cdist_e(const CdistEArgs<T, F>& a, int blocks, cudaStream_t s);
-
 // dst[i][k] = (float)src[row ? row[i] : i][k] for k < K, zero up to kstride.
 acg_status launch_convert_rows(const double* src, const int* row, long long n, int K, float* dst,
                                int kstride, cudaStream_t s);
-
-// Static per-vertex reductions over a CSR of dE rows.
-//   src mode: dEmin, B = LSE(-dE), Rbuf = max of the quirk buffer, over out-edges
-//   dst mode: Fbuf = max of the quirk buffer, over in-edges
-template <typename T>
-struct RowPassArgs {
-  const int4* items;
-  int nitems;
-  const int* row_of;  // src mode: dst-CSR row of each src-CSR position; dst mode: null
-  const int* eid_of_row;  // [De] original edge id of each dst-CSR row
-  const T* dE;
-  T* partial;         // [npartial][4][Pp]
-  const int* hbase;
-  const int* hcount;
-  const int* hvert;
-  int nheavy;
-  int chunk;
-  const int* off;     // CSR offsets (for chunk index)
-  T* out_min;         // src: dEmin
-  T* out_lse;         // src: B
-  T* out_buf;         // src: Rbuf, dst: Fbuf
-  long long De;
-  long long lim;
-  int Dn, Pe, Pp;
-  int src_mode;
-};
-template <typename T>
-acg_status launch_row_pass(const RowPassArgs<T>& a, GroupShape gs, int blocks, bool heavy,
-                           cudaStream_t s);
 
 template <typename T>
 struct InitArgs {
@@ -103,8 +45,8 @@ struct InitArgs {
   const int* s_off;
   T* CV;               // [Dn][Pnp]: raw dV in, normalised cost out
   T* CVlo;             // [Dn][Pnp] out: low part of the cost (FP32 only, else null)
-  const T* Rbuf;       // [Dn][Pp]
-  const T* Fbuf;       // [Dn][Pp]
+  const T* Rq;         // [Dn][Pqc] quirk maximum over out-edges, columns < qcov
+  const T* Fq;         // [Dn][Pqc] quirk maximum over in-edges, columns < qcov
   const T* B;          // [Dn][Pp]
   const T* dEmin;      // [Dn][Pp]
   T* vf;               // [Dn][Pp] out: Y = VF - dEmin of iteration 1 (shift 0)
@@ -116,6 +58,7 @@ struct InitArgs {
   long long De;
   long long lim;
   int Dn, Pn, Pe, Pp, Pnp;
+  int Pqc, qcov;       // (the later quirk columns are zero over any edge)
 };
 template <typename T>
 acg_status launch_init_vertex(const InitArgs<T>& a, GroupShape gs, int blocks, cudaStream_t s);

@@ -282,88 +282,4 @@ acg_status build_csr(const uint32_t* key, const uint32_t* other, int n, int m, C
   return st;
 }
 
-// ---------------------------------------------------------------- items
-namespace {
-
-__global__ void item_counts_kernel(const int* __restrict__ off, int n, int chunk,
-                                   uint32_t* __restrict__ nch, uint32_t* __restrict__ heavy,
-                                   uint32_t* __restrict__ hch) {
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= n) return;
-  const int deg = off[v + 1] - off[v];
-  const int c = deg <= chunk ? 1 : (deg + chunk - 1) / chunk;
-  nch[v] = (uint32_t)c;
-  heavy[v] = c > 1 ? 1u : 0u;
-  hch[v] = c > 1 ? (uint32_t)c : 0u;
-}
-
-__global__ void item_fill_kernel(const int* __restrict__ off, int n, int chunk,
-                                 const uint32_t* __restrict__ item_off,
-                                 const uint32_t* __restrict__ hidx,
-                                 const uint32_t* __restrict__ hrow, int4* __restrict__ items,
-                                 int* __restrict__ hbase, int* __restrict__ hcount,
-                                 int* __restrict__ hvert) {
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= n) return;
-  const int i0 = off[v], i1 = off[v + 1];
-  const int deg = i1 - i0;
-  const int c = deg <= chunk ? 1 : (deg + chunk - 1) / chunk;
-  const int h = c > 1 ? (int)hidx[v] : -1;
-  if (h >= 0) {
-    hbase[h] = (int)hrow[v];
-    hcount[h] = c;
-    hvert[h] = v;
-  }
-  const uint32_t base = item_off[v];
-  for (int j = 0; j < c; ++j) {
-    const int a = i0 + j * chunk;
-    const int b = c > 1 ? min(i1, a + chunk) : i1;
-    items[base + j] = make_int4(v, a, b, h);
-  }
-}
-
-}  // namespace
-
-acg_status build_items(const Csr& csr, int chunk, Items* out, std::vector<DevBuf>* owned,
-                       cudaStream_t s) {
-  const int n = csr.n;
-  out->chunk = chunk;
-  if (n == 0) {
-    out->nitems = out->nheavy = out->npartial = 0;
-    ACG_TRY(dev_alloc(owned, 16, (void**)&out->items, s));
-    ACG_TRY(dev_alloc(owned, 16, (void**)&out->hbase, s));
-    ACG_TRY(dev_alloc(owned, 16, (void**)&out->hcount, s));
-    ACG_TRY(dev_alloc(owned, 16, (void**)&out->hvert, s));
-    return ACG_OK;
-  }
-  const size_t nn = (size_t)n + 1;  // one extra slot so the scan yields totals
-  uint32_t* tmp = nullptr;
-  ACG_CUDA_TRY(cudaMallocAsync((void**)&tmp, 3 * nn * sizeof(uint32_t), s));
-  uint32_t *nch = tmp, *heavy = tmp + nn, *hch = tmp + 2 * nn;
-  cudaMemsetAsync(tmp, 0, 3 * nn * sizeof(uint32_t), s);
-  item_counts_kernel<<<ceil_div(n, 256), 256, 0, s>>>(csr.off, n, chunk, nch, heavy, hch);
-  ACG_LAUNCH_CHECK();
-  ACG_TRY(scan_exclusive_u32(nch, nch, nn, s));
-  ACG_TRY(scan_exclusive_u32(heavy, heavy, nn, s));
-  ACG_TRY(scan_exclusive_u32(hch, hch, nn, s));
-  uint32_t tot[3];
-  ACG_CUDA_TRY(cudaMemcpyAsync(&tot[0], nch + n, 4, cudaMemcpyDeviceToHost, s));
-  ACG_CUDA_TRY(cudaMemcpyAsync(&tot[1], heavy + n, 4, cudaMemcpyDeviceToHost, s));
-  ACG_CUDA_TRY(cudaMemcpyAsync(&tot[2], hch + n, 4, cudaMemcpyDeviceToHost, s));
-  ACG_CUDA_TRY(cudaStreamSynchronize(s));
-  out->nitems = (int)tot[0];
-  out->nheavy = (int)tot[1];
-  out->npartial = (int)tot[2];
-  ACG_TRY(dev_alloc(owned, sizeof(int4) * (size_t)out->nitems, (void**)&out->items, s));
-  ACG_TRY(dev_alloc(owned, sizeof(int) * (size_t)out->nheavy, (void**)&out->hbase, s));
-  ACG_TRY(dev_alloc(owned, sizeof(int) * (size_t)out->nheavy, (void**)&out->hcount, s));
-  ACG_TRY(dev_alloc(owned, sizeof(int) * (size_t)out->nheavy, (void**)&out->hvert, s));
-  item_fill_kernel<<<ceil_div(n, 256), 256, 0, s>>>(csr.off, n, chunk, nch, heavy, hch,
-                                                    out->items, out->hbase, out->hcount,
-                                                    out->hvert);
-  ACG_LAUNCH_CHECK();
-  cudaFreeAsync(tmp, s);
-  return ACG_OK;
-}
-
 }  // namespace acg

@@ -28,20 +28,27 @@ struct Csr {
   int* other = nullptr;    // [m] the other endpoint at each position
 };
 
-// Work items of one CSR: item = {vertex, first position, end position, heavy
-// vertex index or -1}.  A vertex with more than `chunk` edges is split into
-// ceil(deg / chunk) items that each reduce into a partial row; a second launch
-// combines each heavy vertex's rows (no waiting, no atomics).
-struct Items {
-  int4* items = nullptr;   // [nitems]
+// Work of a warp-per-item segmented pass over one CSR (built on the host from
+// its offsets): item = {vertex, first position, end position, partial row or
+// -1}; warp w does items [wsplit[w], wsplit[w+1]), contiguous and of near-equal
+// cost (load steps + a per-item overhead).  A vertex whose edges would take a
+// large share of one warp's work is split into chunks that reduce into partial
+// rows; heavy vertex h owns partial rows [hbase[h], hbase[h] + hcount[h]),
+// combined afterwards in chunk order (no atomics: results are deterministic).
+struct WarpWork {
+  int4* items = nullptr;
   int nitems = 0;
-  int chunk = 0;
-  int nheavy = 0;          // vertices split into chunks
-  int npartial = 0;        // partial rows = total chunks of heavy vertices
-  int* hbase = nullptr;    // [nheavy] first partial row of heavy vertex h
-  int* hcount = nullptr;   // [nheavy] number of chunks of heavy vertex h
-  int* hvert = nullptr;    // [nheavy] vertex id of heavy vertex h
+  int* wsplit = nullptr;   // [nwarps + 1]
+  int nwarps = 0;
+  int chunk = 0;           // positions per chunk
+  int* hbase = nullptr;
+  int* hcount = nullptr;
+  int* hvert = nullptr;
+  int nheavy = 0, npartial = 0;
 };
+// `step` = positions one warp loads per step of its pass (the cost unit).
+acg_status build_warp_work(const Csr& c, int nwarps, int step, WarpWork* out,
+                           std::vector<DevBuf>* owned, cudaStream_t s);
 
 // ---- primitives (acg_csr.cu)
 // Exclusive scan of n uint32 values (in and out may alias); stream ordered.
@@ -53,9 +60,6 @@ acg_status radix_sort_pairs_u32(uint32_t* keys, uint32_t* vals, uint32_t* keys_t
 // Build the CSR grouping edges by `key[e]` (the other endpoint is `other[e]`).
 acg_status build_csr(const uint32_t* key, const uint32_t* other, int n, int m, Csr* out,
                      std::vector<DevBuf>* owned, cudaStream_t s);
-// Work items for a CSR with the given chunk length (synchronises `s`).
-acg_status build_items(const Csr& csr, int chunk, Items* out, std::vector<DevBuf>* owned,
-                       cudaStream_t s);
 
 // Allocate `bytes` (>= 1) of device memory, zero it, record it in `owned`.
 acg_status dev_alloc(std::vector<DevBuf>* owned, size_t bytes, void** out, cudaStream_t s);

@@ -67,8 +67,11 @@ __device__ __forceinline__ typename VecT<T>::type vfill(T x) {
 __host__ __device__ inline size_t a16(size_t b) { return (b + 15) & ~size_t(15); }
 
 // ------------------------------------------------------------------ phase A
+// (An explicit minimum of one block per SM lets the compiler keep more of the
+// pipelined loads in registers: 72 registers and 3 blocks/SM measured faster
+// than 56 registers and 4 blocks/SM at RMAT-22, 4.47 ms against 5.30 ms.)
 template <typename T, int NPOW, int NQV>
-__global__ void __launch_bounds__(kAT)
+__global__ void __launch_bounds__(kAT, 1)
 edge_max_kernel(const EdgeMaxArgs<T> a) {
   using VT = typename VecT<T>::type;
   constexpr int W = VecT<T>::W;
@@ -959,9 +962,9 @@ int vertex_update_blocks(int pn, int pe, int pp, int pnp, int maxdeg, int num_sm
 }
 
 template <typename T>
-acg_status launch_fill_neg_inf(T* p, size_t n, cudaStream_t s) {
+acg_status launch_fill(T* p, size_t n, T v, cudaStream_t s) {
   if (n == 0) return ACG_OK;
-  fill_kernel<T><<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, s>>>(p, n, -std::numeric_limits<T>::infinity());
+  fill_kernel<T><<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, s>>>(p, n, v);
   ACG_LAUNCH_CHECK();
   return ACG_OK;
 }
@@ -988,8 +991,8 @@ template int edge_max_blocks_per_sm<double>(WarpShape);
 template int edge_max_blocks_per_sm<float>(WarpShape);
 template int vertex_update_blocks<double>(int, int, int, int, int, int, int);
 template int vertex_update_blocks<float>(int, int, int, int, int, int, int);
-template acg_status launch_fill_neg_inf<double>(double*, size_t, cudaStream_t);
-template acg_status launch_fill_neg_inf<float>(float*, size_t, cudaStream_t);
+template acg_status launch_fill<double>(double*, size_t, double, cudaStream_t);
+template acg_status launch_fill<float>(float*, size_t, float, cudaStream_t);
 template int vertex_update_blocks_per_sm<double>(int, int, int);
 template int vertex_update_blocks_per_sm<float>(int, int, int);
 

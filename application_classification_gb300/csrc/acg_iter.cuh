@@ -71,9 +71,9 @@ int vertex_update_blocks_per_sm(int pn, int pe, int pp);
 // of resident blocks; the tile form one block per tile up to resident blocks.
 template <typename T>
 int vertex_update_blocks(int pn, int pe, int pp, int pnp, int maxdeg, int num_sms, int dn);
-// Set every element of p[0, n) to -inf (rows of vertices without in-edges).
+// Set every element of p[0, n) to v.
 template <typename T>
-acg_status launch_fill_neg_inf(T* p, size_t n, cudaStream_t s);
+acg_status launch_fill(T* p, size_t n, T v, cudaStream_t s);
 // Resident blocks per SM of the edge kernel for this shape (the grid is one
 // wave of them: the warp ranges are static, so every warp must be resident).
 template <typename T>

@@ -1,0 +1,658 @@
+// acg_static.cu -- the static per-vertex reductions of a match.
+//
+// The reference builds, once per match, the quirk buffers and their edge
+// maxima (main.cu:113-114, 135-146: RowSoftmax2 + EdgeMaxReduce2_t over the
+// negated cost matrix); the restructured iteration also needs, per data vertex
+// v and pattern edge q, dEmin = min over v's out-edges of dE and
+// B = log sum over v's out-edges of exp(-dE).  Both sides are segmented
+// reductions over a CSR and use the edge phase's structure (acg_iter.cu):
+// one warp per work item, lanes = (edge slot, 16-byte column), kU loads per
+// slot issued back to back with the next step's row indices in flight,
+// static cost-balanced warp ranges, hubs split into chunks whose partial rows
+// are combined in chunk order.
+//   src_stats_kernel  out-edges (source-sorted CSR, dE rows gathered from
+//                     their destination-sorted position): dEmin, B, and the
+//                     quirk maximum of the columns q < qcov
+//   dst_quirk_kernel  in-edges (consecutive destination-sorted rows): the
+//                     quirk maximum of the columns q < qcov only; the other
+//                     columns of the quirk buffer are all zero
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "acg_bp.cuh"
+#include "acg_device.cuh"
+#include "acg_static.cuh"
+
+namespace acg {
+
+namespace {
+
+constexpr int kST = 256;  // threads per block (the edge phase's warp work uses 8 warps per block)
+constexpr int kSU = 4;    // load steps issued back to back (the edge phase's kU)
+
+template <typename T>
+struct SV;
+template <>
+struct SV<double> {
+  using type = double2;
+  static constexpr int W = 2;
+};
+template <>
+struct SV<float> {
+  using type = float4;
+  static constexpr int W = 4;
+};
+template <typename T>
+__device__ __forceinline__ T sg(const typename SV<T>::type& v, int w) {
+  return reinterpret_cast<const T*>(&v)[w];
+}
+template <typename T>
+__device__ __forceinline__ typename SV<T>::type sfill(T x) {
+  typename SV<T>::type r;
+#pragma unroll
+  for (int w = 0; w < SV<T>::W; ++w) reinterpret_cast<T*>(&r)[w] = x;
+  return r;
+}
+
+__device__ __forceinline__ float exp_fast(float x) { return __expf(x); }
+__device__ __forceinline__ double exp_fast(double x) { return exp(x); }
+template <typename T>
+__device__ __forceinline__ void kahan_add(T& s, T& c, T x) {
+  const T y = x - c;
+  const T t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+// (m, s) log-sum-exp pairs: s = sum exp(x - m); m = -inf means empty.
+template <typename T>
+__device__ __forceinline__ void lse_pair_merge(T& m, T& s, T m2, T s2) {
+  if (!(m2 > neg_inf<T>()) || !(s2 > T(0))) return;
+  if (!(m > neg_inf<T>()) || !(s > T(0))) {
+    m = m2;
+    s = s2;
+    return;
+  }
+  if (m2 > m) {
+    s = s * dev_exp(m - m2) + s2;
+    m = m2;
+  } else {
+    s += s2 * dev_exp(m2 - m);
+  }
+}
+
+template <typename T, int NPOW, int NQV>
+__global__ void __launch_bounds__(kST, 1)
+src_stats_kernel(const SrcStatsArgs<T> a) {
+  using VT = typename SV<T>::type;
+  constexpr int W = SV<T>::W;
+  constexpr int S = 32 / NPOW;
+  constexpr int NQ = NQV * W;
+  constexpr int STEP = S * kSU;
+  const int Pp = a.Pp, Pqc = a.Pqc, qcov = a.qcov;
+  const int lane = threadIdx.x & 31;
+  const int slot = lane / NPOW, qc = lane % NPOW;
+  const int gw = (blockIdx.x * kST + threadIdx.x) >> 5;
+  const int it_end = __ldg(a.wsplit + gw + 1);
+  int it = __ldg(a.wsplit + gw);
+  if (it >= it_end) return;
+
+  int4 item = __ldg(a.items + it);
+  int4 item_next = it + 1 < it_end ? __ldg(a.items + it + 1) : make_int4(0, 0, 0, -1);
+  int base = item.y;
+  int ridx[kSU], eidx[kSU];
+#pragma unroll
+  for (int u = 0; u < kSU; ++u) {
+    const int e = base + slot + S * u;
+    const bool ok = e < item.z;
+    ridx[u] = ok ? __ldg(a.row_of + e) : 0;
+    eidx[u] = ok ? __ldg(a.eid + e) : 0;
+  }
+  // Per column: the running minimum mn of dE, and sum_i exp(mn - dE_i) (with
+  // a compensation term) rescaled when the minimum moves, so that
+  // B = -mn + log(sum) takes one exponential per element.
+  T mn[NQ], qx[NQ], sm[NQ], sc[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    mn[k] = pos_inf<T>();
+    qx[k] = neg_inf<T>();
+    sm[k] = T(0);
+    sc[k] = T(0);
+  }
+  for (;;) {
+    VT x[kSU][NQV];
+    bool okv[kSU];
+    int ecur[kSU];
+#pragma unroll
+    for (int u = 0; u < kSU; ++u) {
+      const int e = base + slot + S * u;
+      okv[u] = e < item.z;
+      ecur[u] = eidx[u];
+#pragma unroll
+      for (int k = 0; k < NQV; ++k) {
+        const int qv = qc + NPOW * k;
+        x[u][k] = (okv[u] && qv * W < Pp)
+                      ? __ldg(reinterpret_cast<const VT*>(a.dE + (size_t)ridx[u] * Pp) + qv)
+                      : sfill<T>(pos_inf<T>());
+      }
+    }
+    const bool item_done = base + STEP >= item.z;
+    int nbase = base + STEP, nend = item.z;
+    bool more = true;
+    if (item_done) {
+      more = it + 1 < it_end;
+      nbase = item_next.y;
+      nend = item_next.z;
+    }
+#pragma unroll
+    for (int u = 0; u < kSU; ++u) {
+      const int e = nbase + slot + S * u;
+      const bool ok = more && e < nend;
+      ridx[u] = ok ? __ldg(a.row_of + e) : 0;
+      eidx[u] = ok ? __ldg(a.eid + e) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kSU; ++u) {
+      if (!okv[u]) continue;
+#pragma unroll
+      for (int k = 0; k < NQV; ++k)
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+          const int q = (qc + NPOW * k) * W + w;
+          const T d = sg<T>(x[u][k], w);
+          const int j = k * W + w;
+          if (d < mn[j]) {  // new minimum (rare after the first few elements)
+            const T f = mn[j] < pos_inf<T>() ? exp_fast(d - mn[j]) : T(0);
+            sm[j] *= f;
+            sc[j] *= f;
+            mn[j] = d;
+            kahan_add(sm[j], sc[j], T(1));
+          } else if (d < pos_inf<T>()) {
+            kahan_add(sm[j], sc[j], exp_fast(mn[j] - d));
+          }
+          if (q < qcov) {
+            const bool covered = (long long)q * a.De + ecur[u] < a.lim;
+            qx[k * W + w] = fmax(qx[k * W + w], covered ? -d : T(0));
+          }
+        }
+    }
+    if (item_done) {
+      T lm[NQ], lsum[NQ];  // (max, sum) of exp(-dE): max = -mn
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        lm[k] = -mn[k];
+        lsum[k] = sm[k] - sc[k];
+      }
+#pragma unroll
+      for (int o = NPOW; o < 32; o <<= 1)
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) {
+          mn[k] = fmin(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+          qx[k] = fmax(qx[k], __shfl_xor_sync(0xffffffffu, qx[k], o));
+          const T m2 = __shfl_xor_sync(0xffffffffu, lm[k], o);
+          const T s2 = __shfl_xor_sync(0xffffffffu, lsum[k], o);
+          lse_pair_merge<T>(lm[k], lsum[k], m2, s2);
+        }
+      if (slot == 0) {
+        const int v = item.x;
+#pragma unroll
+        for (int k = 0; k < NQV; ++k)
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            const int q = (qc + NPOW * k) * W + w;
+            if (q >= Pp) continue;
+            const int j = k * W + w;
+            if (item.w >= 0) {
+              T* pr = a.partial + (size_t)item.w * (3 * Pp + Pqc);
+              pr[q] = mn[j];
+              pr[Pp + q] = lm[j];
+              pr[2 * Pp + q] = lsum[j];
+              if (q < Pqc) pr[3 * Pp + q] = qx[j];
+            } else {
+              a.dEmin[(size_t)v * Pp + q] = mn[j];
+              a.B[(size_t)v * Pp + q] =
+                  (lm[j] > neg_inf<T>() && lsum[j] > T(0)) ? lm[j] + dev_log(lsum[j]) : neg_inf<T>();
+              if (q < Pqc) a.Rq[(size_t)v * Pqc + q] = qx[j];
+            }
+          }
+      }
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        mn[k] = pos_inf<T>();
+        qx[k] = neg_inf<T>();
+        sm[k] = T(0);
+        sc[k] = T(0);
+      }
+      if (!more) break;
+      ++it;
+      item = item_next;
+      item_next = it + 1 < it_end ? __ldg(a.items + it + 1) : make_int4(0, 0, 0, -1);
+    }
+    base = nbase;
+  }
+}
+
+// One warp per heavy vertex: its chunk rows merged in chunk order (FP64).
+template <typename T>
+__global__ void __launch_bounds__(256)
+src_stats_combine_kernel(const SrcStatsArgs<T> a, const int* __restrict__ hbase,
+                         const int* __restrict__ hcount, const int* __restrict__ hvert,
+                         int nheavy) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= nheavy) return;
+  const int Pp = a.Pp, Pqc = a.Pqc;
+  const size_t rs = (size_t)3 * Pp + Pqc;
+  const T* p0 = a.partial + (size_t)hbase[warp] * rs;
+  const int cnt = hcount[warp];
+  const size_t v = (size_t)hvert[warp];
+  for (int q = lane; q < Pp; q += 32) {
+    T mn = pos_inf<T>(), qx = neg_inf<T>();
+    double m = -CUDART_INF, s = 0.0;
+    for (int r = 0; r < cnt; ++r) {
+      const T* pr = p0 + (size_t)r * rs;
+      mn = fmin(mn, pr[q]);
+      lse_merge(m, s, (double)pr[Pp + q], (double)pr[2 * Pp + q]);
+      if (q < Pqc) qx = fmax(qx, pr[3 * Pp + q]);
+    }
+    a.dEmin[v * Pp + q] = mn;
+    a.B[v * Pp + q] = (m > -CUDART_INF && s > 0.0) ? (T)(m + log(s)) : neg_inf<T>();
+    if (q < Pqc) a.Rq[v * Pqc + q] = qx;
+  }
+}
+
+template <typename T, int NPOW, int NQV>
+__global__ void __launch_bounds__(kST)
+dst_quirk_kernel(const DstQuirkArgs<T> a) {
+  using VT = typename SV<T>::type;
+  constexpr int W = SV<T>::W;
+  constexpr int S = 32 / NPOW;
+  constexpr int NQ = NQV * W;
+  constexpr int STEP = S * kSU;
+  const int Pp = a.Pp, Pqc = a.Pqc, qcov = a.qcov;
+  const int lane = threadIdx.x & 31;
+  const int slot = lane / NPOW, qc = lane % NPOW;
+  const int gw = (blockIdx.x * kST + threadIdx.x) >> 5;
+  const int it_end = __ldg(a.wsplit + gw + 1);
+  int it = __ldg(a.wsplit + gw);
+  if (it >= it_end) return;
+  int4 item = __ldg(a.items + it);
+  int base = item.y;
+  T qx[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) qx[k] = neg_inf<T>();
+  for (;;) {
+    VT x[kSU][NQV];
+    int ev[kSU];
+    bool okv[kSU];
+#pragma unroll
+    for (int u = 0; u < kSU; ++u) {
+      const int e = base + slot + S * u;
+      okv[u] = e < item.z;
+      ev[u] = okv[u] ? __ldg(a.eid + e) : 0;
+#pragma unroll
+      for (int k = 0; k < NQV; ++k) {
+        const int qv = qc + NPOW * k;
+        x[u][k] = (okv[u] && qv * W < Pqc)
+                      ? __ldcs(reinterpret_cast<const VT*>(a.dE + (size_t)e * Pp) + qv)
+                      : sfill<T>(pos_inf<T>());
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kSU; ++u) {
+      if (!okv[u]) continue;
+#pragma unroll
+      for (int k = 0; k < NQV; ++k)
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+          const int q = (qc + NPOW * k) * W + w;
+          if (q < qcov) {
+            const bool covered = (long long)q * a.De + ev[u] < a.lim;
+            qx[k * W + w] = fmax(qx[k * W + w], covered ? -sg<T>(x[u][k], w) : T(0));
+          }
+        }
+    }
+    if (base + STEP >= item.z) {
+#pragma unroll
+      for (int o = NPOW; o < 32; o <<= 1)
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) qx[k] = fmax(qx[k], __shfl_xor_sync(0xffffffffu, qx[k], o));
+      if (slot == 0) {
+        T* row = item.w >= 0 ? a.partial + (size_t)item.w * Pqc : a.Fq + (size_t)item.x * Pqc;
+#pragma unroll
+        for (int k = 0; k < NQV; ++k)
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            const int q = (qc + NPOW * k) * W + w;
+            if (q < Pqc) row[q] = qx[k * W + w];
+          }
+      }
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) qx[k] = neg_inf<T>();
+      if (++it >= it_end) break;
+      item = __ldg(a.items + it);
+      base = item.y;
+    } else {
+      base += STEP;
+    }
+  }
+}
+
+// ------------------------------------------------------------ init, warp form
+// The first VF, VR of the iteration loop and their statistics (main.cu:112-133,
+// 135-146, 165-176): CV = dV - LSE_v(dV), MU0 = -dV - LSE_v(-dV), RMax0 / FMax0
+// from the quirk-buffer maxima, Y = VF' - dEmin and Z = VR' (shift 0).  Lanes
+// own fixed columns as in the vertex phase's warp form (QPL edge columns,
+// PPL pattern vertices); each warp walks a contiguous vertex range with the
+// next vertex's rows loaded while the current one is computed.  In FP32 the
+// FP64 constants enter as hi/lo pairs and CV, MU0 are formed with TwoSum, so
+// that no per-element arithmetic runs at the FP64 rate.
+template <typename T>
+__device__ __forceinline__ void two_sum(T a, T b, T& s, T& e) {
+  s = a + b;
+  const T bp = s - a;
+  e = (a - (s - bp)) + (b - bp);
+}
+
+template <typename T, int QPL, int PPL>
+struct InitRow {
+  T b[QPL], em[QPL], rq[QPL], fq[QPL], cv[PPL];
+};
+
+template <typename T, int QPL, int PPL>
+__global__ void __launch_bounds__(kST)
+init_warp_kernel(const InitArgs<T> a) {
+  constexpr int kW = kST / 32;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int Pe = a.Pe, Pn = a.Pn, Pp = a.Pp, Pnp = a.Pnp, Pqc = a.Pqc, qcov = a.qcov, Dn = a.Dn;
+  const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
+  int* s_pat = reinterpret_cast<int*>(smem);
+  const int npat = 4 * Pe + 2 * (Pn + 1);
+  T* s_mu = reinterpret_cast<T*>(smem + ((sizeof(int) * (size_t)npat + 15) & ~size_t(15)));
+  T* smu = s_mu + (size_t)wib * 64 * PPL;  // hi | lo
+  for (int t = tid; t < npat; t += kST) s_pat[t] = a.pat[t];
+  __syncthreads();
+  const int* s_psrc = s_pat;
+  const int* s_pdst = s_pat + Pe;
+  const double* gv = a.gv;  // [maxneg(Pn) | lse_pos(Pn) | lse_neg(Pn)]
+
+  const int qo = lane * QPL;
+  const bool qon = qo < Pp;
+  T vfm[QPL], vrm[QPL], lbh[QPL], lbl[QPL];
+  int qd[QPL], qs[QPL];
+#pragma unroll
+  for (int k = 0; k < QPL; ++k) {
+    const int q = qo + k;
+    vfm[k] = vrm[k] = lbh[k] = lbl[k] = T(0);
+    qd[k] = qs[k] = 0;
+    if (q < Pe) {
+      qd[k] = s_pdst[q];
+      qs[k] = s_psrc[q];
+      vfm[k] = (T)(gv[qd[k]] - gv[2 * Pn + qd[k]]);  // max_v MU0[dst_q]
+      vrm[k] = (T)(gv[qs[k]] - gv[2 * Pn + qs[k]]);
+      // LSE of the whole quirk row q: its covered part, plus exp(0) per zero
+      long long covered = a.lim - (long long)q * a.De;
+      covered = covered < 0 ? 0 : (covered > a.De ? a.De : covered);
+      LseD r;
+      r.init();
+      if (a.ge[q] > -CUDART_INF) r.merge(a.ge[q], 1.0);
+      const long long zeros = a.De - covered;
+      if (zeros > 0) r.merge(0.0, (double)zeros);
+      const double lb = r.value();
+      lbh[k] = (T)lb;
+      lbl[k] = (T)(lb - (double)lbh[k]);
+    }
+  }
+  T l1h[PPL], l1l[PPL], l2h[PPL], l2l[PPL];
+#pragma unroll
+  for (int j = 0; j < PPL; ++j) {
+    const int p = lane + 32 * j;
+    const double l1 = p < Pn ? gv[Pn + p] : 0.0, l2 = p < Pn ? gv[2 * Pn + p] : 0.0;
+    l1h[j] = (T)l1;
+    l1l[j] = (T)(l1 - (double)l1h[j]);
+    l2h[j] = (T)l2;
+    l2l[j] = (T)(l2 - (double)l2h[j]);
+  }
+  T mxF[QPL], mxR[QPL];
+  OnlineLse<T> lr[QPL], lf[QPL];
+#pragma unroll
+  for (int k = 0; k < QPL; ++k) {
+    mxF[k] = mxR[k] = neg_inf<T>();
+    lr[k].init();
+    lf[k].init();
+  }
+
+  auto load = [&](int v, InitRow<T, QPL, PPL>& r) {
+#pragma unroll
+    for (int k = 0; k < QPL; ++k) {
+      const int q = qo + k;
+      const bool on = q < Pp;
+      r.b[k] = on ? __ldcs(a.B + (size_t)v * Pp + q) : T(0);
+      r.em[k] = on ? __ldcs(a.dEmin + (size_t)v * Pp + q) : T(0);
+      r.rq[k] = q < qcov ? __ldcs(a.Rq + (size_t)v * Pqc + q) : T(0);
+      r.fq[k] = q < qcov ? __ldcs(a.Fq + (size_t)v * Pqc + q) : T(0);
+    }
+#pragma unroll
+    for (int j = 0; j < PPL; ++j) {
+      const int p = lane + 32 * j;
+      r.cv[j] = p < Pn ? __ldcs(a.CV + (size_t)v * Pnp + p) : T(0);
+    }
+  };
+
+  const long long nw = (long long)gridDim.x * kW;
+  const long long gw = (long long)blockIdx.x * kW + wib;
+  const int vb = (int)(gw * Dn / nw), ve = (int)((gw + 1) * Dn / nw);
+  InitRow<T, QPL, PPL> cur, nxt;
+  if (vb < ve) load(vb, cur);
+  for (int v0 = vb; v0 < ve; v0 += 32) {
+    const int nv = min(32, ve - v0);
+    bool hi = false, ho = false;
+    if (lane < nv) {
+      const int v = v0 + lane;
+      hi = __ldg(a.d_off + v + 1) > __ldg(a.d_off + v);
+      ho = __ldg(a.s_off + v + 1) > __ldg(a.s_off + v);
+    }
+    const unsigned inmask = __ballot_sync(0xffffffffu, hi);
+    const unsigned outmask = __ballot_sync(0xffffffffu, ho);
+    for (int jv = 0; jv < nv; ++jv) {
+      const int v = v0 + jv;
+      if (v + 1 < ve) load(v + 1, nxt);
+      // p side: CV = dV - lse1 (hi/lo, written back), MU0 = -dV - lse2 (hi/lo)
+#pragma unroll
+      for (int j = 0; j < PPL; ++j) {
+        const int p = lane + 32 * j;
+        T s1, e1, s2, e2;
+        two_sum(cur.cv[j], -l1h[j], s1, e1);
+        e1 -= l1l[j];
+        const T ch = s1 + e1, cl = e1 - (ch - s1);
+        two_sum(-cur.cv[j], -l2h[j], s2, e2);
+        e2 -= l2l[j];
+        const T mh = s2 + e2, ml = e2 - (mh - s2);
+        if (p < Pn) {
+          a.CV[(size_t)v * Pnp + p] = ch;
+          if constexpr (sizeof(T) == 4) a.CVlo[(size_t)v * Pnp + p] = cl;
+        }
+        smu[p] = mh;
+        smu[32 * PPL + p] = ml;
+      }
+      __syncwarp();
+      if (qon) {
+        const bool hin = (inmask >> jv) & 1u, hout = (outmask >> jv) & 1u;
+#pragma unroll
+        for (int k = 0; k < QPL; ++k) {
+          const int q = qo + k;
+          T yo = T(0), zo = T(0);
+          if (q < Pe) {
+            T R0 = vfm[k], F0 = vrm[k];
+            if (hout) R0 = fmax(R0, ((q < qcov ? cur.rq[k] : T(0)) - lbh[k]) - lbl[k]);
+            if (hin) F0 = fmax(F0, ((q < qcov ? cur.fq[k] : T(0)) - lbh[k]) - lbl[k]);
+            const T f = (smu[qd[k]] - F0) + smu[32 * PPL + qd[k]];
+            const T r = (smu[qs[k]] - R0) + smu[32 * PPL + qs[k]];
+            mxF[k] = fmax(mxF[k], f);
+            mxR[k] = fmax(mxR[k], r);
+            lr[k].add_fast(f + cur.b[k]);
+            lf[k].add_fast(r + cur.b[k]);
+            yo = f - cur.em[k];  // no out-edges: dEmin = +inf, Y = -inf
+            zo = r;
+          }
+          if (q < Pp) {
+            a.vf[(size_t)v * Pp + q] = yo;
+            a.vr[(size_t)v * Pp + q] = zo;
+          }
+        }
+      }
+      __syncwarp();
+      cur = nxt;
+    }
+  }
+
+  // block partials: mVF, mVR (max), lR, lF (lse); warps combined in order
+  __syncthreads();
+  const int nmax = 2 * Pe, nlse = 2 * Pe, slots = nmax + 2 * nlse;
+  double* red = reinterpret_cast<double*>(s_mu);  // the MU rows are free now
+  double* r = red + (size_t)wib * slots;
+#pragma unroll
+  for (int k = 0; k < QPL; ++k) {
+    const int q = qo + k;
+    if (q < Pe) {
+      r[q] = (double)mxF[k];
+      r[Pe + q] = (double)mxR[k];
+      r[nmax + 2 * q] = lr[k].mval();
+      r[nmax + 2 * q + 1] = lr[k].sval();
+      r[nmax + 2 * (Pe + q)] = lf[k].mval();
+      r[nmax + 2 * (Pe + q) + 1] = lf[k].sval();
+    }
+  }
+  __syncthreads();
+  write_block_partials(red, kW, nmax, nlse, a.bpart, gridDim.x, blockIdx.x);
+}
+
+template <typename T, int QPL, int PPL>
+size_t init_warp_smem(int pn, int pe) {
+  const size_t pat = (sizeof(int) * (size_t)(4 * pe + 2 * (pn + 1)) + 15) & ~size_t(15);
+  const size_t mu = sizeof(T) * (size_t)(kST / 32) * 64 * PPL;
+  const size_t red = sizeof(double) * (size_t)(kST / 32) * 6 * pe;
+  return pat + (mu > red ? mu : red);
+}
+
+// Resident blocks per SM of the init kernel's shape (sets its shared-memory
+// attribute); the shape is chosen as for the vertex phase.
+template <typename T, int QPL, int PPL>
+int init_warp_fit(int pn, int pe, size_t* sm) {
+  *sm = init_warp_smem<T, QPL, PPL>(pn, pe);
+  if (*sm > 48 * 1024)
+    cudaFuncSetAttribute(init_warp_kernel<T, QPL, PPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)*sm);
+  int nb = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, init_warp_kernel<T, QPL, PPL>, kST, *sm) !=
+      cudaSuccess)
+    nb = 1;
+  return nb < 1 ? 1 : nb;
+}
+
+template <typename T, typename F>
+bool init_warp_shape(int pn, int pp, F&& f) {
+  if (pp > 64 || pn > 64) return false;
+  if (pp <= 32 && pn <= 32) f.template operator()<1, 1>();
+  else if (pp <= 32) f.template operator()<1, 2>();
+  else if (pn <= 32) f.template operator()<2, 1>();
+  else f.template operator()<2, 2>();
+  return true;
+}
+
+#define ACG_STATIC_SHAPES(X) \
+  X(1, 1) X(2, 1) X(4, 1) X(8, 1) X(16, 1) X(32, 1) X(32, 2) X(32, 4)
+
+}  // namespace
+
+#define ACG_SRC_LAUNCH(NP_, NQ_)                                           \
+  if (ws.npow == NP_ && ws.nqv == NQ_) {                                   \
+    src_stats_kernel<T, NP_, NQ_><<<blocks, kST, 0, s>>>(a);               \
+    ACG_LAUNCH_CHECK();                                                    \
+    return ACG_OK;                                                         \
+  }
+
+template <typename T>
+acg_status launch_src_stats(const SrcStatsArgs<T>& a, WarpShape ws, int blocks, cudaStream_t s) {
+  if (a.nitems == 0) return ACG_OK;
+  ACG_STATIC_SHAPES(ACG_SRC_LAUNCH)
+  return set_error(ACG_ERR_UNSUPPORTED, "no source-side kernel for npow=%d nqv=%d", ws.npow, ws.nqv);
+}
+
+template <typename T>
+acg_status launch_src_stats_combine(const SrcStatsArgs<T>& a, const WarpWork& w, cudaStream_t s) {
+  if (w.nheavy == 0) return ACG_OK;
+  src_stats_combine_kernel<T><<<ceil_div(w.nheavy, 8), 256, 0, s>>>(a, w.hbase, w.hcount, w.hvert,
+                                                                    w.nheavy);
+  ACG_LAUNCH_CHECK();
+  return ACG_OK;
+}
+
+#define ACG_DST_LAUNCH(NP_, NQ_)                                           \
+  if (ws.npow == NP_ && ws.nqv == NQ_) {                                   \
+    dst_quirk_kernel<T, NP_, NQ_><<<blocks, kST, 0, s>>>(a);               \
+    ACG_LAUNCH_CHECK();                                                    \
+    return ACG_OK;                                                         \
+  }
+
+template <typename T>
+acg_status launch_dst_quirk(const DstQuirkArgs<T>& a, WarpShape ws, int blocks, cudaStream_t s) {
+  if (a.nitems == 0 || a.qcov == 0) return ACG_OK;
+  ACG_STATIC_SHAPES(ACG_DST_LAUNCH)
+  return set_error(ACG_ERR_UNSUPPORTED, "no quirk kernel for npow=%d nqv=%d", ws.npow, ws.nqv);
+}
+
+#define ACG_SRC_OCC(NP_, NQ_)                                                           \
+  if (ws.npow == NP_ && ws.nqv == NQ_) {                                                \
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, src_stats_kernel<T, NP_, NQ_>, \
+                                                      kST, 0) != cudaSuccess)           \
+      nb = 1;                                                                           \
+  }
+
+template <typename T>
+int src_stats_blocks_per_sm(WarpShape ws) {
+  int nb = 1;
+  ACG_STATIC_SHAPES(ACG_SRC_OCC)
+  return nb < 1 ? 1 : nb;
+}
+
+template <typename T>
+int init_warp_blocks(int pn, int pe, int pp, int num_sms) {
+  int nb = 0;
+  const bool ok = init_warp_shape<T>(pn, pp, [&]<int QPL, int PPL>() {
+    size_t sm = 0;
+    nb = init_warp_fit<T, QPL, PPL>(pn, pe, &sm);
+  });
+  return ok ? num_sms * nb : 0;
+}
+
+template <typename T>
+acg_status launch_init_warp(const InitArgs<T>& a, int blocks, cudaStream_t s) {
+  cudaError_t le = cudaSuccess;
+  const bool ok = init_warp_shape<T>(a.Pn, a.Pp, [&]<int QPL, int PPL>() {
+    size_t sm = 0;
+    init_warp_fit<T, QPL, PPL>(a.Pn, a.Pe, &sm);
+    init_warp_kernel<T, QPL, PPL><<<blocks, kST, sm, s>>>(a);
+    le = cudaGetLastError();
+  });
+  if (!ok) return set_error(ACG_ERR_UNSUPPORTED, "init warp form: pattern too large");
+  if (le != cudaSuccess) return set_error(ACG_ERR_CUDA, "init_warp_kernel launch: %s", cudaGetErrorString(le));
+  return ACG_OK;
+}
+
+template int init_warp_blocks<double>(int, int, int, int);
+template int init_warp_blocks<float>(int, int, int, int);
+template acg_status launch_init_warp<double>(const InitArgs<double>&, int, cudaStream_t);
+template acg_status launch_init_warp<float>(const InitArgs<float>&, int, cudaStream_t);
+
+template acg_status launch_src_stats<double>(const SrcStatsArgs<double>&, WarpShape, int, cudaStream_t);
+template acg_status launch_src_stats<float>(const SrcStatsArgs<float>&, WarpShape, int, cudaStream_t);
+template acg_status launch_src_stats_combine<double>(const SrcStatsArgs<double>&, const WarpWork&, cudaStream_t);
+template acg_status launch_src_stats_combine<float>(const SrcStatsArgs<float>&, const WarpWork&, cudaStream_t);
+template acg_status launch_dst_quirk<double>(const DstQuirkArgs<double>&, WarpShape, int, cudaStream_t);
+template acg_status launch_dst_quirk<float>(const DstQuirkArgs<float>&, WarpShape, int, cudaStream_t);
+template int src_stats_blocks_per_sm<double>(WarpShape);
+template int src_stats_blocks_per_sm<float>(WarpShape);
+
+}  // namespace acg

@@ -108,7 +108,8 @@ class Plan:
     """``acg_plan``: one pattern matched against one :class:`DataGraph`."""
 
     def __init__(self, data: DataGraph, pattern, precision: str = "fp64", num_iters: int = -1,
-                 stream=None, kernel_timing: bool = False):
+                 stream=None, kernel_timing: bool = False, edge_blocks_per_sm: int = 0,
+                 vertex_blocks_per_sm: int = 0):
         self.data = data
         self.pat = pattern if isinstance(pattern, DeviceGraph) else DeviceGraph(pattern)
         self._c = self.pat.c_graph()
@@ -119,6 +120,8 @@ class Plan:
         opt.precision = PRECISIONS[precision]
         opt.num_iters = num_iters
         opt.kernel_timing = 1 if kernel_timing else 0
+        opt.edge_blocks_per_sm = int(edge_blocks_per_sm)
+        opt.vertex_blocks_per_sm = int(vertex_blocks_per_sm)
         self.precision = precision
         self.handle = C.c_void_p()
         _lib.check(_lib.lib().acg_plan_create(data.handle, C.byref(self._c), C.byref(opt),

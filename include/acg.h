@@ -73,7 +73,10 @@ typedef struct acg_options {
                          what the reference runs (main.cu:160) */
   int32_t kernel_timing; /* nonzero: bracket each iteration's edge and vertex
                             phases with CUDA events (acg_stats.ms_*_phase) */
-  int32_t reserved[5];
+  int32_t edge_blocks_per_sm;   /* resident 256-thread blocks per SM of the edge
+                                   phase and the static passes (0: as many as fit) */
+  int32_t vertex_blocks_per_sm; /* the same for the vertex phase (0: as many as fit) */
+  int32_t reserved[3];
 } acg_options;
 
 /* Fill `opt` with the defaults (FP64, num_iters = -1). */
