@@ -1,12 +1,15 @@
 """ctypes declarations of the C ABI in ``include/acg.h`` and ``include/acg_io.h``.
 
-The library is loaded from the package's ``_build/libacg.so``.  There is no
-fallback: if the library is missing, :func:`lib` raises, so that nothing can
-silently run on another code path.
+The library is loaded from the package's ``_build/libacg.so`` (or from the
+path in the environment variable ``ACG_LIBRARY``, a variant built by
+``build.build(out_dir=...)``).  There is no fallback: if the library is
+missing, :func:`lib` raises, so that nothing can silently run on another code
+path.
 """
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 from . import build as _build
@@ -132,7 +135,8 @@ _LIB: C.CDLL | None = None
 
 
 def lib_path() -> Path:
-    return _build.LIB
+    env = os.environ.get("ACG_LIBRARY")
+    return Path(env) if env else _build.LIB
 
 
 def lib() -> C.CDLL:

@@ -47,13 +47,13 @@ def _stale(obj: Path, src: Path, deps: list[Path]) -> bool:
     return any(p.stat().st_mtime > t for p in [src, *deps])
 
 
-def _compile(src: Path, verbose: bool) -> Path:
-    obj = BUILD / (src.name + ".o")
+def _compile(src: Path, verbose: bool, out: Path = BUILD, defines: tuple = ()) -> Path:
+    obj = out / (src.name + ".o")
     if src.suffix == ".cu":
         cmd = [
             _nvcc(), ARCH, "-lineinfo", "-O3", "-std=c++20", "-c", str(src), "-o", str(obj),
             "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", "--expt-relaxed-constexpr",
-            "-I", str(INCLUDE), "-I", str(CSRC),
+            "-I", str(INCLUDE), "-I", str(CSRC), *[f"-D{d}" for d in defines],
         ]
         if os.environ.get("ACG_PTXAS_VERBOSE"):
             cmd += ["-Xptxas", "-v"]
@@ -73,17 +73,24 @@ def _compile(src: Path, verbose: bool) -> Path:
     return obj
 
 
-def build(verbose: bool = False, force: bool = False) -> Path:
-    """Compile and link ``libacg.so``; return its path."""
-    BUILD.mkdir(parents=True, exist_ok=True)
+def build(verbose: bool = False, force: bool = False, out_dir: Path | None = None,
+          defines: tuple = ()) -> Path:
+    """Compile and link ``libacg.so``; return its path.
+
+    ``out_dir`` and ``defines`` (``NAME=VALUE`` preprocessor definitions for the
+    CUDA sources) build a variant elsewhere, e.g. to compare tuning constants;
+    load one with the environment variable ``ACG_LIBRARY``."""
+    out = Path(out_dir) if out_dir else BUILD
+    lib = out / "libacg.so"
+    out.mkdir(parents=True, exist_ok=True)
     srcs = sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp")))
     deps = _headers()
-    todo = [s for s in srcs if force or _stale(BUILD / (s.name + ".o"), s, deps)]
+    todo = [s for s in srcs if force or _stale(out / (s.name + ".o"), s, deps)]
     with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(todo)))) as ex:
-        list(ex.map(lambda s: _compile(s, verbose), todo))
-    objs = [BUILD / (s.name + ".o") for s in srcs]
-    if force or todo or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
-        tmp = BUILD / "libacg.so.tmp"
+        list(ex.map(lambda s: _compile(s, verbose, out, tuple(defines)), todo))
+    objs = [out / (s.name + ".o") for s in srcs]
+    if force or todo or not lib.exists() or any(o.stat().st_mtime > lib.stat().st_mtime for o in objs):
+        tmp = out / "libacg.so.tmp"
         cmd = [_nvcc(), ARCH, "-shared", "-o", str(tmp), *map(str, objs),
                "-Xcompiler", "-fopenmp", "-lgomp", "-cudart", "static"]
         if verbose:
@@ -91,8 +98,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -29,7 +29,13 @@ namespace acg {
 namespace {
 
 constexpr int kST = 256;  // threads per block (the edge phase's warp work uses 8 warps per block)
-constexpr int kSU = 4;    // load steps issued back to back (the edge phase's kU)
+#ifndef ACG_SRC_KU
+#define ACG_SRC_KU 4
+#endif
+#ifndef ACG_SRC_MINB
+#define ACG_SRC_MINB 0
+#endif
+constexpr int kSU = ACG_SRC_KU;  // load steps issued back to back
 
 template <typename T>
 struct SV;
@@ -65,25 +71,18 @@ __device__ __forceinline__ void kahan_add(T& s, T& c, T x) {
   s = t;
 }
 
-// (m, s) log-sum-exp pairs: s = sum exp(x - m); m = -inf means empty.
+// Largest dEmin for which exp(-dE) of the nearest out-edge is still a normal
+// number; above it a column's sum is redone relative to its minimum.
 template <typename T>
-__device__ __forceinline__ void lse_pair_merge(T& m, T& s, T m2, T s2) {
-  if (!(m2 > neg_inf<T>()) || !(s2 > T(0))) return;
-  if (!(m > neg_inf<T>()) || !(s > T(0))) {
-    m = m2;
-    s = s2;
-    return;
-  }
-  if (m2 > m) {
-    s = s * dev_exp(m - m2) + s2;
-    m = m2;
-  } else {
-    s += s2 * dev_exp(m2 - m);
-  }
-}
+__device__ __forceinline__ T exp_ref_limit() { return sizeof(T) == 4 ? T(60) : T(600); }
 
+#if ACG_SRC_MINB > 0
+#define ACG_SRC_BOUNDS __launch_bounds__(kST, ACG_SRC_MINB)
+#else
+#define ACG_SRC_BOUNDS __launch_bounds__(kST)
+#endif
 template <typename T, int NPOW, int NQV>
-__global__ void __launch_bounds__(kST, 1)
+__global__ void ACG_SRC_BOUNDS
 src_stats_kernel(const SrcStatsArgs<T> a) {
   using VT = typename SV<T>::type;
   constexpr int W = SV<T>::W;
@@ -109,9 +108,11 @@ src_stats_kernel(const SrcStatsArgs<T> a) {
     ridx[u] = ok ? __ldg(a.row_of + e) : 0;
     eidx[u] = ok ? __ldg(a.eid + e) : 0;
   }
-  // Per column: the running minimum mn of dE, and sum_i exp(mn - dE_i) (with
-  // a compensation term) rescaled when the minimum moves, so that
-  // B = -mn + log(sum) takes one exponential per element.
+  // Per column: the minimum mn of dE and sum_i exp(-dE_i) (with a compensation
+  // term; -dE <= 0, so the sum cannot overflow): one exponential and no branch
+  // per element.  A column whose nearest edge is so far (mn above
+  // exp_ref_limit) that the terms leave the normal range is summed again
+  // relative to its minimum, which is rare and uniform across the warp.
   T mn[NQ], qx[NQ], sm[NQ], sc[NQ];
 #pragma unroll
   for (int k = 0; k < NQ; ++k) {
@@ -162,15 +163,8 @@ src_stats_kernel(const SrcStatsArgs<T> a) {
           const int q = (qc + NPOW * k) * W + w;
           const T d = sg<T>(x[u][k], w);
           const int j = k * W + w;
-          if (d < mn[j]) {  // new minimum (rare after the first few elements)
-            const T f = mn[j] < pos_inf<T>() ? exp_fast(d - mn[j]) : T(0);
-            sm[j] *= f;
-            sc[j] *= f;
-            mn[j] = d;
-            kahan_add(sm[j], sc[j], T(1));
-          } else if (d < pos_inf<T>()) {
-            kahan_add(sm[j], sc[j], exp_fast(mn[j] - d));
-          }
+          mn[j] = fmin(mn[j], d);
+          kahan_add(sm[j], sc[j], exp_fast(-d));  // d = +inf (padding) adds 0
           if (q < qcov) {
             const bool covered = (long long)q * a.De + ecur[u] < a.lim;
             qx[k * W + w] = fmax(qx[k * W + w], covered ? -d : T(0));
@@ -178,22 +172,52 @@ src_stats_kernel(const SrcStatsArgs<T> a) {
         }
     }
     if (item_done) {
-      T lm[NQ], lsum[NQ];  // (max, sum) of exp(-dE): max = -mn
+      T lm[NQ], lsum[NQ];  // the column's (reference, sum of exp(-dE - reference))
 #pragma unroll
-      for (int k = 0; k < NQ; ++k) {
-        lm[k] = -mn[k];
-        lsum[k] = sm[k] - sc[k];
-      }
+      for (int k = 0; k < NQ; ++k) lsum[k] = sm[k] - sc[k];
 #pragma unroll
       for (int o = NPOW; o < 32; o <<= 1)
 #pragma unroll
         for (int k = 0; k < NQ; ++k) {
           mn[k] = fmin(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
           qx[k] = fmax(qx[k], __shfl_xor_sync(0xffffffffu, qx[k], o));
-          const T m2 = __shfl_xor_sync(0xffffffffu, lm[k], o);
-          const T s2 = __shfl_xor_sync(0xffffffffu, lsum[k], o);
-          lse_pair_merge<T>(lm[k], lsum[k], m2, s2);
+          lsum[k] += __shfl_xor_sync(0xffffffffu, lsum[k], o);
         }
+      bool far = false;
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        lm[k] = T(0);
+        far |= mn[k] > exp_ref_limit<T>() && mn[k] < pos_inf<T>();
+      }
+      if (__any_sync(0xffffffffu, far)) {
+        // sum exp(mn - dE) again over this item's edges, for every column
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) {
+          sm[k] = T(0);
+          sc[k] = T(0);
+        }
+        for (int e = item.y + slot; e < item.z; e += S) {
+          const T* row = a.dE + (size_t)__ldg(a.row_of + e) * Pp;
+#pragma unroll
+          for (int k = 0; k < NQV; ++k) {
+            const int qv = qc + NPOW * k;
+            if (qv * W >= Pp) continue;
+            const VT xv = __ldg(reinterpret_cast<const VT*>(row) + qv);
+#pragma unroll
+            for (int w = 0; w < W; ++w)
+              kahan_add(sm[k * W + w], sc[k * W + w], exp_fast(mn[k * W + w] - sg<T>(xv, w)));
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) {
+          lsum[k] = sm[k] - sc[k];
+          lm[k] = -mn[k];
+        }
+#pragma unroll
+        for (int o = NPOW; o < 32; o <<= 1)
+#pragma unroll
+          for (int k = 0; k < NQ; ++k) lsum[k] += __shfl_xor_sync(0xffffffffu, lsum[k], o);
+      }
       if (slot == 0) {
         const int v = item.x;
 #pragma unroll
