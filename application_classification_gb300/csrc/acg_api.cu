@@ -279,8 +279,12 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
     ACG_TRY(launch_src_stats<T>(sa, P->ws, P->src_blocks, s));
     ACG_TRY(launch_src_stats_combine<T>(sa, P->sw, s));
     DstQuirkArgs<T> qa{P->ew.items, P->ew.nitems, P->ew.wsplit, D->dcsr.eid, (const T*)P->dE,
-                       (T*)P->Fq, (T*)P->part_iter, De, lim, Pp, P->Pqc, P->qcov};
+                       (T*)P->Fq, (T*)P->part_iter, P->bpart, De, lim, Pp, P->Pqc, P->qcov};
     ACG_TRY(launch_dst_quirk<T>(qa, P->qws, P->edge_blocks, s));
+    if (P->qcov > 0 && P->ew.nitems > 0) {  // ge[q < Pqc]; the later columns stay -inf
+      ACG_TRY(launch_finalize(P->bpart, P->edge_blocks, StatSpec{0, P->Pqc}, P->ge, s));
+      P->launches += 1;
+    }
     if (P->qcov > 0)
       ACG_TRY(launch_heavy_combine<T>((const T*)P->part_iter, P->ew.hbase, P->ew.hcount,
                                       P->ew.hvert, P->ew.nheavy, P->Pqc, (T*)P->Fq, s));
@@ -352,10 +356,9 @@ acg_status run_cdist(acg_plan* P, acg_data* D, long long lim, const F* nf, int n
   ACG_TRY(launch_finalize(P->bpart, P->cv_blocks, StatSpec{P->Pn, 2 * P->Pn}, P->gv, s));
   // rows in dst-CSR order; with no data edges the kernel writes empty partials
   CdistRbArgs<T, F> ae{ef, gather ? D->dcsr.eid : nullptr, D->dcsr.eid, P->pe, (T*)P->dE,
-                       P->bpart, D->De, D->De, lim, D->Ke, efs, P->Pe, P->Pp, P->Pp};
-  ACG_TRY(launch_cdist_rb(ae, kCdistEdge, P->ce_blocks, s));
-  ACG_TRY(launch_finalize(P->bpart, P->ce_blocks, StatSpec{0, P->Pe}, P->ge, s));
-  P->launches += 4;
+                       nullptr, D->De, D->De, lim, D->Ke, efs, P->Pe, P->Pp, P->Pp};
+  ACG_TRY(launch_cdist_edges(ae, P->ce_blocks, s));
+  P->launches += 3;
   return ACG_OK;
 }
 
@@ -577,7 +580,7 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
     }
   }
   P->cv_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), 64), nsm * 2));
-  P->ce_blocks = std::max(1, std::min(ceil_div(std::max(1, De), 64), nsm * 2));
+  P->ce_blocks = std::max(1, std::min(ceil_div(std::max(1, De), 256), nsm * 8));
 
   const size_t vrow = (size_t)Dn * Pp * eb;
   alloc((size_t)De * Pp * eb, &P->dE);
@@ -615,10 +618,13 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
   }
   const size_t bp = std::max({(size_t)(6 * Pe + 2 * Pn) * P->vert_blocks,
                               (size_t)5 * Pn * P->cv_blocks, (size_t)2 * Pe * P->ce_blocks,
-                              (size_t)6 * Pe * P->init_blocks});
+                              (size_t)6 * Pe * P->init_blocks,
+                              (size_t)2 * P->Pqc * P->edge_blocks});
   alloc(sizeof(double) * bp, (void**)&P->bpart);
   alloc(sizeof(double) * 3 * Pn, (void**)&P->gv);
-  alloc(sizeof(double) * std::max(1, Pe), (void**)&P->ge);
+  alloc(sizeof(double) * std::max(P->Pqc, Pe), (void**)&P->ge);
+  if (st == ACG_OK)  // columns without covered elements (and the case De = 0)
+    st = launch_fill<double>(P->ge, (size_t)std::max(P->Pqc, Pe), -std::numeric_limits<double>::infinity(), s);
   alloc(sizeof(double) * glob_doubles(Pn, Pe), (void**)&P->gi[0]);
   alloc(sizeof(double) * glob_doubles(Pn, Pe), (void**)&P->gi[1]);
   if (st != ACG_OK) return fail(st);

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "acg_cdist.cuh"
 #include "acg_device.cuh"
@@ -144,6 +145,7 @@ cdist_rb_kernel(const CdistRbArgs<T, F> a) {
   }
   // ---- block partials per column, row groups combined in order (one of the
   // QB columns of every thread at a time)
+  if (a.bpart == nullptr) return;
   const int ncols = gridDim.x, col = blockIdx.x;
 #pragma unroll
   for (int j = 0; j < QB; ++j) {
@@ -188,6 +190,57 @@ cdist_rb_kernel(const CdistRbArgs<T, F> a) {
   }
 }
 
+
+// One thread per data row, for the edge cost matrix with K <= 32: the row's
+// features in registers (KM = K rounded up to 4, zero padded: (0 - 0)^2 adds
+// nothing), the pattern features in shared memory read as broadcast 16-byte
+// loads, the distances of one row written by its thread as 16-byte stores (L2
+// merges them into full lines).  No block-wide barrier after the prologue.
+template <typename T, typename F, int KM>
+__global__ void __launch_bounds__(kCT)
+cdist_rows_kernel(const CdistRbArgs<T, F> a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  T* s_y = reinterpret_cast<T*>(smem);  // [Pp][KM]
+  const int K = a.K, P = a.P, Pp = a.Pp;
+  for (int t = threadIdx.x; t < Pp * KM; t += kCT) {
+    const int q = t / KM, k = t % KM;
+    s_y[t] = (q < P && k < K) ? (T)a.y[(size_t)q * K + k] : T(0);
+  }
+  __syncthreads();
+  constexpr int VW = 16 / sizeof(T);
+  using VT = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  for (long long r = (long long)blockIdx.x * kCT + threadIdx.x; r < a.nrows;
+       r += (long long)gridDim.x * kCT) {
+    const long long src = a.row ? (long long)__ldg(a.row + r) : r;
+    const F* xr = a.x + (size_t)src * a.kstride;
+    T x[KM];
+#pragma unroll
+    for (int k = 0; k < KM; ++k) x[k] = k < K ? (T)__ldg(xr + k) : T(0);
+    T* orow = a.out + (size_t)r * a.ostride;
+    for (int q0 = 0; q0 < Pp; q0 += VW) {
+      T d[VW];
+#pragma unroll
+      for (int j = 0; j < VW; ++j) {
+        const T* yq = s_y + (size_t)(q0 + j) * KM;
+        T acc = T(0);
+#pragma unroll
+        for (int k = 0; k < KM; k += VW) {
+          const VT yv = *reinterpret_cast<const VT*>(yq + k);
+#pragma unroll
+          for (int w = 0; w < VW; ++w) {
+            const T t = x[k + w] - reinterpret_cast<const T*>(&yv)[w];
+            acc = fma(t, t, acc);
+          }
+        }
+        d[j] = q0 + j < P ? sqrt(acc) : T(0);
+      }
+      if constexpr (sizeof(T) == 4)
+        *reinterpret_cast<float4*>(orow + q0) = make_float4(d[0], d[1], d[2], d[3]);
+      else
+        *reinterpret_cast<double2*>(orow + q0) = make_double2(d[0], d[1]);
+    }
+  }
+}
 }  // namespace
 
 // Register blocking per element type: FP32 4 rows x 8 columns, FP64 4 x 4.
@@ -231,6 +284,34 @@ acg_status launch_cdist_rb(const CdistRbArgs<T, F>& a, int mode, int blocks, cud
   ACG_LAUNCH_CHECK();
   return ACG_OK;
 }
+
+
+#define ACG_ROWS_CASE(KM_)                                                                 \
+  if (km == KM_) {                                                                         \
+    const size_t sm = sizeof(T) * (size_t)a.Pp * KM_;                                      \
+    if (sm > 48 * 1024)                                                                    \
+      ACG_CUDA_TRY(cudaFuncSetAttribute(cdist_rows_kernel<T, F, KM_>,                      \
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)); \
+    cdist_rows_kernel<T, F, KM_><<<blocks, kCT, sm, s>>>(a);                               \
+    ACG_LAUNCH_CHECK();                                                                    \
+    return ACG_OK;                                                                         \
+  }
+
+template <typename T, typename F>
+acg_status launch_cdist_edges(const CdistRbArgs<T, F>& a, int blocks, cudaStream_t s) {
+  if (a.P == 0 || a.nrows == 0) return ACG_OK;
+  const int km = (a.K + 3) / 4 * 4;
+  if (km >= 4) {
+    ACG_ROWS_CASE(4) ACG_ROWS_CASE(8) ACG_ROWS_CASE(12) ACG_ROWS_CASE(16)
+    ACG_ROWS_CASE(20) ACG_ROWS_CASE(24) ACG_ROWS_CASE(28) ACG_ROWS_CASE(32)
+  }
+  CdistRbArgs<T, F> b = a;  // wide features: the tiled kernel, no statistics
+  b.bpart = nullptr;
+  return launch_cdist_rb(b, kCdistEdge, blocks, s);
+}
+
+template acg_status launch_cdist_edges<double, double>(const CdistRbArgs<double, double>&, int, cudaStream_t);
+template acg_status launch_cdist_edges<float, float>(const CdistRbArgs<float, float>&, int, cudaStream_t);
 
 template acg_status launch_cdist_rb<double, double>(const CdistRbArgs<double, double>&, int, int, cudaStream_t);
 template acg_status launch_cdist_rb<float, float>(const CdistRbArgs<float, float>&, int, int, cudaStream_t);

@@ -28,5 +28,10 @@ struct CdistRbArgs {
 
 template <typename T, typename F>
 acg_status launch_cdist_rb(const CdistRbArgs<T, F>& a, int mode, int blocks, cudaStream_t s);
+// The edge cost matrix without statistics (the covered-element log-sum-exps
+// come from the destination-side quirk pass): one thread per row for K <= 32,
+// else the tiled kernel.
+template <typename T, typename F>
+acg_status launch_cdist_edges(const CdistRbArgs<T, F>& a, int blocks, cudaStream_t s);
 
 }  // namespace acg

@@ -114,12 +114,17 @@ src_stats_kernel(const SrcStatsArgs<T> a) {
   // exp_ref_limit) that the terms leave the normal range is summed again
   // relative to its minimum, which is rare and uniform across the warp.
   T mn[NQ], qx[NQ], sm[NQ], sc[NQ];
+  // quirk coverage of column q: original edge id < lim - q * De (no edge for
+  // the columns q >= qcov, whose quirk value is never read)
+  long long qlim[NQ];
 #pragma unroll
   for (int k = 0; k < NQ; ++k) {
     mn[k] = pos_inf<T>();
     qx[k] = neg_inf<T>();
     sm[k] = T(0);
     sc[k] = T(0);
+    const int q = (qc + NPOW * (k / W)) * W + k % W;
+    qlim[k] = q < qcov ? a.lim - (long long)q * a.De : 0;
   }
   for (;;) {
     VT x[kSU][NQV];
@@ -153,24 +158,20 @@ src_stats_kernel(const SrcStatsArgs<T> a) {
       ridx[u] = ok ? __ldg(a.row_of + e) : 0;
       eidx[u] = ok ? __ldg(a.eid + e) : 0;
     }
+    // branch-free: a missing edge reads +inf, which changes no minimum, adds
+    // exp(-inf) = 0 and gives a quirk value of -inf
 #pragma unroll
-    for (int u = 0; u < kSU; ++u) {
-      if (!okv[u]) continue;
+    for (int u = 0; u < kSU; ++u)
 #pragma unroll
       for (int k = 0; k < NQV; ++k)
 #pragma unroll
         for (int w = 0; w < W; ++w) {
-          const int q = (qc + NPOW * k) * W + w;
           const T d = sg<T>(x[u][k], w);
           const int j = k * W + w;
           mn[j] = fmin(mn[j], d);
-          kahan_add(sm[j], sc[j], exp_fast(-d));  // d = +inf (padding) adds 0
-          if (q < qcov) {
-            const bool covered = (long long)q * a.De + ecur[u] < a.lim;
-            qx[k * W + w] = fmax(qx[k * W + w], covered ? -d : T(0));
-          }
+          kahan_add(sm[j], sc[j], exp_fast(-d));
+          qx[j] = fmax(qx[j], (long long)ecur[u] < qlim[j] ? -d : T(0));
         }
-    }
     if (item_done) {
       T lm[NQ], lsum[NQ];  // the column's (reference, sum of exp(-dE - reference))
 #pragma unroll
@@ -294,73 +295,101 @@ dst_quirk_kernel(const DstQuirkArgs<T> a) {
   constexpr int S = 32 / NPOW;
   constexpr int NQ = NQV * W;
   constexpr int STEP = S * kSU;
+  extern __shared__ __align__(16) unsigned char smem_q[];
   const int Pp = a.Pp, Pqc = a.Pqc, qcov = a.qcov;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int slot = lane / NPOW, qc = lane % NPOW;
   const int gw = (blockIdx.x * kST + threadIdx.x) >> 5;
   const int it_end = __ldg(a.wsplit + gw + 1);
   int it = __ldg(a.wsplit + gw);
-  if (it >= it_end) return;
-  int4 item = __ldg(a.items + it);
-  int base = item.y;
   T qx[NQ];
+  long long qlim[NQ];
+  // LSE of -dE over the covered elements of each column (the reference's
+  // first softmax of its RE/FE buffers, main.cu:113-114, 135-146)
+  OnlineLse<T> ls[NQ];
 #pragma unroll
-  for (int k = 0; k < NQ; ++k) qx[k] = neg_inf<T>();
-  for (;;) {
-    VT x[kSU][NQV];
-    int ev[kSU];
-    bool okv[kSU];
+  for (int k = 0; k < NQ; ++k) {
+    qx[k] = neg_inf<T>();
+    ls[k].init();
+    const int q = (qc + NPOW * (k / W)) * W + k % W;
+    qlim[k] = q < qcov ? a.lim - (long long)q * a.De : 0;
+  }
+  if (it < it_end) {
+    int4 item = __ldg(a.items + it);
+    int base = item.y;
+    for (;;) {
+      VT x[kSU][NQV];
+      int ev[kSU];
 #pragma unroll
-    for (int u = 0; u < kSU; ++u) {
-      const int e = base + slot + S * u;
-      okv[u] = e < item.z;
-      ev[u] = okv[u] ? __ldg(a.eid + e) : 0;
+      for (int u = 0; u < kSU; ++u) {
+        const int e = base + slot + S * u;
+        const bool ok = e < item.z;
+        ev[u] = ok ? __ldg(a.eid + e) : 0;
 #pragma unroll
-      for (int k = 0; k < NQV; ++k) {
-        const int qv = qc + NPOW * k;
-        x[u][k] = (okv[u] && qv * W < Pqc)
-                      ? __ldcs(reinterpret_cast<const VT*>(a.dE + (size_t)e * Pp) + qv)
-                      : sfill<T>(pos_inf<T>());
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < kSU; ++u) {
-      if (!okv[u]) continue;
-#pragma unroll
-      for (int k = 0; k < NQV; ++k)
-#pragma unroll
-        for (int w = 0; w < W; ++w) {
-          const int q = (qc + NPOW * k) * W + w;
-          if (q < qcov) {
-            const bool covered = (long long)q * a.De + ev[u] < a.lim;
-            qx[k * W + w] = fmax(qx[k * W + w], covered ? -sg<T>(x[u][k], w) : T(0));
-          }
+        for (int k = 0; k < NQV; ++k) {
+          const int qv = qc + NPOW * k;
+          x[u][k] = (ok && qv * W < Pqc)
+                        ? __ldcs(reinterpret_cast<const VT*>(a.dE + (size_t)e * Pp) + qv)
+                        : sfill<T>(pos_inf<T>());
         }
-    }
-    if (base + STEP >= item.z) {
+      }
+      // a missing edge reads +inf: quirk value -inf, nothing added
 #pragma unroll
-      for (int o = NPOW; o < 32; o <<= 1)
-#pragma unroll
-        for (int k = 0; k < NQ; ++k) qx[k] = fmax(qx[k], __shfl_xor_sync(0xffffffffu, qx[k], o));
-      if (slot == 0) {
-        T* row = item.w >= 0 ? a.partial + (size_t)item.w * Pqc : a.Fq + (size_t)item.x * Pqc;
+      for (int u = 0; u < kSU; ++u)
 #pragma unroll
         for (int k = 0; k < NQV; ++k)
 #pragma unroll
           for (int w = 0; w < W; ++w) {
-            const int q = (qc + NPOW * k) * W + w;
-            if (q < Pqc) row[q] = qx[k * W + w];
+            const int j = k * W + w;
+            const T d = sg<T>(x[u][k], w);
+            const bool covered = (long long)ev[u] < qlim[j];
+            qx[j] = fmax(qx[j], covered ? -d : T(0));
+            if (covered) ls[j].add(-d);
           }
-      }
+      if (base + STEP >= item.z) {
 #pragma unroll
-      for (int k = 0; k < NQ; ++k) qx[k] = neg_inf<T>();
-      if (++it >= it_end) break;
-      item = __ldg(a.items + it);
-      base = item.y;
-    } else {
-      base += STEP;
+        for (int o = NPOW; o < 32; o <<= 1)
+#pragma unroll
+          for (int k = 0; k < NQ; ++k) qx[k] = fmax(qx[k], __shfl_xor_sync(0xffffffffu, qx[k], o));
+        if (slot == 0) {
+          T* row = item.w >= 0 ? a.partial + (size_t)item.w * Pqc : a.Fq + (size_t)item.x * Pqc;
+#pragma unroll
+          for (int k = 0; k < NQV; ++k)
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+              const int q = (qc + NPOW * k) * W + w;
+              if (q < Pqc) row[q] = qx[k * W + w];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) qx[k] = neg_inf<T>();
+        if (++it >= it_end) break;
+        item = __ldg(a.items + it);
+        base = item.y;
+      } else {
+        base += STEP;
+      }
     }
   }
+  // column log-sum-exps: slots merged across the warp, warps in order
+  double* red = reinterpret_cast<double*>(smem_q);  // [warp][2 Pqc]
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    double m = ls[k].mval(), sv = ls[k].sval();
+#pragma unroll
+    for (int o = NPOW; o < 32; o <<= 1) {
+      const double m2 = __shfl_xor_sync(0xffffffffu, m, o);
+      const double s2 = __shfl_xor_sync(0xffffffffu, sv, o);
+      lse_merge(m, sv, m2, s2);
+    }
+    const int q = (qc + NPOW * (k / W)) * W + k % W;
+    if (slot == 0 && q < Pqc) {
+      red[(size_t)wib * 2 * Pqc + 2 * q] = m;
+      red[(size_t)wib * 2 * Pqc + 2 * q + 1] = sv;
+    }
+  }
+  __syncthreads();
+  write_block_partials(red, kST / 32, 0, Pqc, a.bpart, gridDim.x, blockIdx.x);
 }
 
 // ------------------------------------------------------------ init, warp form
@@ -613,11 +642,15 @@ acg_status launch_src_stats_combine(const SrcStatsArgs<T>& a, const WarpWork& w,
   return ACG_OK;
 }
 
-#define ACG_DST_LAUNCH(NP_, NQ_)                                           \
-  if (ws.npow == NP_ && ws.nqv == NQ_) {                                   \
-    dst_quirk_kernel<T, NP_, NQ_><<<blocks, kST, 0, s>>>(a);               \
-    ACG_LAUNCH_CHECK();                                                    \
-    return ACG_OK;                                                         \
+#define ACG_DST_LAUNCH(NP_, NQ_)                                                  \
+  if (ws.npow == NP_ && ws.nqv == NQ_) {                                          \
+    const size_t sm = sizeof(double) * (size_t)(kST / 32) * 2 * a.Pqc;            \
+    if (sm > 48 * 1024)                                                           \
+      ACG_CUDA_TRY(cudaFuncSetAttribute(dst_quirk_kernel<T, NP_, NQ_>,            \
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)); \
+    dst_quirk_kernel<T, NP_, NQ_><<<blocks, kST, sm, s>>>(a);                     \
+    ACG_LAUNCH_CHECK();                                                           \
+    return ACG_OK;                                                                \
   }
 
 template <typename T>

@@ -46,7 +46,9 @@ template <typename T>
 acg_status launch_src_stats_combine(const SrcStatsArgs<T>& a, const WarpWork& w, cudaStream_t s);
 
 // Destination-side quirk maximum over each vertex's in-edges (consecutive rows
-// of the destination-sorted dE), columns q < qcov only.
+// of the destination-sorted dE), columns q < qcov only, and per column the
+// log-sum-exp of -dE over its covered elements (block partials, StatSpec{0,
+// Pqc}; every edge is an in-edge of exactly one item).
 template <typename T>
 struct DstQuirkArgs {
   const int4* items;
@@ -56,6 +58,7 @@ struct DstQuirkArgs {
   const T* dE;         // [De][Pp]
   T* Fq;               // [Dn][Pqc]
   T* partial;          // [npartial][Pqc]
+  double* bpart;       // [2 Pqc][blocks]
   long long De, lim;
   int Pp, Pqc, qcov;
 };
