@@ -129,6 +129,8 @@ SIGNATURES: dict[str, tuple] = {
                            _P(HostGraph)]),
     "acg_gen_plant": (i32, [_P(HostGraph), u64, u64, C.c_double, u64, _P(HostGraph), u64p, u64p]),
     "acg_gen_fill_edges": (i32, [_P(HostGraph), u64, u64]),
+    "acg_mu_write_text": (i32, [C.c_char_p, vp, u64, u64]),
+    "acg_mu_write_bin": (i32, [C.c_char_p, vp, u64, u64]),
 }
 
 _LIB: C.CDLL | None = None

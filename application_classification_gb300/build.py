@@ -1,4 +1,6 @@
-"""Build the native library ``_build/libacg.so`` for sm_103a.
+"""Build the native library ``_build/libacg.so`` for sm_103a, and the tools
+``_build/acg_main`` (drop-in for the reference program) and
+``_build/acg_prob2bin`` (its CSV-to-binary converter).
 
 Every ``csrc/*.cu`` is compiled by nvcc for ``sm_103a`` only, every
 ``csrc/*.cpp`` by the host compiler; translation units compile in parallel and
@@ -99,7 +101,30 @@ def build(verbose: bool = False, force: bool = False, out_dir: Path | None = Non
         if r.returncode != 0:
             raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, lib)
+    _build_tools(out, lib, verbose, force)
     return lib
+
+
+CLI = PKG / "cli"
+TOOLS = {"acg_main": "acg_main.cpp", "acg_prob2bin": "acg_prob2bin.cpp"}
+
+
+def _build_tools(out: Path, lib: Path, verbose: bool, force: bool) -> None:
+    """The command-line tools next to the library (rpath $ORIGIN): ``acg_main``
+    (drop-in for the reference program) and ``acg_prob2bin``."""
+    for name, src in TOOLS.items():
+        exe, srcp = out / name, CLI / src
+        if not force and exe.exists() and exe.stat().st_mtime > max(
+                srcp.stat().st_mtime, lib.stat().st_mtime):
+            continue
+        cmd = [_nvcc(), ARCH, "-O2", "-std=c++17", "-x", "cu", str(srcp), "-o", str(exe),
+               "-I", str(INCLUDE), "-L", str(out), "-lacg", "-Xlinker", "-rpath=$ORIGIN",
+               "-Xcompiler", "-fopenmp", "-cudart", "static"]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"build of {name} failed\n{r.stdout}\n{r.stderr}")
 
 
 if __name__ == "__main__":

@@ -8,6 +8,8 @@
 
 #include <algorithm>
 #include <cerrno>
+#include <charconv>
+#include <cstdio>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -652,6 +654,71 @@ acg_status acg_gen_plant(acg_host_graph* data, uint64_t pn, uint64_t pe, double 
     for (uint64_t k = 0; k < ke; ++k)
       pattern->edge_feats[j * ke + k] = data->edge_feats[e * ke + k] + noise * pattern->edge_feats[j * ke + k];
   }
+  return ACG_OK;
+}
+
+// ---------------------------------------------------------------- mu output
+// The reference prints MU with printf("%e\n") per entry, row-major
+// (main.cu:255-257).  std::to_chars with the scientific format and precision 6
+// produces the same characters as "%e" (a correctly rounded decimal, at least
+// two exponent digits, "inf"/"nan" spelled the same); blocks of entries are
+// formatted in parallel and written in order.
+acg_status acg_mu_write_text(const char* path, const double* mu, uint64_t rows, uint64_t cols) {
+  acg::clear_error();
+  const uint64_t n = rows * cols;
+  if (n && !mu) return acg::set_error(ACG_ERR_INVALID_ARGUMENT, "acg_mu_write_text: mu is null");
+  FILE* f = path ? std::fopen(path, "wb") : stdout;
+  if (!f) return acg::set_error(ACG_ERR_IO, "cannot open %s: %s", path, std::strerror(errno));
+  constexpr uint64_t kBlock = 1 << 22;  // entries per block
+  constexpr int kMaxChars = 32;         // "-1.234568e+308\n" and the like
+  const int nt = std::max(1, omp_get_max_threads());
+  std::vector<char> buf((size_t)std::min<uint64_t>(n, kBlock) * kMaxChars + 1);
+  std::vector<size_t> len((size_t)nt + 1);
+  acg_status st = ACG_OK;
+  for (uint64_t b0 = 0; b0 < n && st == ACG_OK; b0 += kBlock) {
+    const uint64_t bn = std::min<uint64_t>(kBlock, n - b0);
+#pragma omp parallel num_threads(nt)
+    {
+      const int t = omp_get_thread_num(), T = omp_get_num_threads();
+      const uint64_t i0 = bn * t / T, i1 = bn * (t + 1) / T;
+      char* o = buf.data() + i0 * kMaxChars;
+      char* p = o;
+      for (uint64_t i = i0; i < i1; ++i) {
+        auto r = std::to_chars(p, p + kMaxChars - 1, mu[b0 + i], std::chars_format::scientific, 6);
+        p = r.ptr;
+        *p++ = '\n';
+      }
+      len[(size_t)t] = (size_t)(p - o);
+#pragma omp barrier
+#pragma omp single
+      {
+        for (int u = 0; u < T && st == ACG_OK; ++u) {
+          const uint64_t j0 = bn * u / T;
+          const size_t L = len[(size_t)u];
+          if (L && std::fwrite(buf.data() + j0 * kMaxChars, 1, L, f) != L)
+            st = acg::set_error(ACG_ERR_IO, "write failed");
+        }
+      }
+    }
+  }
+  if (path) {
+    if (std::fclose(f) != 0 && st == ACG_OK) st = acg::set_error(ACG_ERR_IO, "close failed");
+  } else {
+    std::fflush(f);
+  }
+  return st;
+}
+
+acg_status acg_mu_write_bin(const char* path, const double* mu, uint64_t rows, uint64_t cols) {
+  acg::clear_error();
+  const uint64_t n = rows * cols;
+  if (!path) return acg::set_error(ACG_ERR_INVALID_ARGUMENT, "acg_mu_write_bin: path is null");
+  if (n && !mu) return acg::set_error(ACG_ERR_INVALID_ARGUMENT, "acg_mu_write_bin: mu is null");
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return acg::set_error(ACG_ERR_IO, "cannot open %s: %s", path, std::strerror(errno));
+  const size_t w = n ? std::fwrite(mu, sizeof(double), (size_t)n, f) : 0;
+  const int c = std::fclose(f);
+  if (w != n || c != 0) return acg::set_error(ACG_ERR_IO, "write to %s failed", path);
   return ACG_OK;
 }
 

@@ -69,6 +69,16 @@ acg_status acg_graph_read_csv(const char* vertex_csv, const char* edges_csv,
 acg_status acg_graph_write_csv(const char* vertex_csv, const char* edges_csv,
                                const acg_host_graph* g);
 
+/* ---------------- mu output -------------------------------------------- */
+/* Write mu [rows][cols] (row-major, host memory) as text, one "%e" value per
+ * line, exactly the characters the reference's printf loop prints
+ * (main.cu:255-257), formatted in parallel.  path NULL writes to stdout. */
+acg_status acg_mu_write_text(const char* path, const double* mu, uint64_t rows,
+                             uint64_t cols);
+/* Write mu [rows][cols] as raw native-endian f64 (no header). */
+acg_status acg_mu_write_bin(const char* path, const double* mu, uint64_t rows,
+                            uint64_t cols);
+
 /* ---------------- seeded generators ------------------------------------ */
 /* Every random value is a pure function of (seed, stream, index), so results
  * do not depend on the thread count.  Features are i.i.d. N(0,1) by the

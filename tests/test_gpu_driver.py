@@ -1,0 +1,56 @@
+"""The native host driver (drop-in for the reference program) on the GPU: its
+"%e" text equals the match to print precision, its binary output equals the
+C-ABI match, and the CSV front end gives the same result."""
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from application_classification_gb300 import build
+
+pytestmark = pytest.mark.gpu
+
+EXE = str(build.BUILD / "acg_main")
+FP64_REL = 1e-10
+
+
+def _golden_paths(tmp_path, name):
+    d, p, ref = load_golden(name)
+    dp, pp = tmp_path / "data.bin", tmp_path / "pattern.bin"
+    d.write_bin(dp)
+    p.write_bin(pp)
+    return d, p, ref, dp, pp
+
+
+def test_driver_text_output(cuda, tmp_path):
+    d, p, ref, dp, pp = _golden_paths(tmp_path, "er300")
+    r = subprocess.run([EXE, str(dp), str(pp)], capture_output=True, text=True, check=True)
+    assert r.stderr.startswith("elapsed=")
+    mu = np.array([float(x) for x in r.stdout.split()]).reshape(d.num_nodes, p.num_nodes)
+    # "%e" keeps 7 significant digits
+    assert np.all(np.abs(mu - ref) <= 5e-7 * np.abs(ref) + 1e-300)
+
+
+def test_driver_binary_output_and_csv_front_end(cuda, tmp_path):
+    d, p, ref, dp, pp = _golden_paths(tmp_path, "rmat9")
+    out = tmp_path / "mu.bin"
+    subprocess.run([EXE, "--binary", "--out", str(out), str(dp), str(pp)], check=True,
+                   capture_output=True)
+    mu = np.fromfile(out, dtype=np.float64).reshape(d.num_nodes, p.num_nodes)
+    assert np.abs(mu - ref).max() <= FP64_REL * max(1.0, np.abs(ref).max())
+    d.write_csv(tmp_path / "d.Vertex.csv", tmp_path / "d.Edges.csv")
+    p.write_csv(tmp_path / "p.Vertex.csv", tmp_path / "p.Edges.csv")
+    out2 = tmp_path / "mu2.bin"
+    subprocess.run([EXE, "--csv", "--binary", "--out", str(out2), str(tmp_path / "d"),
+                    str(tmp_path / "p")], check=True, capture_output=True)
+    assert np.array_equal(np.fromfile(out2, dtype=np.float64), mu.ravel())
+
+
+def test_driver_mixed_precision(cuda, tmp_path):
+    d, p, ref, dp, pp = _golden_paths(tmp_path, "er300")
+    out = tmp_path / "mu.bin"
+    subprocess.run([EXE, "--precision", "mixed", "--binary", "--out", str(out), str(dp), str(pp)],
+                   check=True, capture_output=True)
+    mu = np.fromfile(out, dtype=np.float64).reshape(d.num_nodes, p.num_nodes)
+    assert np.abs(mu - ref).max() <= 1e-4
