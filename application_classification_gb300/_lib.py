@@ -90,6 +90,11 @@ class Stats(C.Structure):
     ]
 
 
+class BatchInfo(C.Structure):
+    _fields_ = [("patterns", i32), ("groups", i32), ("widest_group_columns", i32),
+                ("reserved", i32), ("graph_nodes", i64), ("ms_last", C.c_double)]
+
+
 class AcgError(RuntimeError):
     """A C-ABI call returned a non-zero acg_status."""
 
@@ -113,6 +118,10 @@ SIGNATURES: dict[str, tuple] = {
     "acg_plan_stats": (i32, [vp, _P(Stats)]),
     "acg_match_graphs": (i32, [_P(Graph), _P(Graph), _P(Options), vp, vp]),
     "acg_initial_mu_noalloc": (i32, [vp, u64, u64, vp, u64, vp, vp]),
+    "acg_batch_create": (i32, [vp, vp, i32, _P(Options), vp, _P(vp)]),
+    "acg_batch_match": (i32, [vp, vp, vp]),
+    "acg_batch_get_info": (i32, [vp, _P(BatchInfo)]),
+    "acg_batch_destroy": (i32, [vp]),
     "acg_status_string": (C.c_char_p, [i32]),
     "acg_last_error": (C.c_char_p, []),
     "acg_version": (C.c_char_p, []),

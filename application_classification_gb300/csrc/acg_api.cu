@@ -22,25 +22,10 @@
 #include "acg_cdist.cuh"
 #include "acg_static.cuh"
 #include "acg_iter.cuh"
+#include "acg_plan.h"
 
 using namespace acg;
 
-struct acg_data {
-  int device = 0;
-  int Dn = 0, De = 0, Kv = 0, Ke = 0;
-  const double* node_feats = nullptr;  // caller's device memory
-  const double* edge_feats = nullptr;
-  Csr dcsr;                 // grouped by destination; other = source vertex
-  Csr scsr;                 // grouped by source; other = destination vertex
-  int* pos_in_dst = nullptr;  // [De] dst-CSR row of each src-CSR position
-  int num_sms = kNumSMs;
-  // FP32 copies of the features for the mixed path, built on first use:
-  // nodes [Dn][Kv], edges [De][ke32] in dst-CSR order.
-  float* nf32 = nullptr;
-  float* ef32 = nullptr;
-  int ke32 = 0;
-  std::vector<DevBuf> owned;
-};
 
 namespace {
 acg_status ensure_f32(acg_data* D, cudaStream_t s) {
@@ -69,53 +54,8 @@ struct Cdist<float> {
 };
 }  // namespace
 
-struct acg_plan {
-  acg_data* data = nullptr;
-  int prec = ACG_PREC_FP64;
-  int Pn = 0, Pe = 0, Pp = 0, Pnp = 0, iters = 0;
-  const double* pv = nullptr;  // caller's pattern features (device)
-  const double* pe = nullptr;
-  int* pat = nullptr;          // pattern incidence (device)
-  GroupShape gs{32, 1};      // group shape of the init kernel
-  int init_blocks = 1, cv_blocks = 1, ce_blocks = 1;
-  bool init_warp = false;    // init pass in warp form (small patterns)
-  int qcov = 0, Pqc = 0;     // quirk-buffer columns holding -dE; their padded count
-  // warp work over the destination-sorted CSR (edge phase, and the quirk maxima
-  // over in-edges) and over the source-sorted CSR (static per-vertex reductions)
-  WarpShape ws{32, 1};       // edge phase and source-side pass (all Pp columns)
-  WarpShape qws{32, 1};      // destination-side quirk pass (Pqc columns)
-  WarpWork ew, sw;
-  int edge_blocks = 1, src_blocks = 1, vert_blocks = 1;
-  int maxdeg = 0;  // max over pattern vertices of in- plus out-degree
-  // work buffers (element type per precision)
-  void* dE = nullptr;
-  void* vf = nullptr;
-  void* vr[2] = {nullptr, nullptr};
-  void* dEmin = nullptr;
-  void* B = nullptr;
-  void* CV = nullptr;
-  void* CVlo = nullptr;  // mixed precision: low part of CV
-  void* Rq = nullptr;         // [Dn][Pqc] quirk maxima over out-edges
-  void* Fq = nullptr;         // [Dn][Pqc] quirk maxima over in-edges
-  void* M = nullptr;          // [Dn][Pp] edge-phase maxima
-  void* part_iter = nullptr;
-  void* part_src = nullptr;   // [sw.npartial][3 Pp + Pqc] chunk rows of the source-side pass
-  double* bpart = nullptr;
-  double* gv = nullptr;      // [3 Pn]
-  double* ge = nullptr;      // [Pe]
-  double* gi[2] = {nullptr, nullptr};  // [glob_doubles(Pn, Pe)]
-  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  int kernel_timing = 0;
-  std::vector<cudaEvent_t> kev;  // [2 * iters] around each iteration kernel
-  cudaStream_t last_stream = nullptr;
-  int64_t launches = 0;
-  bool ran = false;
-  std::vector<DevBuf> owned;
-};
 
 namespace {
-
-constexpr int kChunk = 256;
 
 __global__ void validate_edges_kernel(const uint64_t* __restrict__ srcs,
                                       const uint64_t* __restrict__ dsts, long long m,
@@ -156,6 +96,19 @@ __global__ void mu_from_cv_kernel(double* __restrict__ mu, const void* __restric
                         : (double)((const float*)cv)[ci] + (double)cvlo[ci];
   // CV holds dV - LSE(dV); MU0 = -dV - LSE(-dV)
   mu[i] = -(c + gv[Pn + p]) - gv[2 * Pn + p];
+}
+
+// out[m][v][p - p0[m]] = mu[v][p] - S[p] for the member m owning union vertex p
+__global__ void union_scatter_kernel(const double* __restrict__ mu, const double* __restrict__ S,
+                                     long long n, int Pn, const UnionOut uo) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const long long v = i / Pn;
+  const int p = (int)(i - v * Pn);
+  int m = 0;
+  while (m + 1 < uo.n && uo.p0[m + 1] <= p) ++m;
+  const int w = uo.p0[m + 1] - uo.p0[m];
+  uo.out[m][v * w + (p - uo.p0[m])] = mu[i] - S[p];
 }
 
 int elem_bytes(int prec) { return prec == ACG_PREC_FP64 ? 8 : 4; }
@@ -260,13 +213,24 @@ acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* ou
 namespace {
 
 template <typename T>
-acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
+acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s, const UnionOut* uo) {
   acg_data* D = P->data;
   const int Dn = D->Dn, Pn = P->Pn, Pe = P->Pe, Pp = P->Pp;
   const long long De = D->De;
   const long long lim = (long long)Pn * (long long)Dn;
   P->launches = 0;
   cudaEventRecord(P->ev[0], s);
+  if (P->fill_at_run) {  // shared workspaces: rows that no pass writes
+    constexpr T inf = std::numeric_limits<T>::infinity();
+    const size_t nv = (size_t)Dn * Pp, nq = (size_t)Dn * P->Pqc;
+    ACG_TRY(launch_fill<T>((T*)P->M, nv, -inf, s));
+    ACG_TRY(launch_fill<T>((T*)P->dEmin, nv, inf, s));
+    ACG_TRY(launch_fill<T>((T*)P->B, nv, -inf, s));
+    ACG_TRY(launch_fill<T>((T*)P->Rq, nq, -inf, s));
+    ACG_TRY(launch_fill<T>((T*)P->Fq, nq, -inf, s));
+    P->launches += 5;
+  }
+  ACG_CUDA_TRY(cudaMemsetAsync(P->S_final, 0, sizeof(double) * Pn, s));
 
   // ---- cdist (ac.hxx:33-56 via main.cu:109-110) + column stats
   ACG_TRY(Cdist<T>::run(P, D, lim, s));
@@ -275,11 +239,12 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
   if (De > 0) {
     SrcStatsArgs<T> sa{P->sw.items, P->sw.nitems, P->sw.wsplit, D->pos_in_dst, D->scsr.eid,
                        (const T*)P->dE, (T*)P->dEmin, (T*)P->B, (T*)P->Rq,
-                       (T*)P->part_src, De, lim, Pp, P->Pqc, P->qcov};
+                       (T*)P->part_src, P->qlim_col, De, lim, Pp, P->Pqc, P->qcov};
     ACG_TRY(launch_src_stats<T>(sa, P->ws, P->src_blocks, s));
     ACG_TRY(launch_src_stats_combine<T>(sa, P->sw, s));
     DstQuirkArgs<T> qa{P->ew.items, P->ew.nitems, P->ew.wsplit, D->dcsr.eid, (const T*)P->dE,
-                       (T*)P->Fq, (T*)P->part_iter, P->bpart, De, lim, Pp, P->Pqc, P->qcov};
+                       (T*)P->Fq, (T*)P->part_iter, P->bpart, P->qlim_col, De, lim, Pp,
+                       P->Pqc, P->qcov};
     ACG_TRY(launch_dst_quirk<T>(qa, P->qws, P->edge_blocks, s));
     if (P->qcov > 0 && P->ew.nitems > 0) {  // ge[q < Pqc]; the later columns stay -inf
       ACG_TRY(launch_finalize(P->bpart, P->edge_blocks, StatSpec{0, P->Pqc}, P->ge, s));
@@ -295,7 +260,7 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
     InitArgs<T> a{D->dcsr.off, D->scsr.off, (T*)P->CV, (T*)P->CVlo, (const T*)P->Rq,
                   (const T*)P->Fq, (const T*)P->B, (const T*)P->dEmin, (T*)P->vf,
                   (T*)P->vr[0], P->gv, P->ge, P->bpart, P->pat, De, lim, Dn, Pn, Pe, Pp,
-                  P->Pnp, P->Pqc, P->qcov};
+                  P->Pnp, P->Pqc, P->qcov, P->qlim_col};
     if (P->init_warp)
       ACG_TRY(launch_init_warp<T>(a, P->init_blocks, s));
     else
@@ -323,22 +288,30 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s) {
     VertexUpdArgs<T> va{D->dcsr.off, (const T*)P->M, (T*)P->vf, (T*)P->vr[t & 1],
                         (const T*)P->dEmin, (const T*)P->B, (const T*)P->CV,
                         (const T*)P->CVlo, P->gi[(t - 1) & 1], P->gi[t & 1], P->bpart,
-                        mu_out, P->pat, Dn, Pn, Pe, Pp, P->Pnp, P->maxdeg, t == 1,
-                        t == P->iters};
+                        mu_out, P->pat, Dn, Pn, Pe, Pp, P->Pnp, P->maxdeg, P->iters_p, t,
+                        t == 1, t == P->iters};
     ACG_TRY(launch_vertex_update<T>(va, P->vert_blocks, s));
     ACG_TRY(launch_finalize(P->bpart, P->vert_blocks, StatSpec{2 * Pe, 2 * Pe + Pn}, P->gi[t & 1], s));
+    ACG_TRY(launch_capture_s(P->gi[t & 1] + 4 * Pe, P->iters_p, t, P->S_final, Pn, s));
     if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1) + 2], s);
-    P->launches += 2;
+    P->launches += 3;
   }
   cudaEventRecord(P->ev[3], s);
   // ---- output [Dn][Pn] (main.cu:247 transpose is implicit in the layout)
-  if (P->iters > 0) {
-    ACG_TRY(launch_mu_output(mu_out, P->gi[P->iters & 1] + 4 * Pe, Dn, Pn, s));
-  } else {
+  if (P->iters > 0 && !P->is_union) {
+    ACG_TRY(launch_mu_output(mu_out, P->S_final, Dn, Pn, s));
+  } else if (P->iters == 0) {
     const long long n = (long long)Dn * Pn;
     if (n > 0) {
       mu_from_cv_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
           mu_out, P->CV, (const float*)P->CVlo, P->prec == ACG_PREC_FP64, P->gv, n, Pn, P->Pnp);
+      ACG_LAUNCH_CHECK();
+    }
+  }
+  if (P->is_union) {  // MU_raw - S_final into each member's output
+    const long long n = (long long)Dn * Pn;
+    if (n > 0 && uo) {
+      union_scatter_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(mu_out, P->S_final, n, Pn, *uo);
       ACG_LAUNCH_CHECK();
     }
   }
@@ -368,6 +341,244 @@ acg_status Cdist<double>::run(acg_plan* P, acg_data* D, long long lim, cudaStrea
 
 acg_status Cdist<float>::run(acg_plan* P, acg_data* D, long long lim, cudaStream_t s) {
   return run_cdist<float, float>(P, D, lim, D->nf32, D->Kv, D->ef32, D->ke32, false, s);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ plan creation
+namespace acg {
+
+acg_status build_incidence(int pn, int pe, const uint64_t* ps, const uint64_t* pd,
+                           std::vector<int>* out) {
+  std::vector<int>& pat = *out;
+  pat.assign(pattern_ints(pn, pe), 0);
+  int* psrc = pat.data();
+  int* pdst = psrc + pe;
+  int* inoff = pdst + pe;
+  int* inq = inoff + pn + 1;
+  int* outoff = inq + pe;
+  int* outq = outoff + pn + 1;
+  for (int q = 0; q < pe; ++q) {
+    if (ps[q] >= (uint64_t)pn || pd[q] >= (uint64_t)pn)
+      return set_error(ACG_ERR_INDEX_OUT_OF_RANGE, "pattern edge %d endpoint >= %d", q, pn);
+    psrc[q] = (int)ps[q];
+    pdst[q] = (int)pd[q];
+    inoff[pd[q] + 1]++;
+    outoff[ps[q] + 1]++;
+  }
+  for (int p = 0; p < pn; ++p) {
+    inoff[p + 1] += inoff[p];
+    outoff[p + 1] += outoff[p];
+  }
+  std::vector<int> ci(inoff, inoff + pn), co(outoff, outoff + pn);
+  for (int q = 0; q < pe; ++q) {  // ascending q within each vertex's lists
+    inq[ci[pdst[q]]++] = q;
+    outq[co[psrc[q]]++] = q;
+  }
+  return ACG_OK;
+}
+
+acg_status resolve_options(const acg_options* opt, acg_options* o) {
+  acg_options_default(o);
+  if (opt) *o = *opt;
+  if (o->precision != ACG_PREC_FP64 && o->precision != ACG_PREC_MIXED)
+    return set_error(ACG_ERR_INVALID_ARGUMENT, "unknown precision %d", o->precision);
+  return ACG_OK;
+}
+
+// The work split for (CSR, warps, step), built once per data graph.
+static acg_status get_work(acg_data* D, int which, int nwarps, int step, WarpWork* out,
+                           cudaStream_t s) {
+  const auto key = std::make_tuple(which, nwarps, step);
+  auto it = D->work.find(key);
+  if (it == D->work.end()) {
+    WarpWork w;
+    ACG_TRY(build_warp_work(which == 0 ? D->dcsr : D->scsr, nwarps, step, &w, &D->owned, s));
+    it = D->work.emplace(key, w).first;
+  }
+  *out = it->second;
+  return ACG_OK;
+}
+
+acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& o, cudaStream_t s,
+                            bool deferred, acg_plan** out) {
+  std::unique_ptr<acg_plan> P(new acg_plan());
+  P->data = D;
+  P->prec = o.precision;
+  P->Pn = spec.Pn;
+  P->Pe = spec.Pe;
+  P->iters = 0;
+  for (int x : spec.iters_p) P->iters = std::max(P->iters, x);
+  P->pv = spec.pv;
+  P->pe = spec.pe;
+  P->is_union = spec.is_union;
+  P->fill_at_run = deferred;
+  const int eb = elem_bytes(P->prec);
+  const int W = 16 / eb;
+  P->Pp = std::max(W, (P->Pe + W - 1) / W * W);
+  P->Pnp = (P->Pn + W - 1) / W * W;
+  const int Pn = P->Pn, Pe = P->Pe, Pp = P->Pp, Dn = D->Dn, De = D->De;
+  auto fail = [&](acg_status st) {
+    dev_free_all(&P->owned);
+    return st;
+  };
+  acg_status st = ACG_OK;
+  auto alloc = [&](size_t bytes, void** p) {
+    if (st == ACG_OK) st = dev_alloc(&P->owned, bytes, p, s);
+  };
+  auto big = [&](size_t bytes, void** p) {  // the large workspaces
+    if (deferred) {
+      *p = nullptr;
+      P->big.emplace_back(std::max<size_t>(bytes, 1), p);
+    } else {
+      alloc(bytes, p);
+    }
+  };
+  alloc(sizeof(int) * spec.pat.size(), (void**)&P->pat);
+  alloc(sizeof(int) * std::max(1, Pn), (void**)&P->iters_p);
+  alloc(sizeof(long long) * Pp, (void**)&P->qlim_col);
+  alloc(sizeof(double) * std::max(1, Pn), (void**)&P->S_final);
+  if (st != ACG_OK) return fail(st);
+  std::vector<long long> qlim(Pp, 0);
+  std::copy(spec.qlim.begin(), spec.qlim.end(), qlim.begin());
+  ACG_CUDA_TRY(cudaMemcpyAsync(P->pat, spec.pat.data(), sizeof(int) * spec.pat.size(),
+                               cudaMemcpyHostToDevice, s));
+  if (Pn > 0)
+    ACG_CUDA_TRY(cudaMemcpyAsync(P->iters_p, spec.iters_p.data(), sizeof(int) * Pn,
+                                 cudaMemcpyHostToDevice, s));
+  ACG_CUDA_TRY(cudaMemcpyAsync(P->qlim_col, qlim.data(), sizeof(long long) * Pp,
+                               cudaMemcpyHostToDevice, s));
+  // covered columns form a prefix (a union orders them first)
+  P->qcov = 0;
+  while (P->qcov < Pe && qlim[P->qcov] > 0) ++P->qcov;
+
+  if (P->prec == ACG_PREC_MIXED) st = ensure_f32(D, s);
+  if (st != ACG_OK) return fail(st);
+
+  P->ws = choose_warp_shape(eb, Pp);
+  // edge phase: one wave of resident blocks (8 warps each)
+  {
+    const int fit = eb == 8 ? edge_max_blocks_per_sm<double>(P->ws) : edge_max_blocks_per_sm<float>(P->ws);
+    P->edge_blocks = D->num_sms * (o.edge_blocks_per_sm > 0 ? std::min(fit, o.edge_blocks_per_sm) : fit);
+  }
+  st = get_work(D, 0, P->edge_blocks * 8, edge_step(P->ws), &P->ew, s);
+  if (st != ACG_OK) return fail(st);
+  // source-side static pass: one wave of resident blocks over the source CSR
+  {
+    const int fit = eb == 8 ? src_stats_blocks_per_sm<double>(P->ws) : src_stats_blocks_per_sm<float>(P->ws);
+    P->src_blocks = D->num_sms * (o.edge_blocks_per_sm > 0 ? std::min(fit, o.edge_blocks_per_sm) : fit);
+  }
+  st = get_work(D, 1, P->src_blocks * 8, edge_step(P->ws), &P->sw, s);
+  if (st != ACG_OK) return fail(st);
+  P->Pqc = std::max(W, (P->qcov + W - 1) / W * W);
+  P->qws = choose_warp_shape(eb, P->Pqc);
+  P->gs = choose_shape(eb, Pp, Pn);
+  const int GPB = 256 / P->gs.G;
+  const int nsm = D->num_sms;
+  {
+    const int* io = spec.pat.data() + 2 * Pe;  // in_off, then in_q, then out_off
+    const int* oo = io + Pn + 1 + Pe;
+    int md = 0;
+    for (int p = 0; p < Pn; ++p) md = std::max(md, io[p + 1] - io[p] + oo[p + 1] - oo[p]);
+    P->maxdeg = md;
+    P->vert_blocks = eb == 8 ? vertex_update_blocks<double>(Pn, Pe, Pp, P->Pnp, md, nsm, Dn)
+                             : vertex_update_blocks<float>(Pn, Pe, Pp, P->Pnp, md, nsm, Dn);
+    if (o.vertex_blocks_per_sm > 0)
+      P->vert_blocks = std::min(P->vert_blocks, nsm * o.vertex_blocks_per_sm);
+  }
+  P->init_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), GPB), nsm * 4));
+  {
+    const int ib = eb == 8 ? init_warp_blocks<double>(Pn, Pe, Pp, nsm)
+                           : init_warp_blocks<float>(Pn, Pe, Pp, nsm);
+    if (ib > 0) {
+      P->init_warp = true;
+      P->init_blocks = ib;
+    }
+  }
+  P->cv_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), 64), nsm * 2));
+  P->ce_blocks = std::max(1, std::min(ceil_div(std::max(1, De), 256), nsm * 8));
+
+  const size_t vrow = (size_t)Dn * Pp * eb;
+  big((size_t)De * Pp * eb, &P->dE);
+  big(vrow, &P->vf);
+  big(vrow, &P->vr[0]);
+  big(vrow, &P->vr[1]);
+  big(vrow, &P->dEmin);
+  big(vrow, &P->B);
+  big((size_t)Dn * P->Pqc * eb, &P->Rq);
+  big((size_t)Dn * P->Pqc * eb, &P->Fq);
+  big((size_t)Dn * P->Pnp * eb, &P->CV);
+  if (P->prec == ACG_PREC_MIXED) big((size_t)Dn * P->Pnp * eb, &P->CVlo);
+  big(vrow, &P->M);
+  big((size_t)std::max(1, P->ew.npartial) * Pp * eb, &P->part_iter);
+  big((size_t)std::max(1, P->sw.npartial) * (3 * Pp + P->Pqc) * eb, &P->part_src);
+  if (!deferred && st == ACG_OK) {
+    // rows that no pass writes: vertices without in-edges (M = -inf) or
+    // without out-edges (dEmin = +inf, B = -inf, quirk maxima -inf)
+    const size_t nv = (size_t)Dn * Pp, nq = (size_t)Dn * P->Pqc;
+    if (eb == 8) {
+      constexpr double inf = std::numeric_limits<double>::infinity();
+      st = launch_fill<double>((double*)P->M, nv, -inf, s);
+      if (st == ACG_OK) st = launch_fill<double>((double*)P->dEmin, nv, inf, s);
+      if (st == ACG_OK) st = launch_fill<double>((double*)P->B, nv, -inf, s);
+      if (st == ACG_OK) st = launch_fill<double>((double*)P->Rq, nq, -inf, s);
+      if (st == ACG_OK) st = launch_fill<double>((double*)P->Fq, nq, -inf, s);
+    } else {
+      constexpr float inf = std::numeric_limits<float>::infinity();
+      st = launch_fill<float>((float*)P->M, nv, -inf, s);
+      if (st == ACG_OK) st = launch_fill<float>((float*)P->dEmin, nv, inf, s);
+      if (st == ACG_OK) st = launch_fill<float>((float*)P->B, nv, -inf, s);
+      if (st == ACG_OK) st = launch_fill<float>((float*)P->Rq, nq, -inf, s);
+      if (st == ACG_OK) st = launch_fill<float>((float*)P->Fq, nq, -inf, s);
+    }
+  }
+  const size_t bp = std::max({(size_t)(6 * Pe + 2 * Pn) * P->vert_blocks,
+                              (size_t)5 * Pn * P->cv_blocks, (size_t)6 * Pe * P->init_blocks,
+                              (size_t)2 * P->Pqc * P->edge_blocks});
+  alloc(sizeof(double) * bp, (void**)&P->bpart);
+  alloc(sizeof(double) * 3 * Pn, (void**)&P->gv);
+  alloc(sizeof(double) * std::max(P->Pqc, Pe), (void**)&P->ge);
+  if (st == ACG_OK)  // columns without covered elements (and the case De = 0)
+    st = launch_fill<double>(P->ge, (size_t)std::max(P->Pqc, Pe), -std::numeric_limits<double>::infinity(), s);
+  alloc(sizeof(double) * glob_doubles(Pn, Pe), (void**)&P->gi[0]);
+  alloc(sizeof(double) * glob_doubles(Pn, Pe), (void**)&P->gi[1]);
+  if (st != ACG_OK) return fail(st);
+  for (auto& e : P->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "cudaEventCreate failed"));
+  P->kernel_timing = o.kernel_timing;
+  if (P->kernel_timing) {
+    P->kev.assign(3 * (size_t)P->iters, nullptr);
+    for (auto& e : P->kev)
+      if (cudaEventCreate(&e) != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "cudaEventCreate failed"));
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess)
+    return fail(set_error(ACG_ERR_CUDA, "acg_plan_create: %s", cudaGetErrorString(cudaGetLastError())));
+  *out = P.release();
+  return ACG_OK;
+}
+
+acg_status run_match_any(acg_plan* P, double* mu_out, cudaStream_t s, const UnionOut* uo) {
+  return P->prec == ACG_PREC_FP64 ? run_match<double>(P, mu_out, s, uo)
+                                  : run_match<float>(P, mu_out, s, uo);
+}
+
+}  // namespace acg
+
+namespace {
+
+acg_status check_pattern(const acg_data* D, const acg_graph* pg) {
+  if (pg->num_nodes == 0) return set_error(ACG_ERR_INVALID_ARGUMENT, "pattern has no vertices");
+  if (pg->node_feat_dim != (uint64_t)D->Kv || pg->edge_feat_dim != (uint64_t)D->Ke)
+    return set_error(ACG_ERR_INVALID_ARGUMENT,
+                     "feature dims differ: data %d/%d, pattern %llu/%llu", D->Kv, D->Ke,
+                     (unsigned long long)pg->node_feat_dim, (unsigned long long)pg->edge_feat_dim);
+  if (pg->num_nodes > 128 || pg->num_edges > 256)
+    return set_error(ACG_ERR_UNSUPPORTED,
+                     "pattern with %llu vertices / %llu edges: at most 128 / 256 are supported",
+                     (unsigned long long)pg->num_nodes, (unsigned long long)pg->num_edges);
+  if (D->Kv > 1024 || D->Ke > 1024)
+    return set_error(ACG_ERR_UNSUPPORTED, "feature dimension above 1024");
+  return ACG_OK;
 }
 
 }  // namespace
@@ -460,36 +671,10 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
   if (!D) return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_plan_create: data is null");
   ACG_TRY(check_graph(pg, "pattern", true));
   acg_options o;
-  acg_options_default(&o);
-  if (opt) o = *opt;
-  if (o.precision != ACG_PREC_FP64 && o.precision != ACG_PREC_MIXED)
-    return set_error(ACG_ERR_INVALID_ARGUMENT, "unknown precision %d", o.precision);
-  if (pg->num_nodes == 0) return set_error(ACG_ERR_INVALID_ARGUMENT, "pattern has no vertices");
-  if (pg->node_feat_dim != (uint64_t)D->Kv || pg->edge_feat_dim != (uint64_t)D->Ke)
-    return set_error(ACG_ERR_INVALID_ARGUMENT,
-                     "feature dims differ: data %d/%d, pattern %llu/%llu", D->Kv, D->Ke,
-                     (unsigned long long)pg->node_feat_dim, (unsigned long long)pg->edge_feat_dim);
-  if (pg->num_nodes > 128 || pg->num_edges > 256)
-    return set_error(ACG_ERR_UNSUPPORTED,
-                     "pattern with %llu vertices / %llu edges: at most 128 / 256 are supported",
-                     (unsigned long long)pg->num_nodes, (unsigned long long)pg->num_edges);
-  if (D->Kv > 1024 || D->Ke > 1024)
-    return set_error(ACG_ERR_UNSUPPORTED, "feature dimension above 1024");
+  ACG_TRY(resolve_options(opt, &o));
+  ACG_TRY(check_pattern(D, pg));
   cudaStream_t s = (cudaStream_t)stream;
-  std::unique_ptr<acg_plan> P(new acg_plan());
-  P->data = D;
-  P->prec = o.precision;
-  P->Pn = (int)pg->num_nodes;
-  P->Pe = (int)pg->num_edges;
-  P->iters = o.num_iters < 0 ? P->Pn : o.num_iters;
-  P->pv = pg->node_feats;
-  P->pe = pg->edge_feats;
-  const int eb = elem_bytes(P->prec);
-  const int W = 16 / eb;
-  P->Pp = std::max(W, (P->Pe + W - 1) / W * W);
-  P->Pnp = (P->Pn + W - 1) / W * W;
-  const int Pn = P->Pn, Pe = P->Pe, Pp = P->Pp, Dn = D->Dn, De = D->De;
-
+  const int Pn = (int)pg->num_nodes, Pe = (int)pg->num_edges;
   // pattern incidence (host build from the device endpoint arrays)
   std::vector<uint64_t> ps(Pe), pd(Pe);
   if (Pe > 0) {
@@ -497,149 +682,17 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
     ACG_CUDA_TRY(cudaMemcpyAsync(pd.data(), pg->dsts, 8 * (size_t)Pe, cudaMemcpyDeviceToHost, s));
     ACG_CUDA_TRY(cudaStreamSynchronize(s));
   }
-  std::vector<int> pat(pattern_ints(Pn, Pe));
-  {
-    int* psrc = pat.data();
-    int* pdst = psrc + Pe;
-    int* inoff = pdst + Pe;
-    int* inq = inoff + Pn + 1;
-    int* outoff = inq + Pe;
-    int* outq = outoff + Pn + 1;
-    for (int q = 0; q < Pe; ++q) {
-      if (ps[q] >= (uint64_t)Pn || pd[q] >= (uint64_t)Pn)
-        return set_error(ACG_ERR_INDEX_OUT_OF_RANGE, "pattern edge %d endpoint >= %d", q, Pn);
-      psrc[q] = (int)ps[q];
-      pdst[q] = (int)pd[q];
-      inoff[pd[q] + 1]++;
-      outoff[ps[q] + 1]++;
-    }
-    for (int p = 0; p < Pn; ++p) {
-      inoff[p + 1] += inoff[p];
-      outoff[p + 1] += outoff[p];
-    }
-    std::vector<int> ci(inoff, inoff + Pn), co(outoff, outoff + Pn);
-    for (int q = 0; q < Pe; ++q) {
-      inq[ci[pdst[q]]++] = q;
-      outq[co[psrc[q]]++] = q;
-    }
-  }
-  auto fail = [&](acg_status st) {
-    dev_free_all(&P->owned);
-    return st;
-  };
-  acg_status st = ACG_OK;
-  auto alloc = [&](size_t bytes, void** p) {
-    if (st == ACG_OK) st = dev_alloc(&P->owned, bytes, p, s);
-  };
-  alloc(sizeof(int) * pat.size(), (void**)&P->pat);
-  if (st != ACG_OK) return fail(st);
-  ACG_CUDA_TRY(cudaMemcpyAsync(P->pat, pat.data(), sizeof(int) * pat.size(), cudaMemcpyHostToDevice, s));
-
-  if (P->prec == ACG_PREC_MIXED) st = ensure_f32(D, s);
-  if (st != ACG_OK) return fail(st);
-
-  P->ws = choose_warp_shape(eb, Pp);
-  // edge phase: one wave of resident blocks (8 warps each)
-  {
-    const int fit = eb == 8 ? edge_max_blocks_per_sm<double>(P->ws) : edge_max_blocks_per_sm<float>(P->ws);
-    P->edge_blocks = D->num_sms * (o.edge_blocks_per_sm > 0 ? std::min(fit, o.edge_blocks_per_sm) : fit);
-  }
-  st = build_warp_work(D->dcsr, P->edge_blocks * 8, edge_step(P->ws), &P->ew, &P->owned, s);
-  if (st != ACG_OK) return fail(st);
-  // source-side static pass: one wave of resident blocks over the source CSR
-  {
-    const int fit = eb == 8 ? src_stats_blocks_per_sm<double>(P->ws) : src_stats_blocks_per_sm<float>(P->ws);
-    P->src_blocks = D->num_sms * (o.edge_blocks_per_sm > 0 ? std::min(fit, o.edge_blocks_per_sm) : fit);
-  }
-  st = build_warp_work(D->scsr, P->src_blocks * 8, edge_step(P->ws), &P->sw, &P->owned, s);
-  if (st != ACG_OK) return fail(st);
-  P->qcov = quirk_columns((long long)Pn * Dn, De, Pe);
-  P->Pqc = std::max(W, (P->qcov + W - 1) / W * W);
-  P->qws = choose_warp_shape(eb, P->Pqc);
-  P->gs = choose_shape(eb, Pp, Pn);
-  const int GPB = 256 / P->gs.G;
-  const int nsm = D->num_sms;
-  {
-    const int* io = pat.data() + 2 * Pe;  // in_off, then in_q, then out_off
-    const int* oo = io + Pn + 1 + Pe;
-    int md = 0;
-    for (int p = 0; p < Pn; ++p) md = std::max(md, io[p + 1] - io[p] + oo[p + 1] - oo[p]);
-    P->maxdeg = md;
-    P->vert_blocks = eb == 8 ? vertex_update_blocks<double>(Pn, Pe, Pp, P->Pnp, md, nsm, Dn)
-                             : vertex_update_blocks<float>(Pn, Pe, Pp, P->Pnp, md, nsm, Dn);
-    if (o.vertex_blocks_per_sm > 0)
-      P->vert_blocks = std::min(P->vert_blocks, nsm * o.vertex_blocks_per_sm);
-  }
-  P->init_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), GPB), nsm * 4));
-  {
-    const int ib = eb == 8 ? init_warp_blocks<double>(Pn, Pe, Pp, nsm)
-                           : init_warp_blocks<float>(Pn, Pe, Pp, nsm);
-    if (ib > 0) {
-      P->init_warp = true;
-      P->init_blocks = ib;
-    }
-  }
-  P->cv_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), 64), nsm * 2));
-  P->ce_blocks = std::max(1, std::min(ceil_div(std::max(1, De), 256), nsm * 8));
-
-  const size_t vrow = (size_t)Dn * Pp * eb;
-  alloc((size_t)De * Pp * eb, &P->dE);
-  alloc(vrow, &P->vf);
-  alloc(vrow, &P->vr[0]);
-  alloc(vrow, &P->vr[1]);
-  alloc(vrow, &P->dEmin);
-  alloc(vrow, &P->B);
-  alloc((size_t)Dn * P->Pqc * eb, &P->Rq);
-  alloc((size_t)Dn * P->Pqc * eb, &P->Fq);
-  alloc((size_t)Dn * P->Pnp * eb, &P->CV);
-  if (P->prec == ACG_PREC_MIXED) alloc((size_t)Dn * P->Pnp * eb, &P->CVlo);
-  alloc(vrow, &P->M);
-  // rows of vertices without in-edges are never written by the edge phase
-  if (st == ACG_OK)
-    st = eb == 8 ? launch_fill<double>((double*)P->M, (size_t)Dn * Pp, -std::numeric_limits<double>::infinity(), s)
-                 : launch_fill<float>((float*)P->M, (size_t)Dn * Pp, -std::numeric_limits<float>::infinity(), s);
-  alloc((size_t)std::max(1, P->ew.npartial) * Pp * eb, &P->part_iter);
-  alloc((size_t)std::max(1, P->sw.npartial) * (3 * Pp + P->Pqc) * eb, &P->part_src);
-  // rows of vertices without out-edges (in-edges) are never written by the
-  // static passes: dEmin = +inf, B = -inf (and -inf quirk maxima, unused)
-  if (st == ACG_OK) {
-    const size_t nv = (size_t)Dn * Pp, nq = (size_t)Dn * P->Pqc;
-    if (eb == 8) {
-      st = launch_fill<double>((double*)P->dEmin, nv, std::numeric_limits<double>::infinity(), s);
-      if (st == ACG_OK) st = launch_fill<double>((double*)P->B, nv, -std::numeric_limits<double>::infinity(), s);
-      if (st == ACG_OK) st = launch_fill<double>((double*)P->Rq, nq, -std::numeric_limits<double>::infinity(), s);
-      if (st == ACG_OK) st = launch_fill<double>((double*)P->Fq, nq, -std::numeric_limits<double>::infinity(), s);
-    } else {
-      st = launch_fill<float>((float*)P->dEmin, nv, std::numeric_limits<float>::infinity(), s);
-      if (st == ACG_OK) st = launch_fill<float>((float*)P->B, nv, -std::numeric_limits<float>::infinity(), s);
-      if (st == ACG_OK) st = launch_fill<float>((float*)P->Rq, nq, -std::numeric_limits<float>::infinity(), s);
-      if (st == ACG_OK) st = launch_fill<float>((float*)P->Fq, nq, -std::numeric_limits<float>::infinity(), s);
-    }
-  }
-  const size_t bp = std::max({(size_t)(6 * Pe + 2 * Pn) * P->vert_blocks,
-                              (size_t)5 * Pn * P->cv_blocks, (size_t)2 * Pe * P->ce_blocks,
-                              (size_t)6 * Pe * P->init_blocks,
-                              (size_t)2 * P->Pqc * P->edge_blocks});
-  alloc(sizeof(double) * bp, (void**)&P->bpart);
-  alloc(sizeof(double) * 3 * Pn, (void**)&P->gv);
-  alloc(sizeof(double) * std::max(P->Pqc, Pe), (void**)&P->ge);
-  if (st == ACG_OK)  // columns without covered elements (and the case De = 0)
-    st = launch_fill<double>(P->ge, (size_t)std::max(P->Pqc, Pe), -std::numeric_limits<double>::infinity(), s);
-  alloc(sizeof(double) * glob_doubles(Pn, Pe), (void**)&P->gi[0]);
-  alloc(sizeof(double) * glob_doubles(Pn, Pe), (void**)&P->gi[1]);
-  if (st != ACG_OK) return fail(st);
-  for (auto& e : P->ev)
-    if (cudaEventCreate(&e) != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "cudaEventCreate failed"));
-  P->kernel_timing = o.kernel_timing;
-  if (P->kernel_timing) {
-    P->kev.assign(3 * (size_t)P->iters, nullptr);
-    for (auto& e : P->kev)
-      if (cudaEventCreate(&e) != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "cudaEventCreate failed"));
-  }
-  if (cudaStreamSynchronize(s) != cudaSuccess)
-    return fail(set_error(ACG_ERR_CUDA, "acg_plan_create: %s", cudaGetErrorString(cudaGetLastError())));
-  *out = P.release();
-  return ACG_OK;
+  PatternSpec spec;
+  spec.Pn = Pn;
+  spec.Pe = Pe;
+  ACG_TRY(build_incidence(Pn, Pe, ps.data(), pd.data(), &spec.pat));
+  const long long lim = (long long)Pn * D->Dn;
+  spec.qlim.resize(Pe);
+  for (int q = 0; q < Pe; ++q) spec.qlim[q] = std::max(0LL, lim - (long long)q * D->De);
+  spec.iters_p.assign(Pn, o.num_iters < 0 ? Pn : o.num_iters);
+  spec.pv = pg->node_feats;
+  spec.pe = pg->edge_feats;
+  return plan_create_impl(D, std::move(spec), o, s, false, out);
 }
 
 acg_status acg_plan_destroy(acg_plan* P) {
@@ -661,8 +714,7 @@ acg_status acg_match(acg_plan* P, double* mu_out, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
   P->last_stream = s;
   if (P->data->Dn == 0) return ACG_OK;
-  acg_status st = P->prec == ACG_PREC_FP64 ? run_match<double>(P, mu_out, s)
-                                           : run_match<float>(P, mu_out, s);
+  acg_status st = run_match_any(P, mu_out, s, nullptr);
   P->ran = st == ACG_OK;
   return st;
 }

@@ -221,7 +221,7 @@ init_vertex_kernel(const InitArgs<T> a) {
     s_vfmax0[q] = a.gv[s_pdst[q]] - a.gv[2 * Pn + s_pdst[q]];
     s_vrmax0[q] = a.gv[s_psrc[q]] - a.gv[2 * Pn + s_psrc[q]];
     // zeros of quirk row q: elements with flat index >= lim
-    long long covered = a.lim - (long long)q * a.De;
+    long long covered = a.qlim_col[q];
     covered = covered < 0 ? 0 : (covered > a.De ? a.De : covered);
     LseD r;  // LSE of the whole quirk row: covered part (ge) plus its zeros
     r.init();

@@ -59,6 +59,7 @@ struct InitArgs {
   long long lim;
   int Dn, Pn, Pe, Pp, Pnp;
   int Pqc, qcov;       // (the later quirk columns are zero over any edge)
+  const long long* qlim_col;  // [Pe] column q covers original edge ids < qlim_col[q]
 };
 template <typename T>
 acg_status launch_init_vertex(const InitArgs<T>& a, GroupShape gs, int blocks, cudaStream_t s);

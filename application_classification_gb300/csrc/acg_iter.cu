@@ -338,6 +338,7 @@ vertex_update_kernel(const VertexUpdArgs<T> a) {
   }
   const int in0 = s_inoff[pc], in1 = s_inoff[pc + 1];
   const int out0 = s_outoff[pc], out1 = s_outoff[pc + 1];
+  const bool my_last = __ldg(a.iters_p + pc) == a.t;
   T mxF[W], mxR[W];
   OnlineLse<T> lr[W], lf[W], lmu;
 #pragma unroll
@@ -439,7 +440,7 @@ vertex_update_kernel(const VertexUpdArgs<T> a) {
       s_MU[j * Pn + pc] = mu.hi;
       if constexpr (sizeof(T) == 4) s_MUlo[j * Pn + pc] = mu.lo;
       lmu.add2(mu.hi, mu.lo);
-      if (a.last) a.mu_raw[(size_t)vv * Pn + pc] = mu.dvalue();
+      if (my_last) a.mu_raw[(size_t)vv * Pn + pc] = mu.dvalue();
     }
     __syncthreads();
     if (!a.last && vok) {
@@ -680,6 +681,7 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
   }
   T mxF[QPL], mxR[QPL];
   OnlineLse<T> lr[QPL], lf[QPL], lmu[PPL];
+  bool plast[PPL];  // this iteration is the last of pattern vertex p's pattern
 #pragma unroll
   for (int k = 0; k < QPL; ++k) {
     mxF[k] = mxR[k] = neg_inf<T>();
@@ -687,7 +689,11 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
     lf[k].init();
   }
 #pragma unroll
-  for (int j = 0; j < PPL; ++j) lmu[j].init();
+  for (int j = 0; j < PPL; ++j) {
+    lmu[j].init();
+    const int p = lane + 32 * j;
+    plast[j] = p < Pn && __ldg(a.iters_p + p) == a.t;
+  }
   __syncthreads();  // s_inc complete
 
   const long long nw = (long long)gridDim.x * kVw;
@@ -762,7 +768,7 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
         if constexpr (sizeof(T) == 4) smu[32 * PPL + p] = mu.lo;
         if (p < Pn) {
           lmu[j].add2(mu.hi, mu.lo);
-          if (a.last) a.mu_raw[(size_t)v * Pn + p] = mu.dvalue();
+          if (plast[j]) a.mu_raw[(size_t)v * Pn + p] = mu.dvalue();
         }
       }
       __syncwarp();
@@ -825,6 +831,12 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
   }
   __syncthreads();
   write_block_partials(red, kVw, nmax, nlse, a.bpart, gridDim.x, blockIdx.x);
+}
+
+__global__ void capture_s_kernel(const double* __restrict__ S, const int* __restrict__ iters_p,
+                                 int t, double* __restrict__ S_final, int Pn) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < Pn && iters_p[p] == t) S_final[p] = S[p];
 }
 
 template <typename T>
@@ -959,6 +971,14 @@ int vertex_update_blocks(int pn, int pe, int pp, int pnp, int maxdeg, int num_sm
   const long long tiles = (dn + V - 1) / V;
   const long long b = (long long)num_sms * vertex_update_blocks_per_sm<T>(pn, pe, pp);
   return (int)(tiles < 1 ? 1 : (tiles < b ? tiles : b));
+}
+
+acg_status launch_capture_s(const double* S, const int* iters_p, int t, double* S_final, int Pn,
+                            cudaStream_t s) {
+  if (Pn == 0) return ACG_OK;
+  capture_s_kernel<<<ceil_div(Pn, 128), 128, 0, s>>>(S, iters_p, t, S_final, Pn);
+  ACG_LAUNCH_CHECK();
+  return ACG_OK;
 }
 
 template <typename T>

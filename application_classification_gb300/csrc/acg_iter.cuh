@@ -47,8 +47,15 @@ struct VertexUpdArgs {
   const int* pat;
   int Dn, Pn, Pe, Pp, Pnp;
   int maxdeg;          // max over pattern vertices of in- plus out-degree
-  int first, last;
+  const int* iters_p;  // [Pn] iteration count of each pattern vertex's pattern:
+                       // MU_raw is written at iteration t == iters_p[p]
+  int t;               // this iteration (1-based)
+  int first, last;     // first iteration; last iteration of every pattern
 };
+// S_final[p] = S[p] of this iteration where it is p's last (S = the column
+// log-sum-exp of MU_raw in the statistics just finalised).
+acg_status launch_capture_s(const double* S, const int* iters_p, int t, double* S_final, int Pn,
+                            cudaStream_t s);
 
 struct WarpShape {
   int npow;  // lanes covering one [Pp] row (power of two <= 32)

@@ -124,7 +124,7 @@ src_stats_kernel(const SrcStatsArgs<T> a) {
     sm[k] = T(0);
     sc[k] = T(0);
     const int q = (qc + NPOW * (k / W)) * W + k % W;
-    qlim[k] = q < qcov ? a.lim - (long long)q * a.De : 0;
+    qlim[k] = q < qcov ? __ldg(a.qlim_col + q) : 0;
   }
   for (;;) {
     VT x[kSU][NQV];
@@ -312,7 +312,7 @@ dst_quirk_kernel(const DstQuirkArgs<T> a) {
     qx[k] = neg_inf<T>();
     ls[k].init();
     const int q = (qc + NPOW * (k / W)) * W + k % W;
-    qlim[k] = q < qcov ? a.lim - (long long)q * a.De : 0;
+    qlim[k] = q < qcov ? __ldg(a.qlim_col + q) : 0;
   }
   if (it < it_end) {
     int4 item = __ldg(a.items + it);
@@ -445,7 +445,7 @@ init_warp_kernel(const InitArgs<T> a) {
       vfm[k] = (T)(gv[qd[k]] - gv[2 * Pn + qd[k]]);  // max_v MU0[dst_q]
       vrm[k] = (T)(gv[qs[k]] - gv[2 * Pn + qs[k]]);
       // LSE of the whole quirk row q: its covered part, plus exp(0) per zero
-      long long covered = a.lim - (long long)q * a.De;
+      long long covered = a.qlim_col[q];
       covered = covered < 0 ? 0 : (covered > a.De ? a.De : covered);
       LseD r;
       r.init();

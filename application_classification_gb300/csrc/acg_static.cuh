@@ -12,8 +12,11 @@
 namespace acg {
 
 // Quirk buffer of main.cu:113-114: element (q, e) holds -dE[q, e] if its flat
-// index q * De + e is below lim = Pn * Dn, else 0.  Only columns q < qcov =
-// ceil(lim / De) hold any -dE; the later ones are all zero.
+// index q * De + e is below lim = Pn * Dn, else 0: column q covers the original
+// edge ids below qlim[q] = lim - q * De.  Only columns q < qcov = ceil(lim / De)
+// hold any -dE; the later ones are all zero.  (A group of patterns matched as
+// one disjoint union keeps each pattern's own Pn and local q in qlim, with the
+// covered columns of all its patterns ordered first.)
 inline int quirk_columns(long long lim, long long de, int pe) {
   if (de <= 0) return 0;
   const long long c = (lim + de - 1) / de;
@@ -36,6 +39,7 @@ struct SrcStatsArgs {
   T* B;                // [Dn][Pp]
   T* Rq;               // [Dn][Pqc] quirk maximum over out-edges (columns < qcov)
   T* partial;          // [npartial][3 Pp + Pqc]: min | lse max | lse sum | quirk
+  const long long* qlim_col;  // [Pp] column q covers original edge ids < qlim_col[q]
   long long De, lim;
   int Pp, Pqc, qcov;
 };
@@ -59,6 +63,7 @@ struct DstQuirkArgs {
   T* Fq;               // [Dn][Pqc]
   T* partial;          // [npartial][Pqc]
   double* bpart;       // [2 Pqc][blocks]
+  const long long* qlim_col;  // [Pp] as for the source side
   long long De, lim;
   int Pp, Pqc, qcov;
 };

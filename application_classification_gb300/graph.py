@@ -248,3 +248,22 @@ def workload(name: str):
     d = gen_rmat(s, 16, seed=seed)
     d, p, tv, _ = plant(d, pn, pe, 0.05, seed=seed)
     return d, p, tv
+
+
+def batch_workload(scale: int = 20, npatterns: int = 64, seed: int = 3):
+    """Many patterns of uneven size planted in one R-MAT graph.
+
+    Data: R-MAT scale ``scale``, edge factor 16, seed ``seed``.  Pattern i:
+    Pn uniform in 4..48, Pe uniform in 2 Pn..4 Pn, planted with seed
+    1000 * seed + i (features + N(0, 0.05^2)).  Returns (data, patterns,
+    truth_vertices)."""
+    rng = np.random.default_rng(seed)
+    d = gen_rmat(scale, 16, seed=seed)
+    pats, truths = [], []
+    for i in range(npatterns):
+        pn = int(rng.integers(4, 49))
+        pe = int(rng.integers(2 * pn, 4 * pn + 1))
+        d, p, tv, _ = plant(d, pn, pe, 0.05, seed=1000 * seed + i)
+        pats.append(p)
+        truths.append(tv)
+    return d, pats, truths

@@ -173,3 +173,61 @@ def match(data: Graph, pattern: Graph, precision: str = "fp64", num_iters: int =
                                            C.c_void_p(out.data_ptr()), _stream_ptr(None)),
                "acg_match_graphs")
     return out.cpu().numpy()
+
+
+class Batch:
+    """``acg_batch``: many patterns matched against one :class:`DataGraph`.
+
+    The patterns are packed into groups matched as disjoint unions and the whole
+    batch runs as one CUDA graph launch per :meth:`run`."""
+
+    def __init__(self, data: DataGraph, patterns, precision: str = "fp64", num_iters: int = -1,
+                 stream=None):
+        self.data = data
+        self.pats = [p if isinstance(p, DeviceGraph) else DeviceGraph(p) for p in patterns]
+        arr = (_lib.Graph * len(self.pats))(*[p.c_graph() for p in self.pats])
+        self._arr = arr
+        opt = _lib.Options()
+        _lib.lib().acg_options_default(C.byref(opt))
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
+        opt.precision = PRECISIONS[precision]
+        opt.num_iters = num_iters
+        self.precision = precision
+        self.handle = C.c_void_p()
+        _lib.check(_lib.lib().acg_batch_create(data.handle, C.cast(arr, C.c_void_p), len(self.pats),
+                                               C.byref(opt), _stream_ptr(stream),
+                                               C.byref(self.handle)), "acg_batch_create")
+        self.outs = None
+
+    def run(self, outs=None, stream=None):
+        """Match every pattern; returns (or fills) one [Dn][Pn_i] float64 tensor each.
+
+        Reusing the same output tensors relaunches the captured CUDA graph."""
+        torch = _torch()
+        if outs is None:
+            if self.outs is None:
+                dev = self.data.dev.node_feats.device
+                self.outs = [torch.empty((self.data.num_nodes, p.num_nodes), dtype=torch.float64,
+                                         device=dev) for p in self.pats]
+            outs = self.outs
+        ptrs = (C.c_void_p * len(outs))(*[o.data_ptr() for o in outs])
+        _lib.check(_lib.lib().acg_batch_match(self.handle, C.cast(ptrs, C.c_void_p),
+                                              _stream_ptr(stream)), "acg_batch_match")
+        return outs
+
+    def info(self) -> dict:
+        inf = _lib.BatchInfo()
+        _lib.check(_lib.lib().acg_batch_get_info(self.handle, C.byref(inf)), "acg_batch_get_info")
+        return {k: getattr(inf, k) for k, _ in _lib.BatchInfo._fields_ if k != "reserved"}
+
+    def close(self):
+        if self.handle:
+            _lib.lib().acg_batch_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

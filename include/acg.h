@@ -142,6 +142,35 @@ acg_status acg_match_graphs(const acg_graph* data, const acg_graph* pattern,
                             const acg_options* opt, double* mu_out,
                             void* stream);
 
+/* ---------------- many patterns against one data graph ----------------- */
+/* No counterpart in the reference, which matches one pattern per run
+ * (main.cu:72-75).  The data graph is prepared once; the patterns are packed
+ * into groups matched as disjoint unions (each member's mu equals its own
+ * acg_match result up to summation order), groups share one set of
+ * workspaces, and the whole batch is one CUDA graph launched per
+ * acg_batch_match.  Patterns: device arrays as for acg_plan_create (at most
+ * 128 vertices / 256 edges each); opt as for acg_plan_create (num_iters < 0:
+ * each pattern's own vertex count). */
+typedef struct acg_batch acg_batch;
+typedef struct acg_batch_info {
+  int32_t patterns;
+  int32_t groups;               /* unions matched */
+  int32_t widest_group_columns; /* pattern edges of the widest group */
+  int32_t reserved;
+  int64_t graph_nodes;          /* nodes of the captured CUDA graph */
+  double ms_last;               /* device time of the last acg_batch_match */
+} acg_batch_info;
+acg_status acg_batch_create(acg_data* data, const acg_graph* patterns,
+                            int32_t npatterns, const acg_options* opt,
+                            void* stream, acg_batch** out);
+/* mu_out[i]: device [Dn][patterns[i].num_nodes] f64.  The first call (and any
+ * call with other outputs or another stream) captures the CUDA graph; later
+ * calls only launch it.  Asynchronous on `stream`. */
+acg_status acg_batch_match(acg_batch* b, double* const* mu_out, void* stream);
+/* Synchronises on the last match. */
+acg_status acg_batch_get_info(acg_batch* b, acg_batch_info* out);
+acg_status acg_batch_destroy(acg_batch* b);
+
 /* ---------------- no-allocation entry point ---------------------------- */
 /* The match's initial mu, before any BP iteration:
  *   mu_out[v][p] = -d(v,p) - log sum_v' exp(-d(v',p)),  d = || x_v - y_p ||_2,
