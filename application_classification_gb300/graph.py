@@ -254,7 +254,7 @@ def batch_workload(scale: int = 20, npatterns: int = 64, seed: int = 3):
     """Many patterns of uneven size planted in one R-MAT graph.
 
     Data: R-MAT scale ``scale``, edge factor 16, seed ``seed``.  Pattern i:
-    Pn uniform in 4..48, Pe uniform in 2 Pn..4 Pn, planted with seed
+    Pn uniform in 4..48, Pe uniform in 2 Pn..4 Pn (at most Pn (Pn - 1)), planted with seed
     1000 * seed + i (features + N(0, 0.05^2)).  Returns (data, patterns,
     truth_vertices)."""
     rng = np.random.default_rng(seed)
@@ -262,7 +262,7 @@ def batch_workload(scale: int = 20, npatterns: int = 64, seed: int = 3):
     pats, truths = [], []
     for i in range(npatterns):
         pn = int(rng.integers(4, 49))
-        pe = int(rng.integers(2 * pn, 4 * pn + 1))
+        pe = min(int(rng.integers(2 * pn, 4 * pn + 1)), pn * (pn - 1))  # distinct edges only
         d, p, tv, _ = plant(d, pn, pe, 0.05, seed=1000 * seed + i)
         pats.append(p)
         truths.append(tv)
