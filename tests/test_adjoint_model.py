@@ -1,0 +1,37 @@
+"""On the CPU: the restructured forward reproduces the reference's golden mu,
+and the hand-derived adjoint the CUDA backward follows (adjoint_model.py)
+equals torch autograd through an FP64 re-implementation of the reference's own
+passes (adjoint_ref.py), for all four feature gradients."""
+import numpy as np
+import pytest
+import torch
+
+import adjoint_model
+import adjoint_ref
+from conftest import load_golden
+from application_classification_gb300 import graph
+
+
+def _check(d, p, iters=None, seed=0):
+    mu_m, rec = adjoint_model.forward(d, p, iters)
+    mu, feats = adjoint_ref.match_graphs(d, p, iters)
+    assert np.abs(mu_m - mu.detach().numpy()).max() <= 1e-10 * max(1.0, float(mu.abs().max()))
+    gmu = np.random.default_rng(seed).normal(size=mu.shape)
+    (mu * torch.tensor(gmu)).sum().backward()
+    for f, g in zip(feats, adjoint_model.backward(rec, gmu)):
+        a = f.grad.numpy() if f.grad is not None else np.zeros(tuple(f.shape))  # unused input
+        assert np.abs(a - g).max() <= 1e-9 * max(1.0, np.abs(a).max())
+
+
+@pytest.mark.parametrize("name", ["tiny", "irregular", "er300", "rmat9"])
+def test_adjoint_model_vs_autograd_golden(name):
+    d, p, ref = load_golden(name)
+    mu_m, _ = adjoint_model.forward(d, p)
+    assert np.abs(mu_m - ref).max() <= 1e-10 * max(1.0, np.abs(ref).max())
+    _check(d, p)
+
+
+@pytest.mark.parametrize("iters", [0, 1, 2])
+def test_adjoint_model_few_iterations(iters):
+    d, p, _ = graph.workload("rmat8_5_9")
+    _check(d, p, iters, seed=iters)
