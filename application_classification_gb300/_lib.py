@@ -122,6 +122,8 @@ SIGNATURES: dict[str, tuple] = {
     "acg_batch_match": (i32, [vp, vp, vp]),
     "acg_batch_get_info": (i32, [vp, _P(BatchInfo)]),
     "acg_batch_destroy": (i32, [vp]),
+    "acg_match_record": (i32, [vp, vp, i32, vp]),
+    "acg_backward": (i32, [vp, vp, vp, vp, vp, vp, vp]),
     "acg_status_string": (C.c_char_p, [i32]),
     "acg_last_error": (C.c_char_p, []),
     "acg_version": (C.c_char_p, []),

@@ -213,6 +213,44 @@ acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* ou
 namespace {
 
 template <typename T>
+acg_status iterate(acg_plan* P, int t, double* mu_out, cudaStream_t s) {
+  acg_data* D = P->data;
+  const int Dn = D->Dn, Pn = P->Pn, Pe = P->Pe, Pp = P->Pp;
+  if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1)], s);
+  if (Pe > 0) {
+    EdgeMaxArgs<T> ea{P->ew.items, P->ew.nitems, P->ew.wsplit, D->dcsr.other,
+                      (const T*)P->dE, (const T*)P->vr[(t - 1) & 1], (T*)P->M,
+                      (T*)P->part_iter, Pp};
+    ACG_TRY(launch_edge_max<T>(ea, P->ws, P->edge_blocks, s));
+    ACG_TRY(launch_heavy_combine<T>((const T*)P->part_iter, P->ew.hbase, P->ew.hcount,
+                                    P->ew.hvert, P->ew.nheavy, Pp, (T*)P->M, s));
+    P->launches += 1 + (P->ew.nheavy > 0);
+  }
+  if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1) + 1], s);
+  VertexUpdArgs<T> va{D->dcsr.off, (const T*)P->M, (T*)P->vf, (T*)P->vr[t & 1],
+                      (const T*)P->dEmin, (const T*)P->B, (const T*)P->CV,
+                      (const T*)P->CVlo, P->gi[(t - 1) & 1], P->gi[t & 1], P->bpart,
+                      mu_out, P->pat, Dn, Pn, Pe, Pp, P->Pnp, P->maxdeg, P->iters_p, t,
+                      t == 1, t == P->iters};
+  const bool rec = P->rec && P->rec->has(t);
+  if (rec) {
+    va.rec_f = (T*)P->rec->f[t];
+    va.rec_r = (T*)P->rec->r[t];
+    va.rec_mh = (T*)P->rec->mh[t];
+    va.rec_ml = (T*)P->rec->ml[t];
+  }
+  ACG_TRY(launch_vertex_update<T>(va, P->vert_blocks, s));
+  ACG_TRY(launch_finalize(P->bpart, P->vert_blocks, StatSpec{2 * Pe, 2 * Pe + Pn}, P->gi[t & 1], s));
+  ACG_TRY(launch_capture_s(P->gi[t & 1] + 4 * Pe, P->iters_p, t, P->S_final, Pn, s));
+  if (rec)
+    ACG_CUDA_TRY(cudaMemcpyAsync(P->rec->glob[t], P->gi[t & 1], sizeof(double) * glob_doubles(Pn, Pe),
+                                 cudaMemcpyDeviceToDevice, s));
+  if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1) + 2], s);
+  P->launches += 3;
+  return ACG_OK;
+}
+
+template <typename T>
 acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s, const UnionOut* uo) {
   acg_data* D = P->data;
   const int Dn = D->Dn, Pn = P->Pn, Pe = P->Pe, Pp = P->Pp;
@@ -261,6 +299,12 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s, const UnionOut
                   (const T*)P->Fq, (const T*)P->B, (const T*)P->dEmin, (T*)P->vf,
                   (T*)P->vr[0], P->gv, P->ge, P->bpart, P->pat, De, lim, Dn, Pn, Pe, Pp,
                   P->Pnp, P->Pqc, P->qcov, P->qlim_col};
+    const bool rec0 = P->rec && P->rec->has(0);
+    if (rec0) {
+      a.rec_f = (T*)P->rec->f[0];
+      a.rec_mh = (T*)P->rec->mh[0];
+      a.rec_ml = (T*)P->rec->ml[0];
+    }
     if (P->init_warp)
       ACG_TRY(launch_init_warp<T>(a, P->init_blocks, s));
     else
@@ -270,32 +314,16 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s, const UnionOut
                                  sizeof(double) * (glob_doubles(Pn, Pe) - 4 * Pe), s));
     ACG_TRY(launch_finalize(P->bpart, P->init_blocks, StatSpec{2 * Pe, 2 * Pe}, P->gi[0], s));
     P->launches += 2;
+    if (rec0) {
+      ACG_CUDA_TRY(cudaMemcpyAsync(P->rec->r[0], P->vr[0], sizeof(T) * (size_t)Dn * Pp,
+                                   cudaMemcpyDeviceToDevice, s));
+      ACG_CUDA_TRY(cudaMemcpyAsync(P->rec->glob[0], P->gi[0], sizeof(double) * glob_doubles(Pn, Pe),
+                                   cudaMemcpyDeviceToDevice, s));
+    }
   }
   cudaEventRecord(P->ev[2], s);
   // ---- BP iterations (main.cu:160-245): edge phase, heavy combine, vertex phase
-  for (int t = 1; t <= P->iters; ++t) {
-    if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1)], s);
-    if (Pe > 0) {
-      EdgeMaxArgs<T> ea{P->ew.items, P->ew.nitems, P->ew.wsplit, D->dcsr.other,
-                        (const T*)P->dE, (const T*)P->vr[(t - 1) & 1], (T*)P->M,
-                        (T*)P->part_iter, Pp};
-      ACG_TRY(launch_edge_max<T>(ea, P->ws, P->edge_blocks, s));
-      ACG_TRY(launch_heavy_combine<T>((const T*)P->part_iter, P->ew.hbase, P->ew.hcount,
-                                      P->ew.hvert, P->ew.nheavy, Pp, (T*)P->M, s));
-      P->launches += 1 + (P->ew.nheavy > 0);
-    }
-    if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1) + 1], s);
-    VertexUpdArgs<T> va{D->dcsr.off, (const T*)P->M, (T*)P->vf, (T*)P->vr[t & 1],
-                        (const T*)P->dEmin, (const T*)P->B, (const T*)P->CV,
-                        (const T*)P->CVlo, P->gi[(t - 1) & 1], P->gi[t & 1], P->bpart,
-                        mu_out, P->pat, Dn, Pn, Pe, Pp, P->Pnp, P->maxdeg, P->iters_p, t,
-                        t == 1, t == P->iters};
-    ACG_TRY(launch_vertex_update<T>(va, P->vert_blocks, s));
-    ACG_TRY(launch_finalize(P->bpart, P->vert_blocks, StatSpec{2 * Pe, 2 * Pe + Pn}, P->gi[t & 1], s));
-    ACG_TRY(launch_capture_s(P->gi[t & 1] + 4 * Pe, P->iters_p, t, P->S_final, Pn, s));
-    if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1) + 2], s);
-    P->launches += 3;
-  }
+  for (int t = 1; t <= P->iters; ++t) ACG_TRY(iterate<T>(P, t, mu_out, s));
   cudaEventRecord(P->ev[3], s);
   // ---- output [Dn][Pn] (main.cu:247 transpose is implicit in the layout)
   if (P->iters > 0 && !P->is_union) {
@@ -557,6 +585,10 @@ acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& 
   return ACG_OK;
 }
 
+acg_status run_iteration_any(acg_plan* P, int t, double* mu_out, cudaStream_t s) {
+  return P->prec == ACG_PREC_FP64 ? iterate<double>(P, t, mu_out, s) : iterate<float>(P, t, mu_out, s);
+}
+
 acg_status run_match_any(acg_plan* P, double* mu_out, cudaStream_t s, const UnionOut* uo) {
   return P->prec == ACG_PREC_FP64 ? run_match<double>(P, mu_out, s, uo)
                                   : run_match<float>(P, mu_out, s, uo);
@@ -697,6 +729,7 @@ acg_status acg_plan_create(acg_data* D, const acg_graph* pg, const acg_options* 
 
 acg_status acg_plan_destroy(acg_plan* P) {
   if (!P) return ACG_OK;
+  adj_free(P);
   for (auto& e : P->ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : P->kev)

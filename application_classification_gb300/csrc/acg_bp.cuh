@@ -60,6 +60,11 @@ struct InitArgs {
   int Dn, Pn, Pe, Pp, Pnp;
   int Pqc, qcov;       // (the later quirk columns are zero over any edge)
   const long long* qlim_col;  // [Pe] column q covers original edge ids < qlim_col[q]
+  // Recording for the adjoint (warp form only; null otherwise): f = VF of the
+  // first iteration ([Dn][Pp], zero past Pe) and MU0 as hi + lo ([Dn][Pn]).
+  T* rec_f = nullptr;
+  T* rec_mh = nullptr;
+  T* rec_ml = nullptr;
 };
 template <typename T>
 acg_status launch_init_vertex(const InitArgs<T>& a, GroupShape gs, int blocks, cudaStream_t s);

@@ -769,11 +769,15 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
         if (p < Pn) {
           lmu[j].add2(mu.hi, mu.lo);
           if (plast[j]) a.mu_raw[(size_t)v * Pn + p] = mu.dvalue();
+          if (a.rec_mh) {
+            a.rec_mh[(size_t)v * Pn + p] = mu.hi;
+            a.rec_ml[(size_t)v * Pn + p] = mu.lo;
+          }
         }
       }
       __syncwarp();
       if (!a.last && qon) {
-        T yo[QPL], zo[QPL];
+        T yo[QPL], zo[QPL], fo[QPL];
 #pragma unroll
         for (int k = 0; k < QPL; ++k) {
           // f = VF' - cR, r = VR' - cF: the shift comes off the compensated
@@ -793,12 +797,17 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
             lf[k].add_fast(r + b[k]);
             yo[k] = f - em[k];  // no out-edges: dEmin = +inf, Y = -inf
             zo[k] = r;
+            fo[k] = f;
           } else {
-            yo[k] = zo[k] = T(0);
+            yo[k] = zo[k] = fo[k] = T(0);
           }
         }
         st_n<T, QPL>(a.vf + (size_t)v * Pp + qo, yo);
         st_n<T, QPL>(a.vr_out + (size_t)v * Pp + qo, zo);
+        if (a.rec_f) {
+          st_n<T, QPL>(a.rec_f + (size_t)v * Pp + qo, fo);
+          st_n<T, QPL>(a.rec_r + (size_t)v * Pp + qo, zo);
+        }
       }
     }
     __syncwarp();  // this stage's buffer is free for the stage after next

@@ -51,6 +51,13 @@ struct VertexUpdArgs {
                        // MU_raw is written at iteration t == iters_p[p]
   int t;               // this iteration (1-based)
   int first, last;     // first iteration; last iteration of every pattern
+  // Recording for the adjoint (all null otherwise): the state this iteration
+  // produces -- f = VF' - cR and r = VR' - cF ([Dn][Pp], zero past Pe; not on
+  // the last iteration) and MU_raw as hi + lo ([Dn][Pn]).
+  T* rec_f = nullptr;
+  T* rec_r = nullptr;
+  T* rec_mh = nullptr;
+  T* rec_ml = nullptr;
 };
 // S_final[p] = S[p] of this iteration where it is p's last (S = the column
 // log-sum-exp of MU_raw in the statistics just finalised).

@@ -41,6 +41,26 @@ struct acg_data {
   std::vector<acg::DevBuf> owned;
 };
 
+namespace acg {
+// States of a match recorded for the adjoint, indexed by t (0 = after init,
+// t = after iteration t): f = VF' - cR and r = VR' - cF ([Dn][Pp]), MU_raw as
+// hi + lo ([Dn][Pn]) and the iteration's statistics ([glob_doubles]); null
+// where state t is not recorded.
+struct StateRec {
+  std::vector<void*> f, r, mh, ml;
+  std::vector<double*> glob;
+  void resize(int n) {
+    f.assign(n, nullptr);
+    r.assign(n, nullptr);
+    mh.assign(n, nullptr);
+    ml.assign(n, nullptr);
+    glob.assign(n, nullptr);
+  }
+  bool has(int t) const { return t >= 0 && t < (int)f.size() && mh[t] != nullptr; }
+};
+struct AdjWork;  // the adjoint's checkpoints and work buffers (acg_adjoint.cu)
+}  // namespace acg
+
 struct acg_plan {
   acg_data* data = nullptr;
   int prec = ACG_PREC_FP64;
@@ -90,6 +110,8 @@ struct acg_plan {
   cudaStream_t last_stream = nullptr;
   int64_t launches = 0;
   bool ran = false;
+  const acg::StateRec* rec = nullptr;  // states to record during a match (adjoint)
+  acg::AdjWork* adj = nullptr;         // owned; freed by acg_plan_destroy
   std::vector<acg::DevBuf> owned;
 };
 
@@ -130,5 +152,13 @@ struct UnionOut {
 // One whole match on stream s.  Single plans write mu_out [Dn][Pn]; union
 // plans use mu_out as [Dn][Pn] scratch and scatter into uo.
 acg_status run_match_any(acg_plan* P, double* mu_out, cudaStream_t s, const UnionOut* uo);
+
+// Iteration t alone (edge phase, vertex phase, statistics), from the working
+// state of iteration t - 1 (vf, vr[(t-1) & 1], gi[(t-1) & 1]); records state t
+// when P->rec asks for it.  mu_out is written only on the last iteration.
+acg_status run_iteration_any(acg_plan* P, int t, double* mu_out, cudaStream_t s);
+
+// Frees the adjoint's buffers of a plan (acg_adjoint.cu).
+void adj_free(acg_plan* P);
 
 }  // namespace acg

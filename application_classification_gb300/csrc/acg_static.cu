@@ -528,6 +528,10 @@ init_warp_kernel(const InitArgs<T> a) {
         }
         smu[p] = mh;
         smu[32 * PPL + p] = ml;
+        if (a.rec_mh && p < Pn) {
+          a.rec_mh[(size_t)v * Pn + p] = mh;
+          a.rec_ml[(size_t)v * Pn + p] = ml;
+        }
       }
       __syncwarp();
       if (qon) {
@@ -535,7 +539,7 @@ init_warp_kernel(const InitArgs<T> a) {
 #pragma unroll
         for (int k = 0; k < QPL; ++k) {
           const int q = qo + k;
-          T yo = T(0), zo = T(0);
+          T yo = T(0), zo = T(0), fo = T(0);
           if (q < Pe) {
             T R0 = vfm[k], F0 = vrm[k];
             if (hout) R0 = fmax(R0, ((q < qcov ? cur.rq[k] : T(0)) - lbh[k]) - lbl[k]);
@@ -548,10 +552,12 @@ init_warp_kernel(const InitArgs<T> a) {
             lf[k].add_fast(r + cur.b[k]);
             yo = f - cur.em[k];  // no out-edges: dEmin = +inf, Y = -inf
             zo = r;
+            fo = f;
           }
           if (q < Pp) {
             a.vf[(size_t)v * Pp + q] = yo;
             a.vr[(size_t)v * Pp + q] = zo;
+            if (a.rec_f) a.rec_f[(size_t)v * Pp + q] = fo;
           }
         }
       }

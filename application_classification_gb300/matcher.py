@@ -138,6 +138,33 @@ class Plan:
                                         _stream_ptr(stream)), "acg_match")
         return out
 
+    def record(self, out=None, checkpoint_every: int = 4, stream=None):
+        """:meth:`run` that also keeps the states the adjoint needs (every
+        ``checkpoint_every``-th BP iteration and the last); returns mu."""
+        torch = _torch()
+        if out is None:
+            out = torch.empty((self.data.num_nodes, self.pat.num_nodes), dtype=torch.float64,
+                              device=self.data.dev.node_feats.device)
+        _lib.check(_lib.lib().acg_match_record(self.handle, C.c_void_p(out.data_ptr()),
+                                               int(checkpoint_every), _stream_ptr(stream)),
+                   "acg_match_record")
+        return out
+
+    def backward(self, grad_mu, stream=None):
+        """Gradients of sum(grad_mu * mu) for the last :meth:`record`: a tuple
+        (data node, data edge, pattern node, pattern edge) of float64 tensors
+        shaped like the four feature arrays."""
+        torch = _torch()
+        dev = self.data.dev.node_feats.device
+        g = grad_mu.to(device=dev, dtype=torch.float64).contiguous()
+        outs = [torch.empty(tuple(t.shape), dtype=torch.float64, device=dev)
+                for t in (self.data.dev.node_feats, self.data.dev.edge_feats,
+                          self.pat.node_feats, self.pat.edge_feats)]
+        _lib.check(_lib.lib().acg_backward(self.handle, C.c_void_p(g.data_ptr()),
+                                           *[C.c_void_p(o.data_ptr()) for o in outs],
+                                           _stream_ptr(stream)), "acg_backward")
+        return tuple(outs)
+
     def stats(self) -> dict:
         st = _lib.Stats()
         _lib.check(_lib.lib().acg_plan_stats(self.handle, C.byref(st)), "acg_plan_stats")

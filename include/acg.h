@@ -189,6 +189,27 @@ acg_status acg_initial_mu_noalloc(const double* data_node_feats, uint64_t num_no
                                   uint64_t feat_dim, const double* pattern_node_feats,
                                   uint64_t pattern_nodes, double* mu_out, void* stream);
 
+/* ---------------- gradients (adjoint of a match) ----------------------- */
+/* No counterpart in the reference, which runs the matcher forward only.
+ * acg_match_record is acg_match (same output) that also keeps the state of
+ * every `checkpoint_every`-th BP iteration (<= 0: 4) and of the last;
+ * acg_backward then returns the gradients of sum(grad_mu * mu) with respect
+ * to the four feature arrays (FP64 device outputs: data [num_nodes][node
+ * feat dim], [num_edges][edge feat dim] in the data graph's own edge order,
+ * pattern [Pn][node feat dim], [Pe][edge feat dim]), recomputing the
+ * iterations between checkpoints.  Maxima pass their gradient to the first
+ * maximal element (smallest data vertex; smallest edge id within a vertex's
+ * edges); log-sum-exps through their softmax.  Deterministic: no atomics.
+ * Limits: single plans of at most 64 pattern vertices and 64 pattern edges
+ * (padded), feature dimensions <= 32 (else ACG_ERR_UNSUPPORTED).  The
+ * checkpoints stay with the plan until it is destroyed or re-recorded.
+ * Asynchronous on `stream`. */
+acg_status acg_match_record(acg_plan* plan, double* mu_out, int32_t checkpoint_every,
+                            void* stream);
+acg_status acg_backward(acg_plan* plan, const double* grad_mu, double* grad_data_node_feats,
+                        double* grad_data_edge_feats, double* grad_pattern_node_feats,
+                        double* grad_pattern_edge_feats, void* stream);
+
 /* ---------------- errors ----------------------------------------------- */
 const char* acg_status_string(acg_status s);
 /* Message of the last failing call on this host thread ("" if none). */
