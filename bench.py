@@ -47,6 +47,10 @@ WORKLOADS = {
     "rmat18": ("RMAT scale 18 (262,144 vertices, edge factor 16), planted pattern 16 / 32, "
                "13/17-dim N(0,1) features, seed 1", "rmat14_16_32"),
     "rmat20": ("RMAT scale 20, planted pattern 16 / 32, seed 3", "rmat14_16_32"),
+    "rmat16": ("RMAT scale 16 (65,536 vertices, edge factor 16), planted pattern 12 / 24, "
+               "13/17-dim N(0,1) features, seed 4", "rmat14_12_24"),
+    "rmat12": ("RMAT scale 12 (4,096 vertices, edge factor 16), planted pattern 12 / 24, "
+               "13/17-dim N(0,1) features, seed 4", "rmat12_12_24"),
     "er1k": ("Erdos-Renyi 1,000 vertices / 20,000 edges, planted pattern 10 / 20, seed 0",
              "er1k"),
 }
@@ -82,6 +86,11 @@ def parse():
     ap.add_argument("--batch", action="store_true",
                     help="the many-pattern workload instead: R-MAT 20 with 64 planted patterns "
                          "(Pn 4..48, Pe 2..4 Pn), batched against sequential single matches")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="time the backward (acg_backward) against the forward of one match "
+                         "(RMAT-16 with a 12/24 pattern by default)")
+    ap.add_argument("--adjoint-workload", default="rmat16")
+    ap.add_argument("--checkpoint-every", type=int, default=4)
     ap.add_argument("--batch-scale", type=int, default=20)
     ap.add_argument("--batch-patterns", type=int, default=64)
     ap.add_argument("--fp64-sample", type=int, default=16,
@@ -541,6 +550,84 @@ def run_batch(args, ws, rank, local):
         }), flush=True)
 
 
+def run_adjoint(args, ws, rank, local):
+    """Forward (acg_match, and acg_match_record which also keeps checkpoints)
+    against the backward (acg_backward) of one match.  Loss: the sum of mu --
+    the log of the normalised assignment probability -- over the planted
+    (data vertex, pattern vertex) pairs, so grad_mu is one-hot there."""
+    import numpy as np
+    import torch
+
+    from application_classification_gb300 import graph, matcher
+
+    torch.cuda.set_device(local)
+    d, p, truth = graph.workload(args.adjoint_workload)
+    dg = matcher.DataGraph(d)
+    stream = torch.cuda.current_stream()
+    gmu = torch.zeros((d.num_nodes, p.num_nodes), dtype=torch.float64, device="cuda")
+    gmu[torch.as_tensor(np.asarray(truth, dtype=np.int64)), torch.arange(p.num_nodes)] = 1.0
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB > L2
+
+    def timed(fn, n):
+        # each call alone between events, L2 flushed before it
+        tot = 0.0
+        for _ in range(n):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / n
+
+    res, grads = {}, {}
+    clk_summary = None
+    for prec in (args.precision, "fp64"):
+        pl = matcher.Plan(dg, p, prec)
+        mu = pl.record(checkpoint_every=args.checkpoint_every)
+        for _ in range(max(1, args.warmup)):
+            pl.run(mu)
+            pl.record(mu, args.checkpoint_every)
+            pl.backward(gmu)
+        torch.cuda.synchronize()
+        barrier(ws)
+        with Clocks(local) as clk:
+            ms_fwd = timed(lambda: pl.run(mu), args.steps)
+            ms_rec = timed(lambda: pl.record(mu, args.checkpoint_every), args.steps)
+            ms_bwd = timed(lambda: pl.backward(gmu), args.steps)
+        if prec == args.precision:
+            clk_summary = clk.summary()
+        barrier(ws)
+        res[prec] = {k: round(max_over_ranks(v, ws), 3)
+                     for k, v in (("forward_ms", ms_fwd), ("forward_record_ms", ms_rec),
+                                  ("backward_ms", ms_bwd))}
+        res[prec]["backward_over_forward"] = round(res[prec]["backward_ms"] / res[prec]["forward_ms"], 3)
+        grads[prec] = [x.cpu().numpy() for x in pl.backward(gmu)]
+        del pl
+    names = ["data_node", "data_edge", "pattern_node", "pattern_edge"]
+    rel = {n: float(np.linalg.norm(a - b) / max(1e-300, np.linalg.norm(b)))
+           for n, a, b in zip(names, grads[args.precision], grads["fp64"])}
+    r = res[args.precision]
+    if rank == 0:
+        print(json.dumps({
+            "metric": "backward time / forward time of one match (gradients of the planted-pair "
+                      "log-probabilities w.r.t. all four feature arrays)",
+            "value": r["backward_over_forward"], "unit": "x", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["backward_ms"], "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
+            "config": {"workload": workload_info(args.adjoint_workload)[0],
+                       "data_vertices": d.num_nodes, "data_edges": d.num_edges,
+                       "pattern": [p.num_nodes, p.num_edges],
+                       "checkpoint_every": args.checkpoint_every, "precision": args.precision,
+                       "l2": "flushed (256 MB write) before every timed call"},
+            "timings": res,
+            "grad_rel_frobenius_vs_fp64": rel,
+            "clocks": clk_summary,
+        }), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -550,6 +637,8 @@ def main():
         ws, rank, local = dist_setup("nccl")
         if args.batch:
             run_batch(args, ws, rank, local)
+        elif args.adjoint:
+            run_adjoint(args, ws, rank, local)
         else:
             run_ours(args, ws, rank, local)
     if ws > 1:

@@ -191,3 +191,66 @@ def test_backward_errors(cuda):
     plan2.close()
     data.close()
     data2.close()
+
+
+def _planted_gmu(d, p, truth):
+    g = np.zeros((d.num_nodes, p.num_nodes))
+    g[np.asarray(truth, dtype=np.int64), np.arange(p.num_nodes)] = 1.0
+    return g
+
+
+def test_rmat12_planted_loss_vs_autograd_reference(cuda):
+    """Loss = sum of mu (the log assignment probability) over the planted
+    pairs, RMAT scale 12 with a 12/24 pattern: the FP64 and mixed gradients
+    against torch autograd through the reference's own passes (FP64, CPU)."""
+    import adjoint_ref
+
+    d, p, truth = graph.workload("rmat12")
+    gmu = _planted_gmu(d, p, truth)
+    mu_t, feats = adjoint_ref.match_graphs(d, p)
+    (mu_t * torch.from_numpy(gmu)).sum().backward()
+    ref = [f.grad.numpy() for f in feats]
+    mu64, g64 = _grads(d, p, gmu, "fp64")
+    assert _rel(mu64, mu_t.detach().numpy()) <= 1e-10
+    for a, b in zip(g64, ref):
+        assert _rel(a, b) <= FP64_REL, _rel(a, b)
+    _, g32 = _grads(d, p, gmu, "mixed")
+    for a, b in zip(g32, ref):
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) <= MIXED_REL
+
+
+def test_rmat12_finite_differences_200(cuda):
+    """FP64 central differences on 200 random coordinates (50 per feature
+    array), perturbing the device features in place under one plan."""
+    d, p, truth = graph.workload("rmat12")
+    gmu = torch.from_numpy(_planted_gmu(d, p, truth)).to(cuda)
+    data = matcher.DataGraph(d)
+    plan = matcher.Plan(data, p, "fp64")
+    try:
+        plan.record()
+        g = [x.cpu().numpy() for x in plan.backward(gmu)]
+        arrays = [data.dev.node_feats, data.dev.edge_feats, plan.pat.node_feats, plan.pat.edge_feats]
+        rng = np.random.default_rng(12)
+        mu = torch.empty((d.num_nodes, p.num_nodes), dtype=torch.float64, device=cuda)
+
+        def f():
+            plan.run(mu)
+            return float((mu * gmu).sum())
+
+        h = 1e-5
+        for k, a in enumerate(arrays):
+            scale = max(1e-3, np.abs(g[k]).max())
+            flat = a.view(-1)
+            for i in rng.integers(0, flat.numel(), 50).tolist():
+                x0 = flat[i].item()
+                flat[i] = x0 + h
+                fp = f()
+                flat[i] = x0 - h
+                fm = f()
+                flat[i] = x0
+                fd = (fp - fm) / (2 * h)
+                idx = np.unravel_index(i, tuple(a.shape))
+                assert abs(fd - g[k][idx]) <= 1e-5 * scale, (k, idx, fd, g[k][idx])
+    finally:
+        plan.close()
+        data.close()
