@@ -131,27 +131,41 @@ __device__ void block_argmax_out(const double* rv, const int* ri, int ncol, doub
   }
 }
 
-// out[c] = sum over blocks in order; argmax columns likewise (strict >).
+// One warp per column: out[c] = the sum of part[c][0, nblk) (lane-strided
+// partial sums, then a fixed shuffle tree: deterministic); argmax columns: the
+// first maximal index (the blocks cover increasing vertex ranges, and ties go
+// to the smaller index).
 __global__ void col_final_kernel(const double* __restrict__ part, int nsum, const double* __restrict__ pv,
                                  const int* __restrict__ pi, int narg, int nblk, double* __restrict__ out,
                                  int* __restrict__ outi) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   if (c < nsum) {
     double s = 0;
-    for (int b = 0; b < nblk; ++b) s += part[(size_t)c * nblk + b];
-    out[c] = s;
+    for (int b = lane; b < nblk; b += 32) s += part[(size_t)c * nblk + b];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) out[c] = s;
   } else if (c < nsum + narg) {
     const int j = c - nsum;
     double bv = -CUDART_INF;
     int bi = -1;
-    for (int b = 0; b < nblk; ++b) {
+    for (int b = lane; b < nblk; b += 32) {
       const int i = pi[(size_t)j * nblk + b];
       if (i >= 0 && (bi < 0 || pv[(size_t)j * nblk + b] > bv)) {
         bv = pv[(size_t)j * nblk + b];
         bi = i;
       }
     }
-    outi[j] = bi;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ov = __shfl_down_sync(0xffffffffu, bv, o);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    if (lane == 0) outi[j] = bi;
   }
 }
 
@@ -233,21 +247,40 @@ __global__ void __launch_bounds__(kT) adj_argmax_kernel(const ArgArgs<T> a) {
       best[k] = neg_inf<T>();
       pos[k] = -1;
     }
-    for (int e = item.y + slot; e < item.z; e += S) {
-      const T* zr = a.Z + (size_t)__ldg(a.src_of + e) * Pp;
-      const T* dr = a.dE + (size_t)e * Pp;
+    // kU edges per lane in flight: their source rows, then both loads, then
+    // the comparisons in increasing position (the first maximum is kept)
+    for (int base = item.y; base < item.z; base += S * kU) {
+      int src[kU];
 #pragma unroll
-      for (int k = 0; k < NQV; ++k) {
-        const int qv = qc + NPOW * k;
-        if (qv * W >= Pp) continue;
-        const VT x = __ldg(reinterpret_cast<const VT*>(zr) + qv);
-        const VT y = __ldg(reinterpret_cast<const VT*>(dr) + qv);
+      for (int u = 0; u < kU; ++u) {
+        const int e = base + slot + S * u;
+        src[u] = e < item.z ? __ldg(a.src_of + e) : -1;
+      }
+      VT z[kU][NQV], d[kU][NQV];
 #pragma unroll
-        for (int w = 0; w < W; ++w) {
-          const T v = ag<T>(x, w) - ag<T>(y, w);
-          if (pos[k * W + w] < 0 || v > best[k * W + w]) {
-            best[k * W + w] = v;
-            pos[k * W + w] = e;
+      for (int u = 0; u < kU; ++u)
+#pragma unroll
+        for (int k = 0; k < NQV; ++k) {
+          const int qv = qc + NPOW * k;
+          if (src[u] >= 0 && qv * W < Pp) {
+            z[u][k] = __ldg(reinterpret_cast<const VT*>(a.Z + (size_t)src[u] * Pp) + qv);
+            d[u][k] = __ldg(reinterpret_cast<const VT*>(a.dE + (size_t)(base + slot + S * u) * Pp) + qv);
+          }
+        }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        if (src[u] < 0) continue;
+        const int e = base + slot + S * u;
+#pragma unroll
+        for (int k = 0; k < NQV; ++k) {
+          if ((qc + NPOW * k) * W >= Pp) continue;
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            const T v = ag<T>(z[u][k], w) - ag<T>(d[u][k], w);
+            if (pos[k * W + w] < 0 || v > best[k * W + w]) {
+              best[k * W + w] = v;
+              pos[k * W + w] = e;
+            }
           }
         }
       }
@@ -319,33 +352,67 @@ struct ScatArgs {
   T* gdE;
   T* gVRe;
   T* part;
-  int Pp;
+  int Pp, Pe;
+};
+
+// A is read with the same 16-byte-per-lane column split as the values
+template <typename T>
+struct IV;
+template <>
+struct IV<double> {
+  using type = int2;
+};
+template <>
+struct IV<float> {
+  using type = int4;
 };
 
 template <typename T, int NPOW, int NQV>
 __global__ void __launch_bounds__(kT) adj_scatter_kernel(const ScatArgs<T> a) {
+  using IVT = typename IV<T>::type;
   constexpr int W = AV<T>::W, S = 32 / NPOW, NQ = NQV * W;
-  const int Pp = a.Pp, lane = threadIdx.x & 31, slot = lane / NPOW, qc = lane % NPOW;
+  const int Pp = a.Pp, Pe = a.Pe, lane = threadIdx.x & 31, slot = lane / NPOW, qc = lane % NPOW;
   const int gw = (blockIdx.x * kT + threadIdx.x) >> 5;
   for (int it = a.wsplit[gw]; it < a.wsplit[gw + 1]; ++it) {
     const int4 item = a.items[it];
     T acc[NQ];
 #pragma unroll
     for (int k = 0; k < NQ; ++k) acc[k] = T(0);
-    for (int j = item.y + slot; j < item.z; j += S) {
-      const int e = __ldg(a.row_of + j);
-      const size_t vr = (size_t)__ldg(a.dst_of + j) * Pp;
+    for (int base = item.y; base < item.z; base += S * kU) {
+      int e[kU], vd[kU];
 #pragma unroll
-      for (int k = 0; k < NQV; ++k)
+      for (int u = 0; u < kU; ++u) {
+        const int j = base + slot + S * u;
+        const bool ok = j < item.z;
+        e[u] = ok ? __ldg(a.row_of + j) : -1;
+        vd[u] = ok ? __ldg(a.dst_of + j) : 0;
+      }
+      IVT av[kU][NQV];
 #pragma unroll
-        for (int w = 0; w < W; ++w) {
-          const int q = (qc + NPOW * k) * W + w;
-          if (q < Pp && __ldg(a.A + vr + q) == e) {
-            const T g = a.gM[vr + q];
-            acc[k * W + w] += g;
-            a.gdE[(size_t)e * Pp + q] -= g;
+      for (int u = 0; u < kU; ++u)
+#pragma unroll
+        for (int k = 0; k < NQV; ++k) {
+          const int qv = qc + NPOW * k;
+          if (e[u] >= 0 && qv * W < Pe)
+            av[u][k] = __ldg(reinterpret_cast<const IVT*>(a.A + (size_t)vd[u] * Pp) + qv);
+        }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        if (e[u] < 0) continue;
+#pragma unroll
+        for (int k = 0; k < NQV; ++k) {
+          if ((qc + NPOW * k) * W >= Pe) continue;
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            const int q = (qc + NPOW * k) * W + w;
+            if (q < Pe && reinterpret_cast<const int*>(&av[u][k])[w] == e[u]) {
+              const T g = a.gM[(size_t)vd[u] * Pp + q];
+              acc[k * W + w] += g;
+              a.gdE[(size_t)e[u] * Pp + q] -= g;
+            }
           }
         }
+      }
     }
 #pragma unroll
     for (int o = NPOW; o < 32; o <<= 1)
@@ -1119,23 +1186,56 @@ adj_cdist_rows_kernel(const F* __restrict__ x, const int* __restrict__ row, int 
 }
 
 // Pattern side: part[block][q][k] = sum over the block's rows of rr[r][q] *
-// x[r][k] (k < K) and rr[r][q] (k = K), rows in order.
+// x[r][k] (k < K) and rr[r][q] (k = K).  The block's rows are staged through
+// shared memory kPR at a time (coalesced loads); each thread owns up to kPO
+// outputs, summed per tile in T and across tiles in FP64, in row order.
+constexpr int kPR = 32;
+constexpr int kPO = 9;  // ceil(64 * 33 / 256): P <= 64, K <= 32
 template <typename T, typename F>
-__global__ void adj_cdist_pat_kernel(const F* __restrict__ x, const int* __restrict__ row, int kstride,
-                                     int K, const T* __restrict__ rr, int ldg, int P, long long nrows,
-                                     double* __restrict__ part) {
+__global__ void __launch_bounds__(256)
+adj_cdist_pat_kernel(const F* __restrict__ x, const int* __restrict__ row, int kstride, int K,
+                     const T* __restrict__ rr, int ldg, int P, long long nrows, double* __restrict__ part) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int K1 = K + 1, nout = P * K1;
+  T* s_r = reinterpret_cast<T*>(sm);  // [kPR][P]
+  T* s_x = s_r + kPR * P;             // [kPR][K + 1], column K = 1
   const long long r0 = nrows * blockIdx.x / gridDim.x, r1 = nrows * (blockIdx.x + 1) / gridDim.x;
-  const int nout = P * (K + 1);
-  for (int o = threadIdx.x; o < nout; o += blockDim.x) {
-    const int q = o / (K + 1), k = o % (K + 1);
-    double s = 0;
-    for (long long r = r0; r < r1; ++r) {
-      const double w = (double)rr[(size_t)r * ldg + q];
-      if (w == 0.0) continue;
-      const long long src = row ? (long long)row[r] : r;
-      s += w * (k < K ? (double)x[(size_t)src * kstride + k] : 1.0);
+  double acc[kPO];
+#pragma unroll
+  for (int j = 0; j < kPO; ++j) acc[j] = 0;
+  for (long long t0 = r0; t0 < r1; t0 += kPR) {
+    const int nr = (int)min((long long)kPR, r1 - t0);
+    __syncthreads();  // the previous tile is consumed
+    for (int i = threadIdx.x; i < kPR * P; i += 256) {
+      const int r = i / P, q = i - r * P;
+      s_r[i] = r < nr ? rr[(size_t)(t0 + r) * ldg + q] : T(0);
     }
-    part[(size_t)blockIdx.x * nout + o] = s;
+    for (int i = threadIdx.x; i < kPR * K1; i += 256) {
+      const int r = i / K1, k = i - r * K1;
+      T v = T(0);
+      if (r < nr) {
+        const long long src = row ? (long long)row[t0 + r] : t0 + r;
+        v = k < K ? (T)x[(size_t)src * kstride + k] : T(1);
+      }
+      s_x[i] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kPO; ++j) {
+      const int o = threadIdx.x + 256 * j;
+      if (o < nout) {
+        const int q = o / K1, k = o - q * K1;
+        T sum = T(0);
+#pragma unroll 8
+        for (int r = 0; r < kPR; ++r) sum = fma(s_r[r * P + q], s_x[r * K1 + k], sum);
+        acc[j] += (double)sum;
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kPO; ++j) {
+    const int o = threadIdx.x + 256 * j;
+    if (o < nout) part[(size_t)blockIdx.x * nout + o] = acc[j];
   }
 }
 
@@ -1187,7 +1287,7 @@ struct Adj {
   acg_status col_final(int nsum, int narg, int nblk) {
     const int n = nsum + narg;
     if (n == 0) return ACG_OK;
-    col_final_kernel<<<ceil_div(n, 128), 128, 0, s>>>(W->part, nsum, W->part + (size_t)nsum * nblk, W->parti,
+    col_final_kernel<<<ceil_div(32LL * n, 256), 256, 0, s>>>(W->part, nsum, W->part + (size_t)nsum * nblk, W->parti,
                                                         narg, nblk, W->cols, W->colsi);
     ACG_LAUNCH_CHECK();
     return ACG_OK;
@@ -1199,7 +1299,7 @@ struct Adj {
     const int nb = std::max(1, std::min(nsm * 2, (int)std::min<long long>(rows, 1 << 20)));
     col_sum_kernel<S><<<nb, 128, 0, s>>>(x, ld, ncol, rows, W->part);
     ACG_LAUNCH_CHECK();
-    col_final_kernel<<<ceil_div(ncol, 128), 128, 0, s>>>(W->part, ncol, nullptr, nullptr, 0, nb, W->cols + off,
+    col_final_kernel<<<ceil_div(32LL * ncol, 256), 256, 0, s>>>(W->part, ncol, nullptr, nullptr, 0, nb, W->cols + off,
                                                           nullptr);
     ACG_LAUNCH_CHECK();
     return ACG_OK;
@@ -1246,7 +1346,7 @@ struct Adj {
 
   acg_status scatter() {
     ScatArgs<T> a{P->sw.items, P->sw.wsplit, D->pos_in_dst, D->scsr.other, W->A, (const T*)W->gM,
-                  (T*)W->gdE, (T*)W->gVRe, (T*)W->pscat, Pp};
+                  (T*)W->gdE, (T*)W->gVRe, (T*)W->pscat, Pp, Pe};
     ACG_TRY(fill(W->gVRe, vrow(), T(0)));  // sources without out-edges
     bool done = false;
 #define ADJ_SC(NP_, NQ_)                                                        \
@@ -1506,13 +1606,14 @@ struct Adj {
     }
     if (le != cudaSuccess) return set_error(ACG_ERR_CUDA, "adj_cdist_rows: %s", cudaGetErrorString(le));
     // pattern side
-    const int pb = std::max(1, std::min(nsm * 2, (int)std::max<long long>(1, nrows / 64)));
+    const int pb = std::max(1, std::min(nsm * 4, ceil_div(nrows, 4 * kPR)));
+    const size_t psm = sizeof(T) * (size_t)kPR * (P_ + K + 1);
     if constexpr (sizeof(T) == 4) {
       const float* x = vertex ? D->nf32 : D->ef32;
-      adj_cdist_pat_kernel<T, float><<<pb, 256, 0, s>>>(x, nullptr, kstride, K, g, ld, P_, nrows, W->ypart);
+      adj_cdist_pat_kernel<T, float><<<pb, 256, psm, s>>>(x, nullptr, kstride, K, g, ld, P_, nrows, W->ypart);
     } else {
       const double* x = vertex ? D->node_feats : D->edge_feats;
-      adj_cdist_pat_kernel<T, double><<<pb, 256, 0, s>>>(x, row, kstride, K, g, ld, P_, nrows, W->ypart);
+      adj_cdist_pat_kernel<T, double><<<pb, 256, psm, s>>>(x, row, kstride, K, g, ld, P_, nrows, W->ypart);
     }
     ACG_LAUNCH_CHECK();
     adj_cdist_pat_final_kernel<<<ceil_div(P_ * K, 128), 128, 0, s>>>(W->ypart, pb, P_, K, y, gy);
@@ -1608,7 +1709,7 @@ acg_status adj_alloc(acg_plan* P, int every, cudaStream_t s) {
   ACG_TRY(adj_buf(W, sizeof(int) * std::max(2 * Pe, Pn) * vb, (void**)&W->parti, s));
   ACG_TRY(adj_buf(W, sizeof(double) * (8 * Pe + 2 * Pn + 8), (void**)&W->cols, s));
   ACG_TRY(adj_buf(W, sizeof(int) * (2 * Pe + Pn + 1), (void**)&W->colsi, s));
-  const size_t ny = 2 * (size_t)nsm * std::max(Pn * (D->Kv + 1), Pe * (D->Ke + 1));
+  const size_t ny = 4 * (size_t)nsm * std::max(Pn * (D->Kv + 1), Pe * (D->Ke + 1));
   ACG_TRY(adj_buf(W, sizeof(double) * ny, (void**)&W->ypart, s));
   return ACG_OK;
 }
