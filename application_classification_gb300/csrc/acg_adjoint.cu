@@ -340,7 +340,8 @@ __global__ void adj_argmax_combine_kernel(const T* __restrict__ pval, const int*
 
 // --------------------------------------------- gradient through the maxima
 // For each source s (source CSR): gVRe[s][q] = sum over its out-edges e whose
-// destination v has A[v][q] == e of gM[v][q]; and gdE[e][q] -= gM[v][q] there.
+// destination v has A[v][q] == e of gM[v][q].  (The matching gdE[e][q] -=
+// gM[v][q] is made by step A, which holds gM[v][q] and reads A[v][q].)
 template <typename T>
 struct ScatArgs {
   const int4* items;
@@ -349,7 +350,6 @@ struct ScatArgs {
   const int* dst_of;   // destination vertex of each src-CSR position
   const int* A;
   const T* gM;
-  T* gdE;
   T* gVRe;
   T* part;
   int Pp, Pe;
@@ -405,11 +405,8 @@ __global__ void __launch_bounds__(kT) adj_scatter_kernel(const ScatArgs<T> a) {
 #pragma unroll
           for (int w = 0; w < W; ++w) {
             const int q = (qc + NPOW * k) * W + w;
-            if (q < Pe && reinterpret_cast<const int*>(&av[u][k])[w] == e[u]) {
-              const T g = a.gM[(size_t)vd[u] * Pp + q];
-              acc[k * W + w] += g;
-              a.gdE[(size_t)e[u] * Pp + q] -= g;
-            }
+            if (q < Pe && reinterpret_cast<const int*>(&av[u][k])[w] == e[u])
+              acc[k * W + w] += a.gM[(size_t)vd[u] * Pp + q];
           }
         }
       }
@@ -463,6 +460,8 @@ struct StepAArgs {
   const T* f;         // [Dn][Pp] f(t-1) = VF(t-1) - cR(t-1)
   const T* r;         // [Dn][Pp] r(t-1)
   const T* M;         // [Dn][Pp] edge maxima of state t-1
+  const int* A;       // [Dn][Pp] their first maximal destination-CSR positions
+  T* gdE;             // accumulated [De][Pp]
   const T* dEmin;
   const double* glob; // statistics of state t-1
   const int* pat;
@@ -544,6 +543,8 @@ __global__ void __launch_bounds__(kT) adj_stepA_kernel(const StepAArgs<T> a) {
       const T gb = sR ? gR : T(0), gm = sF ? gF : T(0);
       a.gbR[i] = gb;
       a.gM[i] = gm;
+      // the maximum's -dE term: each (edge, column) is the maximum of one vertex
+      if (gm != T(0)) a.gdE[(size_t)__ldg(a.A + i) * Pp + q] -= gm;
       a.gdEmin[i] -= gb;
       sa[k][0] += sR ? 0.0 : (double)gR;
       sa[k][1] += sF ? 0.0 : (double)gF;
@@ -1239,18 +1240,24 @@ adj_cdist_pat_kernel(const F* __restrict__ x, const int* __restrict__ row, int k
   }
 }
 
-// gy[q][k] = -sum_r rr x_k + y[q][k] sum_r rr  (blocks summed in order)
+// gy[q][k] = -sum_r rr x_k + y[q][k] sum_r rr: one warp per output, the
+// blocks' partials in a fixed lane-strided order and shuffle tree.
 __global__ void adj_cdist_pat_final_kernel(const double* __restrict__ part, int nblk, int P, int K,
                                            const double* __restrict__ y, double* __restrict__ gy) {
-  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  const int o = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   if (o >= P * K) return;
   const int q = o / K, k = o % K, nout = P * (K + 1);
   double sx = 0, s1 = 0;
-  for (int b = 0; b < nblk; ++b) {
+  for (int b = lane; b < nblk; b += 32) {
     sx += part[(size_t)b * nout + q * (K + 1) + k];
     s1 += part[(size_t)b * nout + q * (K + 1) + K];
   }
-  gy[o] = -sx + y[o] * s1;
+#pragma unroll
+  for (int w = 16; w > 0; w >>= 1) {
+    sx += __shfl_down_sync(0xffffffffu, sx, w);
+    s1 += __shfl_down_sync(0xffffffffu, s1, w);
+  }
+  if (lane == 0) gy[o] = -sx + y[o] * s1;
 }
 
 #define ADJ_SHAPES(X) X(1, 1) X(2, 1) X(4, 1) X(8, 1) X(16, 1) X(32, 1) X(32, 2) X(32, 4)
@@ -1346,7 +1353,7 @@ struct Adj {
 
   acg_status scatter() {
     ScatArgs<T> a{P->sw.items, P->sw.wsplit, D->pos_in_dst, D->scsr.other, W->A, (const T*)W->gM,
-                  (T*)W->gdE, (T*)W->gVRe, (T*)W->pscat, Pp, Pe};
+                  (T*)W->gVRe, (T*)W->pscat, Pp, Pe};
     ACG_TRY(fill(W->gVRe, vrow(), T(0)));  // sources without out-edges
     bool done = false;
 #define ADJ_SC(NP_, NQ_)                                                        \
@@ -1375,7 +1382,7 @@ struct Adj {
     state(t - 1, t0, &f, &r, &mh, &ml, &g);
     if (Pe > 0) ACG_TRY(argmax(r));
     StepAArgs<T> sa{(const T*)W->gMU, first ? nullptr : (const T*)W->gFd,
-                    first ? nullptr : (const T*)W->gRd, f, r, (const T*)W->Mx, (const T*)P->dEmin, g,
+                    first ? nullptr : (const T*)W->gRd, f, r, (const T*)W->Mx, W->A, (T*)W->gdE, (const T*)P->dEmin, g,
                     P->pat, (T*)W->gbR, (T*)W->gM, (T*)W->gdEmin, (T*)W->gCV, W->part,
                     W->part + (size_t)4 * Pe * vblocks, W->parti, Dn, Pn, Pe, Pp};
     const size_t smA = sizeof(T) * kW * 64 * 2 + sizeof(double) * kW * 6 * std::max(1, Pe) +
@@ -1616,7 +1623,7 @@ struct Adj {
       adj_cdist_pat_kernel<T, double><<<pb, 256, psm, s>>>(x, row, kstride, K, g, ld, P_, nrows, W->ypart);
     }
     ACG_LAUNCH_CHECK();
-    adj_cdist_pat_final_kernel<<<ceil_div(P_ * K, 128), 128, 0, s>>>(W->ypart, pb, P_, K, y, gy);
+    adj_cdist_pat_final_kernel<<<ceil_div(32LL * P_ * K, 256), 256, 0, s>>>(W->ypart, pb, P_, K, y, gy);
     ACG_LAUNCH_CHECK();
     return ACG_OK;
   }
