@@ -58,10 +58,10 @@ typedef struct acg_graph {
 /* Arithmetic used by a plan.
  *  ACG_PREC_FP64  : every value and every operation in FP64, as the reference
  *                   (helpers.hxx:3-4 `Real = double`).
- *  ACG_PREC_MIXED : cost matrices on the tensor cores (BF16 hi/lo split, FP32
- *                   accumulate, exact FP32 recompute of near pairs), belief
- *                   propagation in FP32, column log-sum-exp normalisers
- *                   accumulated in FP64. */
+ *  ACG_PREC_MIXED : cost matrices in FP32 (difference form, from FP32 copies
+ *                   of the features), belief propagation in FP32 with the
+ *                   values stored relative to per-column shifts, column
+ *                   log-sum-exp normalisers accumulated in FP64. */
 typedef enum acg_precision {
   ACG_PREC_FP64 = 0,
   ACG_PREC_MIXED = 1
