@@ -10,6 +10,8 @@
 //                              reference)
 //     --iters N                BP iterations (default: the pattern's vertex
 //                              count, main.cu:160)
+//     --cnull                  add the C-null term the reference leaves out
+//                              (acg_options.cnull)
 //     --csv                    DATA and PATTERN are CSV prefixes: P.Vertex.csv
 //                              and P.Edges.csv (the prob2bin.py layout)
 //     --out PATH               write mu to PATH instead of stdout
@@ -36,7 +38,7 @@ int fail(const char* what) {
 
 int usage() {
   std::fprintf(stderr,
-               "usage: acg_main [--precision fp64|mixed] [--iters N] [--csv] [--out PATH] "
+               "usage: acg_main [--precision fp64|mixed] [--iters N] [--cnull] [--csv] [--out PATH] "
                "[--binary] DATA PATTERN\n");
   return 2;
 }
@@ -96,6 +98,8 @@ int main(int argc, char** argv) {
       else return usage();
     } else if (a == "--iters" && i + 1 < argc) {
       opt.num_iters = std::atoi(argv[++i]);
+    } else if (a == "--cnull") {
+      opt.cnull = 1;
     } else if (a == "--csv") {
       csv = true;
     } else if (a == "--binary") {

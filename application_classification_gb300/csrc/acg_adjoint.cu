@@ -1641,6 +1641,7 @@ acg_status adj_buf(AdjWork* W, size_t bytes, void** out, cudaStream_t s) {
 acg_status adj_check(acg_plan* P, const char* who) {
   if (!P) return set_error(ACG_ERR_INVALID_ARGUMENT, "%s: plan is null", who);
   if (P->is_union) return set_error(ACG_ERR_UNSUPPORTED, "%s: a batch group has no adjoint", who);
+  if (P->cnull) return set_error(ACG_ERR_UNSUPPORTED, "%s: no adjoint of the cnull option", who);
   if (P->Pp > 64 || P->Pn > 64 || !P->init_warp)
     return set_error(ACG_ERR_UNSUPPORTED,
                      "%s: the adjoint is built for patterns of at most 64 vertices and 64 padded edge columns",

@@ -232,6 +232,7 @@ acg_status iterate(acg_plan* P, int t, double* mu_out, cudaStream_t s) {
                       (const T*)P->CVlo, P->gi[(t - 1) & 1], P->gi[t & 1], P->bpart,
                       mu_out, P->pat, Dn, Pn, Pe, Pp, P->Pnp, P->maxdeg, P->iters_p, t,
                       t == 1, t == P->iters};
+  va.cnull = P->cnull;
   const bool rec = P->rec && P->rec->has(t);
   if (rec) {
     va.rec_f = (T*)P->rec->f[t];
@@ -272,6 +273,7 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s, const UnionOut
 
   // ---- cdist (ac.hxx:33-56 via main.cu:109-110) + column stats
   ACG_TRY(Cdist<T>::run(P, D, lim, s));
+  ACG_TRY(run_cnull(P, s));
   cudaEventRecord(P->ev[1], s);
   // ---- static per-vertex reductions (acg_static.cu)
   if (De > 0) {
@@ -411,6 +413,8 @@ acg_status resolve_options(const acg_options* opt, acg_options* o) {
   if (opt) *o = *opt;
   if (o->precision != ACG_PREC_FP64 && o->precision != ACG_PREC_MIXED)
     return set_error(ACG_ERR_INVALID_ARGUMENT, "unknown precision %d", o->precision);
+  if (o->cnull != 0 && o->cnull != 1)
+    return set_error(ACG_ERR_INVALID_ARGUMENT, "cnull must be 0 or 1 (got %d)", o->cnull);
   return ACG_OK;
 }
 
@@ -466,6 +470,10 @@ acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& 
   alloc(sizeof(int) * std::max(1, Pn), (void**)&P->iters_p);
   alloc(sizeof(long long) * Pp, (void**)&P->qlim_col);
   alloc(sizeof(double) * std::max(1, Pn), (void**)&P->S_final);
+  if (o.cnull) {
+    alloc(sizeof(double) * 3 * std::max(1, Pe), (void**)&P->cnull);
+    alloc(sizeof(double) * 3 * std::max(1, Pe) * cnull_blocks(D->num_sms), (void**)&P->cnull_part);
+  }
   if (st != ACG_OK) return fail(st);
   std::vector<long long> qlim(Pp, 0);
   std::copy(spec.qlim.begin(), spec.qlim.end(), qlim.begin());

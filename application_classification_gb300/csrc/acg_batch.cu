@@ -137,6 +137,8 @@ acg_status acg_batch_create(acg_data* D, const acg_graph* patterns, int32_t npat
     return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_batch_create: no patterns");
   acg_options o;
   ACG_TRY(resolve_options(opt, &o));
+  if (o.cnull)
+    return set_error(ACG_ERR_UNSUPPORTED, "acg_batch_create: the cnull option is for single plans");
   o.kernel_timing = 0;
   cudaStream_t s = (cudaStream_t)stream;
   std::unique_ptr<acg_batch, void (*)(acg_batch*)> B(new acg_batch(), destroy);

@@ -296,8 +296,14 @@ vertex_update_kernel(const VertexUpdArgs<T> a) {
       }
       const double cRu = g[x0 + q], cFu = g[x0 + Pe + q];
       const double dR = g[2 * Pe + q], dF = g[3 * Pe + q];
-      s_fillR[q] = (T)(g[q] + cRu - g[4 * Pe + s_pdst[q]]);
-      s_fillF[q] = (T)(g[Pe + q] + cFu - g[4 * Pe + s_psrc[q]]);
+      double fr = g[q] + cRu - g[4 * Pe + s_pdst[q]];
+      double ff = g[Pe + q] + cFu - g[4 * Pe + s_psrc[q]];
+      if (a.cnull) {
+        fr -= a.cnull[q];
+        ff -= a.cnull[q];
+      }
+      s_fillR[q] = (T)fr;
+      s_fillF[q] = (T)ff;
       split(dR, s_dR, s_dRlo, q);
       split(dF, s_dF, s_dFlo, q);
       const double lRp = cRu + dR, lFp = cFu + dF;
@@ -655,8 +661,14 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
       qs[k] = s_psrc[q];
       const double cRu = g[x0 + q], cFu = g[x0 + Pe + q];
       const double dR = g[2 * Pe + q], dF = g[3 * Pe + q];
-      fR[k] = (T)(g[q] + cRu - g[4 * Pe + qd[k]]);
-      fF[k] = (T)(g[Pe + q] + cFu - g[4 * Pe + qs[k]]);
+      double fr = g[q] + cRu - g[4 * Pe + qd[k]];
+      double ff = g[Pe + q] + cFu - g[4 * Pe + qs[k]];
+      if (a.cnull) {
+        fr -= a.cnull[q];
+        ff -= a.cnull[q];
+      }
+      fR[k] = (T)fr;
+      fF[k] = (T)ff;
       dRh[k] = (T)dR;
       dRl[k] = (T)(dR - (double)dRh[k]);
       dFh[k] = (T)dF;

@@ -58,6 +58,8 @@ struct VertexUpdArgs {
   T* rec_r = nullptr;
   T* rec_mh = nullptr;
   T* rec_ml = nullptr;
+  // C-null term ([Pe], subtracted from both fills of each column; null: none)
+  const double* cnull = nullptr;
 };
 // S_final[p] = S[p] of this iteration where it is p's last (S = the column
 // log-sum-exp of MU_raw in the statistics just finalised).

@@ -110,6 +110,8 @@ struct acg_plan {
   cudaStream_t last_stream = nullptr;
   int64_t launches = 0;
   bool ran = false;
+  double* cnull = nullptr;     // [Pe] C-null term, then [2 Pe] dE column stats (option cnull)
+  double* cnull_part = nullptr;  // [3 Pe][cnull_blocks] block partials
   const acg::StateRec* rec = nullptr;  // states to record during a match (adjoint)
   acg::AdjWork* adj = nullptr;         // owned; freed by acg_plan_destroy
   std::vector<acg::DevBuf> owned;
@@ -157,6 +159,10 @@ acg_status run_match_any(acg_plan* P, double* mu_out, cudaStream_t s, const Unio
 // state of iteration t - 1 (vf, vr[(t-1) & 1], gi[(t-1) & 1]); records state t
 // when P->rec asks for it.  mu_out is written only on the last iteration.
 acg_status run_iteration_any(acg_plan* P, int t, double* mu_out, cudaStream_t s);
+
+// The C-null term of a plan with the cnull option (acg_cnull.cu), from its dE.
+acg_status run_cnull(acg_plan* P, cudaStream_t s);
+int cnull_blocks(int num_sms);
 
 // Frees the adjoint's buffers of a plan (acg_adjoint.cu).
 void adj_free(acg_plan* P);

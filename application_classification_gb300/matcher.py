@@ -109,7 +109,7 @@ class Plan:
 
     def __init__(self, data: DataGraph, pattern, precision: str = "fp64", num_iters: int = -1,
                  stream=None, kernel_timing: bool = False, edge_blocks_per_sm: int = 0,
-                 vertex_blocks_per_sm: int = 0):
+                 vertex_blocks_per_sm: int = 0, cnull: bool = False):
         self.data = data
         self.pat = pattern if isinstance(pattern, DeviceGraph) else DeviceGraph(pattern)
         self._c = self.pat.c_graph()
@@ -122,6 +122,7 @@ class Plan:
         opt.kernel_timing = 1 if kernel_timing else 0
         opt.edge_blocks_per_sm = int(edge_blocks_per_sm)
         opt.vertex_blocks_per_sm = int(vertex_blocks_per_sm)
+        opt.cnull = 1 if cnull else 0
         self.precision = precision
         self.handle = C.c_void_p()
         _lib.check(_lib.lib().acg_plan_create(data.handle, C.byref(self._c), C.byref(opt),
@@ -183,7 +184,7 @@ class Plan:
 
 
 def match(data: Graph, pattern: Graph, precision: str = "fp64", num_iters: int = -1,
-          device: str = "cuda") -> np.ndarray:
+          device: str = "cuda", cnull: bool = False) -> np.ndarray:
     """One-shot match of host graphs; returns mu as a [Dn][Pn] float64 numpy array.
 
     This is the reference's whole program between reading the two graph files
@@ -195,6 +196,7 @@ def match(data: Graph, pattern: Graph, precision: str = "fp64", num_iters: int =
     _lib.lib().acg_options_default(C.byref(opt))
     opt.precision = PRECISIONS[precision]
     opt.num_iters = num_iters
+    opt.cnull = 1 if cnull else 0
     cd, cp = dg.c_graph(), pg.c_graph()
     _lib.check(_lib.lib().acg_match_graphs(C.byref(cd), C.byref(cp), C.byref(opt),
                                            C.c_void_p(out.data_ptr()), _stream_ptr(None)),

@@ -76,7 +76,14 @@ typedef struct acg_options {
   int32_t edge_blocks_per_sm;   /* resident 256-thread blocks per SM of the edge
                                    phase and the static passes (0: as many as fit) */
   int32_t vertex_blocks_per_sm; /* the same for the vertex phase (0: as many as fit) */
-  int32_t reserved[3];
+  int32_t cnull;      /* 1: the C-null term of the PNNL formulation, which the
+                         reference leaves out (main.cu:83; test.py:93-97):
+                         cnull = log-softmax over pattern edges q of
+                         max(||pe_q||, max_e L(dE)[q][e]), subtracted from both
+                         max-message fills of column q in every iteration.
+                         0 (default): the reference's behaviour.  Single plans
+                         only (acg_batch_create and the adjoint reject it). */
+  int32_t reserved[2];
 } acg_options;
 
 /* Fill `opt` with the defaults (FP64, num_iters = -1). */

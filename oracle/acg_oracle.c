@@ -156,6 +156,11 @@ int acg_oracle_check(const acg_oracle_graph* data, const acg_oracle_graph* patt)
 
 int acg_oracle_match(const acg_oracle_graph* data, const acg_oracle_graph* patt,
                      int64_t num_iters, double* mu_out, double* elapsed_us) {
+  return acg_oracle_match_opts(data, patt, num_iters, 0, mu_out, elapsed_us);
+}
+
+int acg_oracle_match_opts(const acg_oracle_graph* data, const acg_oracle_graph* patt,
+                          int64_t num_iters, int cnull_on, double* mu_out, double* elapsed_us) {
   const int chk = acg_oracle_check(data, patt);
   if (chk) return chk;
   const uint64_t dn = data->num_nodes, de = data->num_edges;
@@ -211,6 +216,33 @@ int acg_oracle_match(const acg_oracle_graph* data, const acg_oracle_graph* patt,
   edge_max_reduce(de, dn, pe, vfmax, re_t, rmax_t, data->srcs); /* main.cu:138-141 */
   edge_max_reduce(de, dn, pe, vrmax, fe_t, fmax_t, data->dsts); /* main.cu:143-146 */
 
+  /* Optional C-null term, test.py:93-97 (commented out there; the reference's
+   * main.cu:83 leaves it out): cnull = normprob over q of
+   * max(||pe_q||, max_e L(ce)[q][e]); ce_t holds L(ce) here. */
+  double* cnull = NULL;
+  if (cnull_on && pe > 0) {
+    cnull = (double*)calloc(pe, sizeof(double));
+    if (!cnull) {
+      free(cv_t); free(mu_t); free(vrmax); free(vfmax); free(ce_t); free(re_t);
+      free(fe_t); free(vr_t); free(vf_t); free(rmax_t); free(fmax_t);
+      return 2;
+    }
+    const uint64_t ke = patt->edge_feat_dim;
+    double cmax = -INFINITY;
+    for (uint64_t q = 0; q < pe; ++q) {
+      double nn = 0.0;
+      for (uint64_t k = 0; k < ke; ++k) nn += patt->edge_feats[q * ke + k] * patt->edge_feats[q * ke + k];
+      double m = sqrt(nn);
+      for (uint64_t e = 0; e < de; ++e) m = fmax(m, ce_t[q * de + e]);
+      cnull[q] = m;
+      cmax = fmax(cmax, m);
+    }
+    double ssum = 0.0;
+    for (uint64_t q = 0; q < pe; ++q) ssum += exp(cnull[q] - cmax);
+    const double lse = cmax + log(ssum);
+    for (uint64_t q = 0; q < pe; ++q) cnull[q] -= lse;
+  }
+
   /* loop, main.cu:160-245 */
   for (uint64_t it = 0; it < iters; ++it) {
 #pragma omp parallel for schedule(static) /* step1, main.cu:165-176 */
@@ -226,9 +258,13 @@ int acg_oracle_match(const acg_oracle_graph* data, const acg_oracle_graph* patt,
       re_t[off] = vf_t[dn * r + data->srcs[c]] - ce_t[off];
     }
     row_max(pe, dn, vf_t, vfmax);                                 /* step3_a */
+    if (cnull) /* test.py:140: bak_max = max(bak_max, v_fwd_max - cnull) */
+      for (uint64_t q = 0; q < pe; ++q) vfmax[q] -= cnull[q];
     row_softmax(pe, de, re_t);                                    /* step3_b */
     edge_max_reduce(de, dn, pe, vfmax, re_t, rmax_t, data->srcs); /* step3_c */
     row_max(pe, dn, vr_t, vrmax);                                 /* step4 */
+    if (cnull) /* test.py:139: fwd_max = max(fwd_max, v_bak_max - cnull) */
+      for (uint64_t q = 0; q < pe; ++q) vrmax[q] -= cnull[q];
     row_softmax(pe, de, fe_t);
     edge_max_reduce(de, dn, pe, vrmax, fe_t, fmax_t, data->dsts);
     compute_mu(dn, pe, pn, cv_t, fmax_t, rmax_t, patt->srcs, patt->dsts, mu_t); /* step5 */
@@ -245,6 +281,7 @@ int acg_oracle_match(const acg_oracle_graph* data, const acg_oracle_graph* patt,
 
   free(cv_t); free(mu_t); free(vrmax); free(vfmax); free(ce_t); free(re_t);
   free(fe_t); free(vr_t); free(vf_t); free(rmax_t); free(fmax_t);
+  free(cnull);
   return 0;
 }
 

@@ -34,6 +34,11 @@ int acg_oracle_check(const acg_oracle_graph* data, const acg_oracle_graph* patt)
 int acg_oracle_match(const acg_oracle_graph* data, const acg_oracle_graph* patt,
                      int64_t num_iters, double* mu_out, double* elapsed_us);
 
+/* The same with the optional C-null term (test.py:93-97, left out by the
+ * reference: main.cu:83) when cnull_on is nonzero. */
+int acg_oracle_match_opts(const acg_oracle_graph* data, const acg_oracle_graph* patt,
+                          int64_t num_iters, int cnull_on, double* mu_out, double* elapsed_us);
+
 int acg_oracle_threads(void);
 void acg_oracle_set_threads(int n);
 

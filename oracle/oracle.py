@@ -50,6 +50,9 @@ def lib():
         L.acg_oracle_match.argtypes = [C.POINTER(_OG), C.POINTER(_OG), C.c_int64, C.c_void_p,
                                        C.POINTER(C.c_double)]
         L.acg_oracle_match.restype = C.c_int
+        L.acg_oracle_match_opts.argtypes = [C.POINTER(_OG), C.POINTER(_OG), C.c_int64, C.c_int,
+                                            C.c_void_p, C.POINTER(C.c_double)]
+        L.acg_oracle_match_opts.restype = C.c_int
         L.acg_oracle_check.argtypes = [C.POINTER(_OG), C.POINTER(_OG)]
         L.acg_oracle_check.restype = C.c_int
         L.acg_oracle_threads.restype = C.c_int
@@ -65,16 +68,17 @@ def _og(g) -> _OG:
 
 
 def match(data, pattern, num_iters: int = -1, threads: int | None = None,
-          return_elapsed: bool = False):
-    """Oracle mu [Dn][Pn] (float64) for host graphs (``graph.Graph``)."""
+          return_elapsed: bool = False, cnull: bool = False):
+    """Oracle mu [Dn][Pn] (float64) for host graphs (``graph.Graph``); ``cnull``
+    adds the optional C-null term."""
     L = lib()
     if threads:
         L.acg_oracle_set_threads(int(threads))
     mu = np.zeros((data.num_nodes, pattern.num_nodes), dtype=np.float64)
     gd, gp = _og(data), _og(pattern)
     el = C.c_double(0.0)
-    rc = L.acg_oracle_match(C.byref(gd), C.byref(gp), int(num_iters),
-                            mu.ctypes.data if mu.size else None, C.byref(el))
+    rc = L.acg_oracle_match_opts(C.byref(gd), C.byref(gp), int(num_iters), 1 if cnull else 0,
+                                 mu.ctypes.data if mu.size else None, C.byref(el))
     if rc != 0:
         raise ValueError(f"oracle rejected the input (code {rc})")
     return (mu, el.value) if return_elapsed else mu

@@ -23,7 +23,7 @@ def seg(vals, keys, n, op, init):
     return out
 
 
-def match(d, p, num_iters=-1, dt=np.float64):
+def match(d, p, num_iters=-1, dt=np.float64, cnull=False):
     Dn, De, Pn, Pe = d.num_nodes, d.num_edges, p.num_nodes, p.num_edges
     iters = Pn if num_iters < 0 else num_iters
     s, t = d.srcs.astype(np.int64), d.dsts.astype(np.int64)
@@ -46,11 +46,17 @@ def match(d, p, num_iters=-1, dt=np.float64):
     ssum = seg(np.exp(-dE - np.where(np.isfinite(mneg[s]), mneg[s], 0)), s, Dn, np.add, 0.0)
     with np.errstate(divide="ignore"):
         B = np.log(ssum) + mneg                            # log sum_out exp(-dE)
+    cn = np.zeros(Pe)
+    if cnull and Pe:  # test.py:93-97: normprob(max(||pe_q||, max_e L(dE)[q]))
+        cn = np.sqrt((np.asarray(p.edge_feats, float) ** 2).sum(1))
+        if De:
+            cn = np.maximum(cn, (dE - lse(dE, 0)).max(0))
+        cn = cn - lse(cn, 0)
     MU, RMax, FMax, CVc, Bc, dEc, dEmin = (a.astype(dt) for a in (MU, RMax, FMax, CV, B, dE, -mneg))
     for _ in range(iters):
         VF = MU[:, pd] - FMax
         VR = MU[:, ps] - RMax
-        VFm, VRm = VF.max(0), VR.max(0)
+        VFm, VRm = VF.max(0) - cn, VR.max(0) - cn
         SR = lse((VF + Bc).astype(np.float64), 0)
         SF = lse((VR + Bc).astype(np.float64), 0)
         with np.errstate(invalid="ignore"):

@@ -159,3 +159,44 @@ def test_pattern_shapes_vs_oracle(cuda, prec, pn, pe):
     tol = FP64_REL * max(1.0, np.abs(ref).max()) if prec == "fp64" else MIXED_ABS
     assert np.abs(mu - ref).max() <= tol
     assert _argmax_same(mu, ref, tol=1e-9 if prec == "fp64" else 1e-5)
+
+
+@pytest.mark.parametrize("case", ["georgiy", "er300", "rmat12", "rmat10_40_60"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_cnull_vs_oracle(cuda, prec, case):
+    """The optional C-null term against the oracle with the same option."""
+    if case in golden_names():
+        d, p, _ = load_golden(case)
+    else:
+        d, p, _ = graph.workload(case)
+    ref = oracle.match(d, p, cnull=True)
+    mu = matcher.match(d, p, prec, cnull=True)
+    if prec == "fp64":
+        assert np.abs(mu - ref).max() <= FP64_REL * max(1.0, np.abs(ref).max())
+        assert _argmax_same(mu, ref)
+    else:
+        assert np.abs(mu - ref).max() <= MIXED_ABS * max(1.0, np.abs(ref).max() / 100.0)
+        assert _argmax_same(mu, ref, tol=1e-5)
+
+
+def test_cnull_rejected_by_batch_and_adjoint(cuda):
+    d, p, _ = load_golden("er300")
+    data = matcher.DataGraph(d)
+    import ctypes as C
+    from application_classification_gb300 import _lib
+
+    pg = matcher.DeviceGraph(p)
+    arr = (_lib.Graph * 1)(pg.c_graph())
+    opt = _lib.Options()
+    _lib.lib().acg_options_default(C.byref(opt))
+    opt.cnull = 1
+    h = C.c_void_p()
+    st = _lib.lib().acg_batch_create(data.handle, C.cast(arr, C.c_void_p), 1, C.byref(opt),
+                                     matcher._stream_ptr(None), C.byref(h))
+    assert st == 5
+    plan = matcher.Plan(data, p, "fp64", cnull=True)
+    with pytest.raises(AcgError) as e:
+        plan.record()
+    assert e.value.status == 5
+    plan.close()
+    data.close()
