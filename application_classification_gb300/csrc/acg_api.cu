@@ -13,6 +13,7 @@
 #include <cstring>
 #include <limits>
 #include <memory>
+#include <type_traits>
 #include <vector>
 
 #include "acg.h"
@@ -360,6 +361,14 @@ acg_status run_cdist(acg_plan* P, acg_data* D, long long lim, const F* nf, int n
   // rows in dst-CSR order; with no data edges the kernel writes empty partials
   CdistRbArgs<T, F> ae{ef, gather ? D->dcsr.eid : nullptr, D->dcsr.eid, P->pe, (T*)P->dE,
                        nullptr, D->De, D->De, lim, D->Ke, efs, P->Pe, P->Pp, P->Pp};
+  if constexpr (std::is_same_v<T, float> && std::is_same_v<F, float>) {
+    if (P->cdist_tc) {
+      ACG_TRY(launch_cdist_edges_tc(ef, efs, D->Ke, P->pe, P->Pe, P->Pp, (float*)P->dE, D->De,
+                                    P->dev_err, D->num_sms, s));
+      P->launches += 3;
+      return ACG_OK;
+    }
+  }
   ACG_TRY(launch_cdist_edges(ae, P->ce_blocks, s));
   P->launches += 3;
   return ACG_OK;
@@ -415,6 +424,8 @@ acg_status resolve_options(const acg_options* opt, acg_options* o) {
     return set_error(ACG_ERR_INVALID_ARGUMENT, "unknown precision %d", o->precision);
   if (o->cnull != 0 && o->cnull != 1)
     return set_error(ACG_ERR_INVALID_ARGUMENT, "cnull must be 0 or 1 (got %d)", o->cnull);
+  if (o->cdist_kernel < 0 || o->cdist_kernel > 2)
+    return set_error(ACG_ERR_INVALID_ARGUMENT, "cdist_kernel must be 0, 1 or 2 (got %d)", o->cdist_kernel);
   return ACG_OK;
 }
 
@@ -470,6 +481,15 @@ acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& 
   alloc(sizeof(int) * std::max(1, Pn), (void**)&P->iters_p);
   alloc(sizeof(long long) * Pp, (void**)&P->qlim_col);
   alloc(sizeof(double) * std::max(1, Pn), (void**)&P->S_final);
+  alloc(sizeof(int), (void**)&P->dev_err);
+  if (P->prec == ACG_PREC_MIXED && o.cdist_kernel != 1) {
+    P->cdist_tc = cdist_tc_eligible(D->Ke, (D->Ke + 3) / 4 * 4, Pe, Pp);
+    if (!P->cdist_tc && o.cdist_kernel == 2) {
+      dev_free_all(&P->owned);
+      return set_error(ACG_ERR_UNSUPPORTED,
+                       "tensor-core cdist: edge feature dim %d, %d pattern edges", D->Ke, Pe);
+    }
+  }
   if (o.cnull) {
     alloc(sizeof(double) * 3 * std::max(1, Pe), (void**)&P->cnull);
     alloc(sizeof(double) * 3 * std::max(1, Pe) * cnull_blocks(D->num_sms), (void**)&P->cnull_part);
@@ -766,6 +786,13 @@ acg_status acg_plan_stats(acg_plan* P, acg_stats* out) {
   std::memset(out, 0, sizeof *out);
   if (!P->ran) return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_plan_stats: no match has run");
   ACG_CUDA_TRY(cudaEventSynchronize(P->ev[4]));
+  {
+    int err = 0;
+    ACG_CUDA_TRY(cudaMemcpy(&err, P->dev_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err)
+      return set_error(ACG_ERR_DEVICE_TIMEOUT,
+                       "acg_plan_stats: a device-side wait of the last match gave up");
+  }
   float t01 = 0, t12 = 0, t23 = 0, t04 = 0;
   cudaEventElapsedTime(&t01, P->ev[0], P->ev[1]);
   cudaEventElapsedTime(&t12, P->ev[1], P->ev[2]);

@@ -34,4 +34,11 @@ acg_status launch_cdist_rb(const CdistRbArgs<T, F>& a, int mode, int blocks, cud
 template <typename T, typename F>
 acg_status launch_cdist_edges(const CdistRbArgs<T, F>& a, int blocks, cudaStream_t s);
 
+// The edge cost matrix of the mixed path on the tensor cores (acg_cdist_tc.cu):
+// out[r][q] = ||x[r] - y[q]|| for q < P, 0 for P <= q < Pp; x FP32 rows of
+// stride kstride in output order.  *err is set to 1 if a bounded wait gave up.
+bool cdist_tc_eligible(int K, int kstride, int P, int Pp);
+acg_status launch_cdist_edges_tc(const float* x, int kstride, int K, const double* y, int P, int Pp,
+                                 float* out, long long nrows, int* err, int num_sms, cudaStream_t s);
+
 }  // namespace acg

@@ -1,0 +1,472 @@
+// acg_cdist_tc.cu -- the edge cost matrix on the 5th-generation tensor cores
+// (tcgen05), for the mixed-precision path.
+//
+// dE[r][q] = ||x_r - y_q|| (ac.hxx:33-56) as ||x||^2 + ||y||^2 - 2 x.y: the
+// cross term is a [128 rows] x [N columns] x [K'] product per tile, in TF32
+// with a three-term split that carries FP32 accuracy:
+//     x = x0 + x1, y = y0 + y1 (x0 = tf32(x), x1 = tf32(x - x0))
+//     x.y ~ x0.y0 + x1.y0 + x0.y1   (the dropped x1.y1 is ~2^-22 relative)
+// laid out along K as A' = [x0 | x1 | x0], B' = [y0 | y0 | y1] in blocks of KM
+// (the feature dimension padded to 4), K' = 3 KM padded to a multiple of 8
+// (one tcgen05.mma.kind::tf32 per 8).  Both sides are
+// first centred on the mean pattern feature vector m (distances do not change)
+// and the norms are FP32 sums.  The norm form's error scales with
+// ||x - m||^2 + ||y - m||^2 (FP32 accumulation, the dropped x1.y1), not with
+// d^2, so a pair with kNear * d^2 < ||x - m||^2 + ||y - m||^2 is recomputed
+// exactly in the difference form from the FP32 features: near pairs (the
+// planted ones) and data whose feature spread is large against the distances
+// keep full FP32 accuracy.  For N(0,1) features almost no pair is recomputed.
+//
+// One persistent CTA (8 warps) walks tiles of 128 data rows:
+//   feature rows [128][kstride] FP32 --cp.async.bulk (TMA) + mbarrier--> smem
+//     (double-buffered: the next tile's copy flies while this one computes)
+//   threads split them into A' in the no-swizzle K-major core-matrix layout
+//   thread 0 issues K'/8 MMAs into a TMEM accumulator, tcgen05.commit -> mbarrier
+//   warps (lane quarter w % 4, column half w / 4) tcgen05.ld the accumulator,
+//     form d and store their rows' 16-column chunks as 16-byte stores.
+// Every mbarrier wait is bounded: on expiry the CTA records an error flag,
+// waits (bounded) for its own operations in flight, frees its TMEM and exits.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "acg_cdist.cuh"
+#include "acg_device.cuh"
+
+namespace acg {
+
+namespace {
+
+constexpr int kTT = 256;               // threads per CTA
+constexpr int kTM = 128;               // data rows per tile (the MMA's M)
+constexpr long long kSpin = 1LL << 22;  // try_wait rounds before a wait gives up
+#ifndef ACG_TC_NEAR
+#define ACG_TC_NEAR 8.0f
+#endif
+constexpr float kNear = ACG_TC_NEAR;  // see the header: the relative recompute threshold
+constexpr int kStg = 20;  // staging row stride (floats): 16 columns + 16 bytes (no bank conflicts)
+
+// Dynamic shared memory layout (byte offsets, each 128-aligned).
+struct TcLayout {
+  uint32_t a, b, x0, x1, y, nx, ny, mean, bar, tslot, total;
+};
+__host__ __device__ inline uint32_t al128(uint32_t v) { return (v + 127u) & ~127u; }
+__host__ __device__ inline TcLayout tc_layout(int K, int kstride, int Pp, int N) {
+  TcLayout L;
+  (void)K;
+  (void)Pp;
+  const uint32_t kp = (uint32_t)(3 * kstride + 7) / 8 * 8;  // K' padded to the MMA's K step
+  uint32_t o = 0;
+  // A' also holds the epilogue's staging rows (8 warps x 32 rows x kStg)
+  const uint32_t abytes = (uint32_t)kTM * kp * 4, sbytes = (uint32_t)(kTT / 32) * 32 * kStg * 4;
+  L.a = o;     o = al128(o + (abytes > sbytes ? abytes : sbytes));
+  L.b = o;     o = al128(o + (uint32_t)N * kp * 4);
+  L.x0 = o;    o = al128(o + (uint32_t)kTM * kstride * 4);
+  L.x1 = o;    o = al128(o + (uint32_t)kTM * kstride * 4);
+  L.y = o;     o = al128(o + (uint32_t)N * kstride * 4);
+  L.nx = o;    o = al128(o + (uint32_t)kTM * 4);
+  L.ny = o;    o = al128(o + (uint32_t)N * 4);
+  L.mean = o;  o = al128(o + 32 * 4);
+  L.bar = o;   o = al128(o + 3 * 8);
+  L.tslot = o; o = al128(o + 4);
+  L.total = o;
+  return L;
+}
+
+// Byte offset of element (row, k) of a K-major operand with `rows` rows in the
+// no-swizzle canonical layout: core matrices of 8 rows x 16 bytes (4 TF32),
+// stored [k / 4][row / 8][row % 8][k % 4].  Adjacent core matrices along K are
+// rows/8 * 128 bytes apart (the descriptor's leading byte offset), along M/N
+// 128 bytes apart (its stride byte offset).
+__device__ __forceinline__ uint32_t kmaj_off(int row, int k, int rows) {
+  return (uint32_t)(((k >> 2) * (rows >> 3) + (row >> 3)) * 128 + (row & 7) * 16 + (k & 3) * 4);
+}
+
+// Shared-memory matrix descriptor: start, leading and stride byte offsets
+// (>> 4), descriptor version 1 (bits 46-47), base offset 0, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::tf32: D FP32 (bits 4-5 = 1), A and B TF32
+// (bits 7-9, 10-12 = 2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ inline uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (long long i = 0; i < kSpin; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+// Bulk copy global -> shared completing on `bar` (which expects `bytes`).
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, int acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+// 16 consecutive TMEM columns of this warp's 32 lanes (no wait).
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+      "[%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+        "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+        "=r"(v[15])
+      : "r"(taddr)
+      : "memory");
+}
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+struct TcArgs {
+  const float* x;   // [nrows][KM] FP32 features (zero past K), in output row order
+  const double* y;  // [P][K]
+  float* out;       // [nrows][Pp]
+  int* err;         // set to 1 when a bounded wait gave up
+  long long nrows;
+  int K, P, Pp, N, tcols;
+};
+
+// KM: the feature dimension padded to 4 (the FP32 row stride).  A' holds
+// [x0 | x1 | x0] in blocks of KM columns, so each 4-wide core column comes
+// from one block and is one 16-byte store.
+template <int KM>
+__global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
+  constexpr int KP = (3 * KM + 7) / 8 * 8;  // K' padded to the MMA's K step
+  constexpr int KB = KM / 4;                // core columns per block
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const TcLayout L = tc_layout(a.K, KM, a.Pp, a.N);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int K = a.K, P = a.P, Pp = a.Pp, N = a.N;
+  const uint32_t sb = (uint32_t)__cvta_generic_to_shared(sm);
+  float* sA = reinterpret_cast<float*>(sm + L.a);
+  float* sB = reinterpret_cast<float*>(sm + L.b);
+  float* sY = reinterpret_cast<float*>(sm + L.y);
+  float* snx = reinterpret_cast<float*>(sm + L.nx);
+  float* sny = reinterpret_cast<float*>(sm + L.ny);
+  float* smean = reinterpret_cast<float*>(sm + L.mean);
+  const uint32_t bar[3] = {sb + L.bar, sb + L.bar + 8, sb + L.bar + 16};  // x buffers 0, 1; MMA
+  const long long ntiles = (a.nrows + kTM - 1) / kTM;
+
+  if (tid == 0) {
+    mbar_init(bar[0], 1);
+    mbar_init(bar[1], 1);
+    mbar_init(bar[2], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sb + L.tslot),
+                 "r"(a.tcols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    tc_fence_before();
+  }
+  // the centre m (mean pattern feature vector, zero past K) and the FP32
+  // pattern rows for the exact recompute
+  for (int k = tid; k < KM; k += kTT) {
+    float s = 0.f;
+    if (k < K)
+      for (int q = 0; q < P; ++q) s += (float)a.y[(size_t)q * K + k];
+    smean[k] = k < K ? s / (float)P : 0.f;
+  }
+  for (int i = tid; i < N * KM; i += kTT) {
+    const int q = i / KM, k = i - q * KM;
+    sY[i] = (q < P && k < K) ? (float)a.y[(size_t)q * K + k] : 0.f;
+  }
+  __syncthreads();
+  // B' = [y0 | y0 | y1] of y - m (zero rows q >= P and columns k >= 3 KM), the
+  // centred norms; A' zeroed (its padding columns stay zero)
+  for (int i = tid; i < N * KP; i += kTT) {
+    const int q = i / KP, k = i - q * KP;
+    float v = 0.f;
+    if (k < 3 * KM) {
+      const int blk = k / KM, kk = k - blk * KM;
+      const float yc = q < P ? sY[(size_t)q * KM + kk] - smean[kk] : 0.f;
+      const float y0 = tf32_round(yc);
+      v = blk == 2 ? tf32_round(yc - y0) : y0;
+    }
+    *reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(sB) + kmaj_off(q, k, N)) = v;
+  }
+  for (int q = tid; q < N; q += kTT) {
+    float s = 0.f;
+    if (q < P)
+      for (int k = 0; k < KM; ++k) {
+        const float yc = sY[(size_t)q * KM + k] - smean[k];
+        s = fmaf(yc, yc, s);
+      }
+    sny[q] = s;
+  }
+  for (int i = tid; i < kTM * KP; i += kTT) sA[i] = 0.f;
+  for (int r = tid; r < kTM; r += kTT) snx[r] = 0.f;
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + L.tslot);
+
+  const uint32_t lboA = (kTM / 8) * 128, lboB = (uint32_t)(N / 8) * 128, sbo = 128;
+  const uint32_t idesc = idesc_tf32(kTM, N);
+  constexpr uint32_t rowb = (uint32_t)KM * 4;
+  uint32_t ph[3] = {0u, 0u, 0u};
+  bool pend[2] = {false, false};  // a bulk load into buffer i is in flight (uniform)
+  bool pend_mma = false;
+  bool ok = true;
+
+  long long tile = blockIdx.x;
+  if (tile < ntiles) {
+    if (tid == 0) {
+      const int nr = (int)min((long long)kTM, a.nrows - tile * kTM);
+      bulk_load(sb + L.x0, a.x + (size_t)tile * kTM * KM, (uint32_t)nr * rowb, bar[0]);
+    }
+    pend[0] = true;
+  }
+  for (int it = 0; tile < ntiles; tile += gridDim.x, ++it) {
+    const int buf = it & 1;
+    const uint32_t xoff = buf ? L.x1 : L.x0;
+    const long long r0 = tile * kTM;
+    const int nr = (int)min((long long)kTM, a.nrows - r0);
+    // the next tile's features into the other buffer (its readers are done:
+    // the barrier at the end of the previous iteration)
+    const long long nt = tile + gridDim.x;
+    if (nt < ntiles) {
+      if (tid == 0) {
+        const int nn = (int)min((long long)kTM, a.nrows - nt * kTM);
+        fence_proxy_async();
+        bulk_load(sb + (buf ? L.x0 : L.x1), a.x + (size_t)nt * kTM * KM, (uint32_t)nn * rowb,
+                  bar[buf ^ 1]);
+      }
+      pend[buf ^ 1] = true;
+    }
+    ok = mbar_wait(bar[buf], ph[buf]);
+    if (!__syncthreads_and(ok)) break;
+    ph[buf] ^= 1u;
+    pend[buf] = false;
+    const float* sXb = reinterpret_cast<const float*>(sm + xoff);
+    // split: thread (row r, half h): h = 0 writes the x0 blocks and the norm,
+    // h = 1 the x1 block; one 16-byte store per core column
+    {
+      const int r = tid & (kTM - 1), h = tid >> 7;
+      if (r < nr) {
+        const float4* xr = reinterpret_cast<const float4*>(sXb + (size_t)r * KM);
+        unsigned char* A = reinterpret_cast<unsigned char*>(sA);
+        const uint32_t rb = (uint32_t)((r >> 3) * 128 + (r & 7) * 16);
+        float s = 0.f;
+#pragma unroll
+        for (int j = 0; j < KB; ++j) {
+          const float4 xv = xr[j];
+          const float4 mv = reinterpret_cast<const float4*>(smean)[j];
+          float c[4] = {xv.x - mv.x, xv.y - mv.y, xv.z - mv.z, xv.w - mv.w};
+          float h0[4], h1[4];
+#pragma unroll
+          for (int w = 0; w < 4; ++w) {
+            h0[w] = tf32_round(c[w]);
+            h1[w] = tf32_round(c[w] - h0[w]);
+            s = fmaf(c[w], c[w], s);
+          }
+          if (h == 0) {
+            const float4 v0 = make_float4(h0[0], h0[1], h0[2], h0[3]);
+            *reinterpret_cast<float4*>(A + (uint32_t)j * lboA + rb) = v0;
+            *reinterpret_cast<float4*>(A + (uint32_t)(2 * KB + j) * lboA + rb) = v0;
+          } else {
+            *reinterpret_cast<float4*>(A + (uint32_t)(KB + j) * lboA + rb) =
+                make_float4(h1[0], h1[1], h1[2], h1[3]);
+          }
+        }
+        if (h == 0) snx[r] = s;
+      }
+    }
+    fence_proxy_async();  // the generic-proxy writes of A' before the MMA reads them
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int st = 0; st < KP / 8; ++st)
+        tc_mma(tmem, smem_desc(sb + L.a + (uint32_t)st * 2 * lboA, lboA, sbo),
+               smem_desc(sb + L.b + (uint32_t)st * 2 * lboB, lboB, sbo), idesc, st > 0);
+      tc_commit(bar[2]);
+    }
+    pend_mma = true;
+    ok = mbar_wait(bar[2], ph[2]);
+    if (!__syncthreads_and(ok)) break;
+    ph[2] ^= 1u;
+    pend_mma = false;
+    tc_fence_after();
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows) and the
+    // 16-column chunks c = w / 4, w / 4 + 2, ...; each chunk goes through the
+    // warp's own staging rows (in A', idle until the next split) so that a
+    // store instruction writes 8 rows x 64 contiguous bytes.  Leftover values
+    // in A's zero-padding columns meet zero columns of B': they add nothing.
+    {
+      const int rw = (warp & 3) * 32, r = rw + lane;
+      const float nx = snx[r];
+      float* stg = sA + warp * 32 * kStg;  // [32][kStg], 16-column rows + padding
+      // one chunk: d from the accumulator column values, staged, stored
+      auto emit = [&](int c, const uint32_t (&v)[16]) {
+        float d[16];
+#pragma unroll
+        for (int j4 = 0; j4 < 4; ++j4) {
+          const float4 ny4 = reinterpret_cast<const float4*>(sny + c * 16)[j4];
+          const float nyv[4] = {ny4.x, ny4.y, ny4.z, ny4.w};
+#pragma unroll
+          for (int w = 0; w < 4; ++w) {
+            const int j = 4 * j4 + w, q = c * 16 + j;
+            const float sn = nx + nyv[w];
+            float d2 = fmaf(-2.f, __uint_as_float(v[j]), sn);
+            if (q < P && kNear * d2 < sn) {  // cancellation: exact difference form
+              const float* yq = sY + (size_t)q * KM;
+              const float* xr = sXb + (size_t)r * KM;
+              float acc = 0.f;
+#pragma unroll
+              for (int k = 0; k < KM; ++k) {
+                const float t = xr[k] - yq[k];
+                acc = fmaf(t, t, acc);
+              }
+              d2 = acc;
+            }
+            d2 = fmaxf(d2, 0.f);
+            d[j] = (q < P && r < nr) ? (d2 > 0.f ? d2 * rsqrtf(d2) : 0.f) : 0.f;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          *reinterpret_cast<float4*>(stg + lane * kStg + 4 * j) =
+              make_float4(d[4 * j], d[4 * j + 1], d[4 * j + 2], d[4 * j + 3]);
+        __syncwarp();
+        // lane t stores quarter t % 4 of row i * 8 + t / 4
+        const int qt = lane & 3, col = c * 16 + qt * 4;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int rr = i * 8 + (lane >> 2);
+          if (rw + rr < nr && col < Pp)
+            *reinterpret_cast<float4*>(a.out + (size_t)(r0 + rw + rr) * Pp + col) =
+                *reinterpret_cast<const float4*>(stg + rr * kStg + qt * 4);
+        }
+        __syncwarp();
+      };
+      for (int c = warp >> 2; c < N / 16; c += 2) {
+        uint32_t v[16];
+        tc_ld16(tmem + ((uint32_t)rw << 16) + (uint32_t)c * 16, v);
+        tc_wait_ld();
+        emit(c, v);
+      }
+    }
+    tc_fence_before();
+    __syncthreads();  // TMEM read, this x buffer free
+  }
+  if (!ok) {
+    // a wait gave up: record it, then wait (bounded) for what is in flight
+    if (tid == 0) atomicExch(a.err, 1);
+    for (int i = 0; i < 2; ++i)
+      if (pend[i]) mbar_wait(bar[i], ph[i]);
+    if (pend_mma) mbar_wait(bar[2], ph[2]);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tcols)
+                 : "memory");
+  }
+}
+
+}  // namespace
+
+bool cdist_tc_eligible(int K, int kstride, int P, int Pp) {
+  const int N = (Pp + 15) / 16 * 16;
+  return P > 0 && K >= 1 && K <= 32 && kstride == (K + 3) / 4 * 4 && N <= 128;
+}
+
+template <int KM>
+static acg_status launch_tc(const TcArgs& a, int num_sms, cudaStream_t s) {
+  const TcLayout L = tc_layout(a.K, KM, a.Pp, a.N);
+  ACG_CUDA_TRY(cudaFuncSetAttribute(cdist_tc_kernel<KM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)L.total));
+  ACG_CUDA_TRY(cudaFuncSetAttribute(cdist_tc_kernel<KM>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                    100));
+  // resident CTAs per SM from shared memory, registers and TMEM (512 columns)
+  int dev = 0, smem_sm = 0, resv = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  cudaFuncAttributes fa{};
+  ACG_CUDA_TRY(cudaFuncGetAttributes(&fa, cdist_tc_kernel<KM>));
+  const int regs = (fa.numRegs + 7) / 8 * 8;
+  int nb = smem_sm / (int)(L.total + resv);
+  nb = std::min(nb, 65536 / std::max(1, regs * kTT));
+  nb = std::max(1, std::min(nb, 512 / a.tcols));
+  const long long ntiles = (a.nrows + kTM - 1) / kTM;
+  const int grid = (int)std::min<long long>(ntiles, (long long)num_sms * nb);
+  cdist_tc_kernel<KM><<<grid, kTT, L.total, s>>>(a);
+  ACG_LAUNCH_CHECK();
+  return ACG_OK;
+}
+
+acg_status launch_cdist_edges_tc(const float* x, int kstride, int K, const double* y, int P, int Pp,
+                                 float* out, long long nrows, int* err, int num_sms, cudaStream_t s) {
+  if (P == 0 || nrows == 0) return ACG_OK;
+  if (!cdist_tc_eligible(K, kstride, P, Pp))
+    return set_error(ACG_ERR_UNSUPPORTED, "tensor-core cdist: K=%d, %d columns", K, P);
+  TcArgs a;
+  a.x = x;
+  a.y = y;
+  a.out = out;
+  a.err = err;
+  a.nrows = nrows;
+  a.K = K;
+  a.P = P;
+  a.Pp = Pp;
+  a.N = (Pp + 15) / 16 * 16;
+  a.tcols = a.N <= 32 ? 32 : (a.N <= 64 ? 64 : 128);
+  switch (kstride) {
+    case 4: return launch_tc<4>(a, num_sms, s);
+    case 8: return launch_tc<8>(a, num_sms, s);
+    case 12: return launch_tc<12>(a, num_sms, s);
+    case 16: return launch_tc<16>(a, num_sms, s);
+    case 20: return launch_tc<20>(a, num_sms, s);
+    case 24: return launch_tc<24>(a, num_sms, s);
+    case 28: return launch_tc<28>(a, num_sms, s);
+    default: return launch_tc<32>(a, num_sms, s);
+  }
+}
+
+}  // namespace acg

@@ -110,6 +110,8 @@ struct acg_plan {
   cudaStream_t last_stream = nullptr;
   int64_t launches = 0;
   bool ran = false;
+  bool cdist_tc = false;       // edge cost matrix on the tensor cores
+  int* dev_err = nullptr;      // set by a device-side bounded wait that gave up
   double* cnull = nullptr;     // [Pe] C-null term, then [2 Pe] dE column stats (option cnull)
   double* cnull_part = nullptr;  // [3 Pe][cnull_blocks] block partials
   const acg::StateRec* rec = nullptr;  // states to record during a match (adjoint)

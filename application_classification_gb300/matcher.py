@@ -23,6 +23,8 @@ from . import _lib
 from .graph import Graph
 
 PRECISIONS = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
+# acg_options.cdist_kernel: the mixed path's edge cost matrix
+CDIST_KERNELS = {"auto": 0, "simt": 1, "tensor": 2}
 
 
 def _torch():
@@ -109,7 +111,7 @@ class Plan:
 
     def __init__(self, data: DataGraph, pattern, precision: str = "fp64", num_iters: int = -1,
                  stream=None, kernel_timing: bool = False, edge_blocks_per_sm: int = 0,
-                 vertex_blocks_per_sm: int = 0, cnull: bool = False):
+                 vertex_blocks_per_sm: int = 0, cnull: bool = False, cdist_kernel: str = "auto"):
         self.data = data
         self.pat = pattern if isinstance(pattern, DeviceGraph) else DeviceGraph(pattern)
         self._c = self.pat.c_graph()
@@ -123,6 +125,7 @@ class Plan:
         opt.edge_blocks_per_sm = int(edge_blocks_per_sm)
         opt.vertex_blocks_per_sm = int(vertex_blocks_per_sm)
         opt.cnull = 1 if cnull else 0
+        opt.cdist_kernel = CDIST_KERNELS[cdist_kernel]
         self.precision = precision
         self.handle = C.c_void_p()
         _lib.check(_lib.lib().acg_plan_create(data.handle, C.byref(self._c), C.byref(opt),

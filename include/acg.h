@@ -83,7 +83,14 @@ typedef struct acg_options {
                          max-message fills of column q in every iteration.
                          0 (default): the reference's behaviour.  Single plans
                          only (acg_batch_create and the adjoint reject it). */
-  int32_t reserved[2];
+  int32_t cdist_kernel; /* the edge cost matrix of the mixed-precision path:
+                           0 (default) tensor cores (tcgen05, TF32 split, see
+                           acg_cdist_tc.cu) when the shape allows it (edge
+                           feature dim <= 32, <= 128 padded pattern edges),
+                           else CUDA cores; 1 always CUDA cores; 2 tensor
+                           cores or ACG_ERR_UNSUPPORTED.  FP64 plans always
+                           use CUDA cores. */
+  int32_t reserved[1];
 } acg_options;
 
 /* Fill `opt` with the defaults (FP64, num_iters = -1). */

@@ -200,3 +200,46 @@ def test_cnull_rejected_by_batch_and_adjoint(cuda):
     assert e.value.status == 5
     plan.close()
     data.close()
+
+
+# (data vertices, data edges, edge feature dim, pattern vertices, pattern edges)
+TC_SHAPES = [(300, 3000, 17, 6, 10), (1000, 127, 17, 4, 5), (2000, 20000, 1, 5, 8),
+             (2000, 20001, 3, 8, 16), (5000, 60000, 32, 10, 33), (3000, 40000, 17, 16, 64),
+             (3000, 40000, 20, 30, 100)]
+
+
+@pytest.mark.parametrize("dn,de,ke,pn,pe", TC_SHAPES)
+def test_cdist_tensor_cores_vs_cuda_cores(cuda, dn, de, ke, pn, pe):
+    """The mixed path's edge cost matrix on the tensor cores (TF32 split,
+    tcgen05) against the CUDA-core kernel and the oracle: ragged last tiles,
+    1..32 feature dims, 1..7 MMA column blocks."""
+    d = graph.gen_er(dn, de - pe, kv=13, ke=ke, seed=dn + de)
+    d, p, _, _ = graph.plant(d, pn, pe, 0.05, seed=ke)
+    ref = oracle.match(d, p)
+    data = matcher.DataGraph(d)
+    out = {}
+    for kern in ("tensor", "simt"):
+        plan = matcher.Plan(data, p, "mixed", cdist_kernel=kern)
+        out[kern] = plan.run().cpu().numpy()
+        plan.stats()  # raises if a device-side wait gave up
+        plan.close()
+    data.close()
+    scale = max(1.0, np.abs(ref).max() / 100.0)
+    assert np.abs(out["tensor"] - ref).max() <= MIXED_ABS * scale
+    assert np.abs(out["tensor"] - out["simt"]).max() <= MIXED_ABS * scale
+    assert _argmax_same(out["tensor"], ref, tol=1e-5)
+
+
+def test_cdist_tensor_cores_unsupported_shape(cuda):
+    d = graph.gen_er(200, 1000, kv=13, ke=40, seed=1)
+    d, p, _, _ = graph.plant(d, 4, 6, 0.05, seed=1)
+    data = matcher.DataGraph(d)
+    with pytest.raises(AcgError) as e:
+        matcher.Plan(data, p, "mixed", cdist_kernel="tensor")
+    assert e.value.status == 5
+    plan = matcher.Plan(data, p, "mixed")  # auto: falls back to the CUDA cores
+    mu = plan.run().cpu().numpy()
+    ref = oracle.match(d, p)
+    assert np.abs(mu - ref).max() <= MIXED_ABS * max(1.0, np.abs(ref).max() / 100.0)
+    plan.close()
+    data.close()
