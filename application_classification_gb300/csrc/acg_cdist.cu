@@ -162,11 +162,14 @@ cdist_rb_kernel(const CdistRbArgs<T, F> a) {
       e[4] = l2[j].sval();
     }
     __syncthreads();
-    for (int g = tid; g < QG; g += kCT) {
+    // one warp per column group: lanes merge row groups lane, lane + 32, ...,
+    // then a fixed shuffle tree (the FP64 merges run in parallel)
+    const int lane = tid & 31;
+    for (int g = tid >> 5; g < QG; g += kCT / 32) {
       const int q = g * QB + j;
-      if (q >= P) continue;
+      if (q >= P) continue;  // uniform over the warp
       double m = -CUDART_INF, am = -CUDART_INF, as = 0, bm = -CUDART_INF, bs = 0;
-      for (int r = 0; r < RG; ++r) {
+      for (int r = lane; r < RG; r += 32) {
         const double* x = s_red + (size_t)(r * QG + g) * NST;
         if (MODE == kCdistEdge) {
           lse_merge(am, as, x[0], x[1]);
@@ -176,6 +179,15 @@ cdist_rb_kernel(const CdistRbArgs<T, F> a) {
           lse_merge(bm, bs, x[3], x[4]);
         }
       }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        lse_merge(am, as, __shfl_xor_sync(0xffffffffu, am, o), __shfl_xor_sync(0xffffffffu, as, o));
+        if (MODE != kCdistEdge) {
+          m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+          lse_merge(bm, bs, __shfl_xor_sync(0xffffffffu, bm, o), __shfl_xor_sync(0xffffffffu, bs, o));
+        }
+      }
+      if (lane != 0) continue;
       if (MODE == kCdistEdge) {  // StatSpec{0, P}
         a.bpart[(size_t)(2 * q) * ncols + col] = am;
         a.bpart[(size_t)(2 * q + 1) * ncols + col] = as;
