@@ -71,7 +71,7 @@ class HostGraph(C.Structure):
 class Options(C.Structure):
     _fields_ = [("precision", i32), ("num_iters", i32), ("kernel_timing", i32),
                 ("edge_blocks_per_sm", i32), ("vertex_blocks_per_sm", i32),
-                ("cnull", i32), ("cdist_kernel", i32), ("reserved", i32 * 1)]
+                ("cnull", i32), ("cdist_kernel", i32), ("autotune", i32)]
 
 
 class Stats(C.Structure):
@@ -92,7 +92,11 @@ class Stats(C.Structure):
 
 class BatchInfo(C.Structure):
     _fields_ = [("patterns", i32), ("groups", i32), ("widest_group_columns", i32),
-                ("reserved", i32), ("graph_nodes", i64), ("ms_last", C.c_double)]
+                ("autotuned", i32), ("graph_nodes", i64), ("ms_last", C.c_double),
+                ("iter_ms_per_column", C.c_double), ("iter_ms_fixed", C.c_double),
+                ("once_ms_per_column", C.c_double), ("once_ms_fixed", C.c_double),
+                ("predicted_ms", C.c_double), ("edge_blocks_per_sm", i32),
+                ("vertex_blocks_per_sm", i32)]
 
 
 class AcgError(RuntimeError):

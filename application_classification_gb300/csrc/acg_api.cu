@@ -424,6 +424,8 @@ acg_status resolve_options(const acg_options* opt, acg_options* o) {
     return set_error(ACG_ERR_INVALID_ARGUMENT, "unknown precision %d", o->precision);
   if (o->cnull != 0 && o->cnull != 1)
     return set_error(ACG_ERR_INVALID_ARGUMENT, "cnull must be 0 or 1 (got %d)", o->cnull);
+  if (o->autotune != 0 && o->autotune != 1)
+    return set_error(ACG_ERR_INVALID_ARGUMENT, "autotune must be 0 or 1 (got %d)", o->autotune);
   if (o->cdist_kernel < 0 || o->cdist_kernel > 2)
     return set_error(ACG_ERR_INVALID_ARGUMENT, "cdist_kernel must be 0, 1 or 2 (got %d)", o->cdist_kernel);
   return ACG_OK;

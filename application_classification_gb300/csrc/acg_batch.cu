@@ -41,6 +41,7 @@ struct acg_batch {
   cudaStream_t exec_stream = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr, fence = nullptr;
   bool timed = false;
+  acg_batch_info tune{};                  // autotune results (model, shape)
 };
 
 namespace {
@@ -123,6 +124,171 @@ acg_status union_spec(acg_data* D, const std::vector<HostPattern>& hp, const std
   return ACG_OK;
 }
 
+// ---------------------------------------------------------------- autotune
+constexpr int kProbeIters = 3;
+
+// One probe: the union of `mem` with every member running kProbeIters BP
+// iterations, on its own (non-shared) workspaces, matched twice; the second
+// match gives the time per iteration and the time outside the iterations.
+acg_status probe(acg_data* D, const std::vector<HostPattern>& hp, const std::vector<int>& mem,
+                 const acg_options& o, double* mu_scratch, cudaStream_t s, double* ms_iter,
+                 double* ms_once) {
+  std::vector<DevBuf> owned;
+  PatternSpec sp;
+  acg_status st = union_spec(D, hp, mem, &owned, s, &sp);
+  acg_plan* P = nullptr;
+  if (st == ACG_OK) {
+    for (int& x : sp.iters_p) x = kProbeIters;
+    st = plan_create_impl(D, std::move(sp), o, s, false, &P);
+  }
+  for (int k = 0; k < 2 && st == ACG_OK; ++k) st = run_match_any(P, mu_scratch, s, nullptr);
+  if (st == ACG_OK) {
+    if (cudaEventSynchronize(P->ev[4]) != cudaSuccess)
+      st = set_error(ACG_ERR_CUDA, "autotune probe: %s", cudaGetErrorString(cudaGetLastError()));
+    float t02 = 0, t23 = 0, t34 = 0, t01 = 0, t12 = 0;
+    cudaEventElapsedTime(&t01, P->ev[0], P->ev[1]);
+    cudaEventElapsedTime(&t12, P->ev[1], P->ev[2]);
+    cudaEventElapsedTime(&t23, P->ev[2], P->ev[3]);
+    cudaEventElapsedTime(&t34, P->ev[3], P->ev[4]);
+    t02 = t01 + t12;
+    *ms_iter = t23 / kProbeIters;
+    *ms_once = t02 + t34;
+  }
+  if (P) acg_plan_destroy(P);
+  cudaStreamSynchronize(s);  // the plan's work is done before its member features go
+  dev_free_all(&owned);
+  return st;
+}
+
+// The first patterns of `order` packed greedily up to `cols` columns.
+std::vector<int> prefix_group(const std::vector<HostPattern>& hp, const std::vector<int>& order,
+                              int cols) {
+  std::vector<int> g;
+  int c = 0, v = 0;
+  for (int i : order) {
+    if (hp[i].pe > kGroupCols || hp[i].pn > kGroupVerts) continue;
+    if (!g.empty() && (c + hp[i].pe > cols || v + hp[i].pn > kGroupVerts || (int)g.size() == kMaxUnion))
+      break;
+    g.push_back(i);
+    c += hp[i].pe;
+    v += hp[i].pn;
+  }
+  return g;
+}
+
+int cols_of(const std::vector<HostPattern>& hp, const std::vector<int>& g) {
+  int c = 0;
+  for (int i : g) c += hp[i].pe;
+  return c;
+}
+
+// Measure the cost model and the launch shape (see acg.h); fills B->tune and
+// the chosen shape into *o.
+acg_status autotune(acg_batch* B, const std::vector<HostPattern>& hp, const std::vector<int>& order,
+                    acg_options* o, cudaStream_t s) {
+  acg_data* D = B->data;
+  std::vector<DevBuf> owned;
+  double* mu = nullptr;
+  acg_status st = dev_alloc(&owned, sizeof(double) * (size_t)D->Dn * kGroupVerts + 8, (void**)&mu, s);
+  const std::vector<int> g64 = prefix_group(hp, order, kGroupCols);
+  if (st == ACG_OK && g64.empty()) st = set_error(ACG_ERR_UNSUPPORTED, "autotune: no pattern fits a group");
+  // launch shape: blocks per SM of the edge-side and the vertex-side passes
+  // (0 = as many as fit)
+  const int shapes[4][2] = {{0, 0}, {2, 0}, {0, 1}, {2, 1}};
+  double best = 1e300, it64 = 0, once64 = 0;
+  int bs = 0;
+  for (int k = 0; k < 4 && st == ACG_OK; ++k) {
+    acg_options oo = *o;
+    oo.edge_blocks_per_sm = shapes[k][0];
+    oo.vertex_blocks_per_sm = shapes[k][1];
+    double mi = 0, mo = 0;
+    st = probe(D, hp, g64, oo, mu, s, &mi, &mo);
+    if (st == ACG_OK && mi < best) {
+      best = mi;
+      bs = k;
+      it64 = mi;
+      once64 = mo;
+    }
+  }
+  if (st == ACG_OK) {
+    o->edge_blocks_per_sm = shapes[bs][0];
+    o->vertex_blocks_per_sm = shapes[bs][1];
+    // the linear model from three widths (least squares in the columns)
+    std::vector<double> xc, yi, yo;
+    xc.push_back(cols_of(hp, g64));
+    yi.push_back(it64);
+    yo.push_back(once64);
+    for (int w : {kGroupCols / 4, kGroupCols / 2}) {
+      const std::vector<int> g = prefix_group(hp, order, w);
+      double mi = 0, mo = 0;
+      st = probe(D, hp, g, *o, mu, s, &mi, &mo);
+      if (st != ACG_OK) break;
+      xc.push_back(cols_of(hp, g));
+      yi.push_back(mi);
+      yo.push_back(mo);
+    }
+    if (st == ACG_OK) {
+      auto fit = [&](const std::vector<double>& y, double* slope, double* icpt) {
+        double mx = 0, my = 0;
+        for (size_t i = 0; i < xc.size(); ++i) {
+          mx += xc[i];
+          my += y[i];
+        }
+        mx /= xc.size();
+        my /= xc.size();
+        double sxy = 0, sxx = 0;
+        for (size_t i = 0; i < xc.size(); ++i) {
+          sxy += (xc[i] - mx) * (y[i] - my);
+          sxx += (xc[i] - mx) * (xc[i] - mx);
+        }
+        *slope = sxx > 0 ? std::max(0.0, sxy / sxx) : 0.0;
+        *icpt = std::max(0.0, my - *slope * mx);
+      };
+      fit(yi, &B->tune.iter_ms_per_column, &B->tune.iter_ms_fixed);
+      fit(yo, &B->tune.once_ms_per_column, &B->tune.once_ms_fixed);
+      B->tune.edge_blocks_per_sm = o->edge_blocks_per_sm;
+      B->tune.vertex_blocks_per_sm = o->vertex_blocks_per_sm;
+      B->tune.autotuned = 1;
+    }
+  }
+  cudaStreamSynchronize(s);
+  dev_free_all(&owned);
+  return st;
+}
+
+// Groups as contiguous runs of `order` (sorted by iteration count) minimising
+// the model's total: a run's cost is iters(last) * (a c + b) + (e c + f).
+std::vector<std::vector<int>> plan_groups(const std::vector<HostPattern>& hp, const std::vector<int>& order,
+                                          const acg_batch_info& m, double* total) {
+  const int n = (int)order.size();
+  std::vector<double> best(n + 1, 1e300);
+  std::vector<int> from(n + 1, 0);
+  best[0] = 0;
+  for (int i = 1; i <= n; ++i) {
+    int cols = 0, verts = 0;
+    bool alone = false;
+    for (int j = i - 1; j >= 0; --j) {
+      const HostPattern& h = hp[order[j]];
+      cols += h.pe;
+      verts += h.pn;
+      alone = alone || h.pe > kGroupCols || h.pn > kGroupVerts;
+      const int cnt = i - j;
+      if (cnt > 1 && (alone || cols > kGroupCols || verts > kGroupVerts || cnt > kMaxUnion)) break;
+      const double cost = hp[order[i - 1]].iters * (m.iter_ms_per_column * cols + m.iter_ms_fixed) +
+                          m.once_ms_per_column * cols + m.once_ms_fixed;
+      if (best[j] + cost < best[i]) {
+        best[i] = best[j] + cost;
+        from[i] = j;
+      }
+    }
+  }
+  std::vector<std::vector<int>> groups;
+  for (int i = n; i > 0; i = from[i]) groups.emplace_back(order.begin() + from[i], order.begin() + i);
+  std::reverse(groups.begin(), groups.end());
+  *total = best[n];
+  return groups;
+}
+
 }  // namespace
 
 extern "C" {
@@ -177,7 +343,12 @@ acg_status acg_batch_create(acg_data* D, const acg_graph* patterns, int32_t npat
   std::vector<int> order(npatterns);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hp[a].iters < hp[b].iters; });
-  {
+  if (o.autotune && D->Dn > 0) {
+    ACG_TRY(autotune(B.get(), hp, order, &o, s));
+    double total = 0;
+    B->members = plan_groups(hp, order, B->tune, &total);
+    B->tune.predicted_ms = total;
+  } else {
     std::vector<int> cur;
     int cols = 0, verts = 0;
     for (int i : order) {
@@ -301,6 +472,14 @@ acg_status acg_batch_get_info(acg_batch* B, acg_batch_info* out) {
   int widest_cols = 0;
   for (acg_plan* P : B->plans) widest_cols = std::max(widest_cols, P->Pe);
   out->widest_group_columns = widest_cols;
+  out->autotuned = B->tune.autotuned;
+  out->iter_ms_per_column = B->tune.iter_ms_per_column;
+  out->iter_ms_fixed = B->tune.iter_ms_fixed;
+  out->once_ms_per_column = B->tune.once_ms_per_column;
+  out->once_ms_fixed = B->tune.once_ms_fixed;
+  out->predicted_ms = B->tune.predicted_ms;
+  out->edge_blocks_per_sm = B->tune.edge_blocks_per_sm;
+  out->vertex_blocks_per_sm = B->tune.vertex_blocks_per_sm;
   if (B->timed) {
     ACG_CUDA_TRY(cudaEventSynchronize(B->e1));
     float ms = 0;

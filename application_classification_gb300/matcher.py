@@ -214,7 +214,7 @@ class Batch:
     batch runs as one CUDA graph launch per :meth:`run`."""
 
     def __init__(self, data: DataGraph, patterns, precision: str = "fp64", num_iters: int = -1,
-                 stream=None):
+                 stream=None, autotune: bool = False):
         self.data = data
         self.pats = [p if isinstance(p, DeviceGraph) else DeviceGraph(p) for p in patterns]
         arr = (_lib.Graph * len(self.pats))(*[p.c_graph() for p in self.pats])
@@ -225,6 +225,7 @@ class Batch:
             raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
         opt.precision = PRECISIONS[precision]
         opt.num_iters = num_iters
+        opt.autotune = 1 if autotune else 0
         self.precision = precision
         self.handle = C.c_void_p()
         _lib.check(_lib.lib().acg_batch_create(data.handle, C.cast(arr, C.c_void_p), len(self.pats),
@@ -251,7 +252,7 @@ class Batch:
     def info(self) -> dict:
         inf = _lib.BatchInfo()
         _lib.check(_lib.lib().acg_batch_get_info(self.handle, C.byref(inf)), "acg_batch_get_info")
-        return {k: getattr(inf, k) for k, _ in _lib.BatchInfo._fields_ if k != "reserved"}
+        return {k: getattr(inf, k) for k, _ in _lib.BatchInfo._fields_}
 
     def close(self):
         if self.handle:

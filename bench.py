@@ -92,6 +92,8 @@ def parse():
     ap.add_argument("--adjoint-workload", default="rmat16")
     ap.add_argument("--checkpoint-every", type=int, default=4)
     ap.add_argument("--batch-scale", type=int, default=20)
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batch mode: greedy grouping with the default launch shapes")
     ap.add_argument("--batch-patterns", type=int, default=64)
     ap.add_argument("--fp64-sample", type=int, default=16,
                     help="patterns timed in sequential FP64 (scaled to all of them)")
@@ -473,7 +475,7 @@ def run_batch(args, ws, rank, local):
     dg = matcher.DataGraph(d)
     prec = args.precision
     t0 = time.time()
-    b = matcher.Batch(dg, pats, prec)
+    b = matcher.Batch(dg, pats, prec, autotune=not args.no_autotune)
     create_s = time.time() - t0
     for _ in range(max(1, args.warmup)):
         b.run()
@@ -492,6 +494,18 @@ def run_batch(args, ws, rank, local):
     info = b.info()
     mus = [o.cpu().numpy() for o in outs]
     del b
+    greedy = None
+    if not args.no_autotune:  # the default grouping, for comparison (one timed run)
+        bg = matcher.Batch(dg, pats, prec)
+        bg.run()
+        torch.cuda.synchronize()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        bg.run()
+        g1.record(stream)
+        torch.cuda.synchronize()
+        greedy = {"ms": round(g0.elapsed_time(g1), 2), "groups": bg.info()["groups"]}
+        del bg
 
     def sequential(precision, subset):
         # one plan at a time (all of them at once would not fit in memory); the
@@ -538,6 +552,7 @@ def run_batch(args, ws, rank, local):
                        "pattern_edges_total": sum(p.num_edges for p in pats),
                        "generation_s": round(gen_s, 1), "batch_create_s": round(create_s, 1)},
             "batch": info,
+            "greedy_grouping": greedy,
             "sequential_same_precision_ms": round(ms_seq, 2),
             "speedup_vs_sequential_same_precision": round(ms_seq / ms_batch, 3),
             "max_abs_dmu_vs_sequential": err,

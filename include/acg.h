@@ -90,7 +90,9 @@ typedef struct acg_options {
                            else CUDA cores; 1 always CUDA cores; 2 tensor
                            cores or ACG_ERR_UNSUPPORTED.  FP64 plans always
                            use CUDA cores. */
-  int32_t reserved[1];
+  int32_t autotune;   /* acg_batch_create only: 1 = measure before grouping
+                         (see acg_batch_create); 0 (default) = greedy packing
+                         with the default launch shapes */
 } acg_options;
 
 /* Fill `opt` with the defaults (FP64, num_iters = -1). */
@@ -170,10 +172,23 @@ typedef struct acg_batch_info {
   int32_t patterns;
   int32_t groups;               /* unions matched */
   int32_t widest_group_columns; /* pattern edges of the widest group */
-  int32_t reserved;
+  int32_t autotuned;            /* 1 if the grouping and launch shape were measured */
   int64_t graph_nodes;          /* nodes of the captured CUDA graph */
   double ms_last;               /* device time of the last acg_batch_match */
+  /* autotune: the fitted cost model of a group with c columns running i
+     iterations, ms = i * (iter_ms_per_column * c + iter_ms_fixed)
+     + once_ms_per_column * c + once_ms_fixed, and the launch shape chosen */
+  double iter_ms_per_column, iter_ms_fixed, once_ms_per_column, once_ms_fixed;
+  double predicted_ms;          /* the model's total for the chosen grouping */
+  int32_t edge_blocks_per_sm, vertex_blocks_per_sm;
 } acg_batch_info;
+/* With opt->autotune = 1, acg_batch_create first measures the data graph:
+ * short probe matches (three BP iterations) of real pattern unions of about
+ * 16, 32 and 64 columns give a linear cost model per iteration and per group,
+ * a few block-per-SM launch shapes are timed on the widest probe, and the
+ * grouping is then chosen by dynamic programming over the patterns sorted by
+ * iteration count to minimise the model's total (a group iterates as long as
+ * its longest member).  Costs a few probe matches at creation. */
 acg_status acg_batch_create(acg_data* data, const acg_graph* patterns,
                             int32_t npatterns, const acg_options* opt,
                             void* stream, acg_batch** out);

@@ -15,9 +15,9 @@ pytestmark = pytest.mark.gpu
 FP64_REL = 1e-10
 
 
-def _batch_vs_single(d, pats, prec, tol_abs=None):
+def _batch_vs_single(d, pats, prec, tol_abs=None, autotune=False):
     dg = matcher.DataGraph(d)
-    b = matcher.Batch(dg, pats, prec)
+    b = matcher.Batch(dg, pats, prec, autotune=autotune)
     outs = [o.cpu().numpy() for o in b.run()]
     info = b.info()
     assert info["patterns"] == len(pats) and info["groups"] < len(pats)
@@ -75,3 +75,19 @@ def test_batch_rejects_bad_pattern(cuda):
     bad = graph.gen_er(5, 6, kv=4, ke=17, seed=1)  # vertex features of another width
     with pytest.raises(AcgError):
         matcher.Batch(matcher.DataGraph(d), [pats[0], bad], "fp64")
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_batch_autotune(cuda, prec):
+    """The autotuned grouping (measured cost model, dynamic programming over
+    the patterns sorted by iteration count, a measured launch shape) keeps
+    every member equal to its single match, and reports its model."""
+    d, pats, _ = graph.batch_workload(12, 16, seed=9)
+    _, b, outs = _batch_vs_single(d, pats, prec, None if prec == "fp64" else 2e-5, autotune=True)
+    info = b.info()
+    assert info["autotuned"] == 1
+    assert info["iter_ms_per_column"] >= 0 and info["once_ms_fixed"] >= 0
+    assert info["predicted_ms"] > 0
+    assert info["edge_blocks_per_sm"] in (0, 2) and info["vertex_blocks_per_sm"] in (0, 1)
+    assert 1 <= info["groups"] <= len(pats)
+    assert info["ms_last"] > 0
