@@ -42,6 +42,7 @@ struct acg_batch {
   cudaEvent_t e0 = nullptr, e1 = nullptr, fence = nullptr;
   bool timed = false;
   acg_batch_info tune{};                  // autotune results (model, shape)
+  double wide_iter_per_col = 0, wide_once_per_col = 0;  // patterns too wide to share a group
 };
 
 namespace {
@@ -246,6 +247,19 @@ acg_status autotune(acg_batch* B, const std::vector<HostPattern>& hp, const std:
       };
       fit(yi, &B->tune.iter_ms_per_column, &B->tune.iter_ms_fixed);
       fit(yo, &B->tune.once_ms_per_column, &B->tune.once_ms_fixed);
+      // patterns too wide to share a group run alone (the tile-form kernels):
+      // a per-column cost from the widest of them
+      int wi = -1;
+      for (int i : order)
+        if ((hp[i].pe > kGroupCols || hp[i].pn > kGroupVerts) && (wi < 0 || hp[i].pe > hp[wi].pe)) wi = i;
+      if (wi >= 0 && hp[wi].pe > 0) {
+        double mi = 0, mo = 0;
+        st = probe(D, hp, {wi}, *o, mu, s, &mi, &mo);
+        if (st == ACG_OK) {
+          B->wide_iter_per_col = mi / hp[wi].pe;
+          B->wide_once_per_col = mo / hp[wi].pe;
+        }
+      }
       B->tune.edge_blocks_per_sm = o->edge_blocks_per_sm;
       B->tune.vertex_blocks_per_sm = o->vertex_blocks_per_sm;
       B->tune.autotuned = 1;
@@ -259,7 +273,8 @@ acg_status autotune(acg_batch* B, const std::vector<HostPattern>& hp, const std:
 // Groups as contiguous runs of `order` (sorted by iteration count) minimising
 // the model's total: a run's cost is iters(last) * (a c + b) + (e c + f).
 std::vector<std::vector<int>> plan_groups(const std::vector<HostPattern>& hp, const std::vector<int>& order,
-                                          const acg_batch_info& m, double* total) {
+                                          const acg_batch_info& m, double wide_iter, double wide_once,
+                                          double* total) {
   const int n = (int)order.size();
   std::vector<double> best(n + 1, 1e300);
   std::vector<int> from(n + 1, 0);
@@ -274,8 +289,10 @@ std::vector<std::vector<int>> plan_groups(const std::vector<HostPattern>& hp, co
       alone = alone || h.pe > kGroupCols || h.pn > kGroupVerts;
       const int cnt = i - j;
       if (cnt > 1 && (alone || cols > kGroupCols || verts > kGroupVerts || cnt > kMaxUnion)) break;
-      const double cost = hp[order[i - 1]].iters * (m.iter_ms_per_column * cols + m.iter_ms_fixed) +
-                          m.once_ms_per_column * cols + m.once_ms_fixed;
+      double cost = hp[order[i - 1]].iters * (m.iter_ms_per_column * cols + m.iter_ms_fixed) +
+                    m.once_ms_per_column * cols + m.once_ms_fixed;
+      if (alone && wide_iter > 0)  // a pattern that runs alone in the tile-form kernels
+        cost = hp[order[i - 1]].iters * wide_iter * cols + wide_once * cols;
       if (best[j] + cost < best[i]) {
         best[i] = best[j] + cost;
         from[i] = j;
@@ -346,7 +363,7 @@ acg_status acg_batch_create(acg_data* D, const acg_graph* patterns, int32_t npat
   if (o.autotune && D->Dn > 0) {
     ACG_TRY(autotune(B.get(), hp, order, &o, s));
     double total = 0;
-    B->members = plan_groups(hp, order, B->tune, &total);
+    B->members = plan_groups(hp, order, B->tune, B->wide_iter_per_col, B->wide_once_per_col, &total);
     B->tune.predicted_ms = total;
   } else {
     std::vector<int> cur;

@@ -553,6 +553,8 @@ def run_batch(args, ws, rank, local):
                        "generation_s": round(gen_s, 1), "batch_create_s": round(create_s, 1)},
             "batch": info,
             "greedy_grouping": greedy,
+            "autotune_model_over_measured": (round(info["predicted_ms"] / ms_batch, 3)
+                                             if info.get("autotuned") else None),
             "sequential_same_precision_ms": round(ms_seq, 2),
             "speedup_vs_sequential_same_precision": round(ms_seq / ms_batch, 3),
             "max_abs_dmu_vs_sequential": err,
