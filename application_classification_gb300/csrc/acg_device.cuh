@@ -68,6 +68,7 @@ struct OnlineLse<double> {
   }
   // add x = hi + lo (lo tiny next to hi)
   __device__ __forceinline__ void add2(double hi, double lo) { add(hi + lo); }
+  __device__ __forceinline__ void add2_fast(double hi, double lo) { add(hi + lo); }
   __device__ __forceinline__ void add_fast(double x) { add(x); }
   __device__ __forceinline__ double mval() const { return m; }
   __device__ __forceinline__ double sval() const { return s; }
@@ -112,6 +113,15 @@ struct OnlineLse<float> {
     } else {
       kahan(expf(hi - m) * (1.f + lo));
     }
+  }
+  // add2 for finite hi, branch-free with the fast exponential (hot path)
+  __device__ __forceinline__ void add2_fast(float hi, float lo) {
+    const float mn = fmaxf(m, hi);
+    const float sc = __expf(m - mn);  // m = -inf -> 0
+    s *= sc;
+    c *= sc;
+    kahan(__expf(hi - mn) * (1.f + lo));
+    m = mn;
   }
   // Branch-free variant with the fast exponential, for the hot per-vertex
   // statistics: m' = max(m, x); s = s e^(m - m') + e^(x - m').  Terms near the

@@ -707,6 +707,24 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
     plast[j] = p < Pn && __ldg(a.iters_p + p) == a.t;
   }
   __syncthreads();  // s_inc complete
+  // With maxdeg <= kPackDeg the lane's incidence codes (< 256) live in
+  // registers, four to a word; the padding codes index a zero.
+  constexpr int kPackDeg = 16;
+  const bool packed = maxdeg <= kPackDeg;
+  uint32_t pk[PPL][kPackDeg / 4];
+#pragma unroll
+  for (int j = 0; j < PPL; ++j)
+#pragma unroll
+    for (int w = 0; w < kPackDeg / 4; ++w) {
+      uint32_t x = 0;
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const int t = 4 * w + b;
+        const uint32_t c = packed && t < maxdeg ? (uint32_t)s_inc[(j * maxdeg + t) * 32 + lane] : (uint32_t)kZero;
+        x |= c << (8 * b);
+      }
+      pk[j][w] = x;
+    }
 
   const long long nw = (long long)gridDim.x * kVw;
   const long long gw = (long long)blockIdx.x * kVw + wib;
@@ -774,12 +792,25 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
         mu.init(p < Pn ? -sC[p] : T(0));
         if constexpr (sizeof(T) == 4)
           mu.lo = p < Pn ? -(reinterpret_cast<const T*>(st + L.oCl) + jv * Pnp)[p] : T(0);
-        const int* inc = s_inc + j * maxdeg * 32 + lane;
-        for (int t = 0; t < maxdeg; ++t) mu.add(sfr[inc[t * 32]]);
+        if (packed) {
+#pragma unroll
+          for (int w = 0; w < kPackDeg / 4; ++w) {
+            if (4 * w < maxdeg) {  // uniform over the warp
+              const uint32_t x = pk[j][w];
+              mu.add(sfr[x & 0xffu]);
+              mu.add(sfr[(x >> 8) & 0xffu]);
+              mu.add(sfr[(x >> 16) & 0xffu]);
+              mu.add(sfr[x >> 24]);
+            }
+          }
+        } else {
+          const int* inc = s_inc + j * maxdeg * 32 + lane;
+          for (int t = 0; t < maxdeg; ++t) mu.add(sfr[inc[t * 32]]);
+        }
         smu[p] = mu.hi;
         if constexpr (sizeof(T) == 4) smu[32 * PPL + p] = mu.lo;
         if (p < Pn) {
-          lmu[j].add2(mu.hi, mu.lo);
+          lmu[j].add2_fast(mu.hi, mu.lo);
           if (plast[j]) a.mu_raw[(size_t)v * Pn + p] = mu.dvalue();
           if (a.rec_mh) {
             a.rec_mh[(size_t)v * Pn + p] = mu.hi;
