@@ -32,8 +32,10 @@ constexpr int kST = 256;  // threads per block (the edge phase's warp work uses 
 #ifndef ACG_SRC_KU
 #define ACG_SRC_KU 4
 #endif
+// An explicit minimum of one block per SM (the compiler then keeps more of the
+// pipelined loads in registers): static passes 14.3 -> 10.3 ms at RMAT-22.
 #ifndef ACG_SRC_MINB
-#define ACG_SRC_MINB 0
+#define ACG_SRC_MINB 1
 #endif
 constexpr int kSU = ACG_SRC_KU;  // load steps issued back to back
 
