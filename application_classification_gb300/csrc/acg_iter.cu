@@ -33,7 +33,12 @@ namespace acg {
 namespace {
 
 constexpr int kAT = 256;       // threads per block, phase A
-constexpr int kU = 4;          // edge steps issued back to back
+// 3 steps in flight measured fastest at RMAT-22 (4.07 ms per edge phase; 2: 4.44,
+// 4: 4.47, 5: 4.36, 6: 5.37, 8: 5.21 ms)
+#ifndef ACG_EDGE_KU
+#define ACG_EDGE_KU 3
+#endif
+constexpr int kU = ACG_EDGE_KU;  // edge steps issued back to back
 constexpr int kBT = 256;       // threads per block, phase B
 
 template <typename T>
@@ -70,8 +75,11 @@ __host__ __device__ inline size_t a16(size_t b) { return (b + 15) & ~size_t(15);
 // (An explicit minimum of one block per SM lets the compiler keep more of the
 // pipelined loads in registers: 72 registers and 3 blocks/SM measured faster
 // than 56 registers and 4 blocks/SM at RMAT-22, 4.47 ms against 5.30 ms.)
+#ifndef ACG_EDGE_MINB
+#define ACG_EDGE_MINB 1
+#endif
 template <typename T, int NPOW, int NQV>
-__global__ void __launch_bounds__(kAT, 1)
+__global__ void __launch_bounds__(kAT, ACG_EDGE_MINB)
 edge_max_kernel(const EdgeMaxArgs<T> a) {
   using VT = typename VecT<T>::type;
   constexpr int W = VecT<T>::W;

@@ -83,7 +83,9 @@ def test_batch_autotune(cuda, prec):
     the patterns sorted by iteration count, a measured launch shape) keeps
     every member equal to its single match, and reports its model."""
     d, pats, _ = graph.batch_workload(12, 16, seed=9)
-    _, b, outs = _batch_vs_single(d, pats, prec, None if prec == "fp64" else 2e-5, autotune=True)
+    # mixed: the tuned launch shape changes the order of the FP32 partial sums;
+    # member and single match are each within ~2e-5 of FP64
+    _, b, outs = _batch_vs_single(d, pats, prec, None if prec == "fp64" else 5e-5, autotune=True)
     info = b.info()
     assert info["autotuned"] == 1
     assert info["iter_ms_per_column"] >= 0 and info["once_ms_fixed"] >= 0
