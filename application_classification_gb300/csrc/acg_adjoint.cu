@@ -50,6 +50,7 @@ struct AdjWork {
   void *gFd = nullptr, *gRd = nullptr;             // [Dn][Pp]
   void *gbR = nullptr, *gM = nullptr, *gVRe = nullptr, *Mx = nullptr;  // [Dn][Pp]
   int* A = nullptr;                                // [Dn][Pp] argmax positions
+  unsigned long long* emask = nullptr;             // [De] columns each edge is the maximum of
   void *gdEmin = nullptr, *gB = nullptr;           // [Dn][Pp]
   void* gCV = nullptr;                             // [Dn][Pn]
   void* gdE = nullptr;                             // [De][Pp]
@@ -82,7 +83,18 @@ namespace {
 
 constexpr int kT = 256;
 constexpr int kW = kT / 32;
-constexpr int kU = 4;
+#ifndef ACG_ADJ_KU
+#define ACG_ADJ_KU 4
+#endif
+#ifndef ACG_ADJ_MINB
+#define ACG_ADJ_MINB 0
+#endif
+constexpr int kU = ACG_ADJ_KU;  // gather steps in flight (edge-max argmax, max-gradient scatter)
+#if ACG_ADJ_MINB > 0
+#define ACG_ADJ_BOUNDS __launch_bounds__(kT, ACG_ADJ_MINB)
+#else
+#define ACG_ADJ_BOUNDS __launch_bounds__(kT)
+#endif
 
 template <typename T>
 struct AV;
@@ -233,7 +245,7 @@ struct ArgArgs {
 };
 
 template <typename T, int NPOW, int NQV>
-__global__ void __launch_bounds__(kT) adj_argmax_kernel(const ArgArgs<T> a) {
+__global__ void ACG_ADJ_BOUNDS adj_argmax_kernel(const ArgArgs<T> a) {
   using VT = typename AV<T>::type;
   constexpr int W = AV<T>::W, S = 32 / NPOW, NQ = NQV * W;
   const int Pp = a.Pp, lane = threadIdx.x & 31, slot = lane / NPOW, qc = lane % NPOW;
@@ -340,36 +352,25 @@ __global__ void adj_argmax_combine_kernel(const T* __restrict__ pval, const int*
 
 // --------------------------------------------- gradient through the maxima
 // For each source s (source CSR): gVRe[s][q] = sum over its out-edges e whose
-// destination v has A[v][q] == e of gM[v][q].  (The matching gdE[e][q] -=
-// gM[v][q] is made by step A, which holds gM[v][q] and reads A[v][q].)
+// destination v has its maximum at column q on e (A[v][q] == e) of gM[v][q].
+// Step A, which holds gM[v][q] and reads A[v][q], makes the matching
+// gdE[e][q] -= gM[v][q] and sets bit q of emask[e] (an OR: the same in any
+// order), so this pass reads 8 bytes per out-edge.
 template <typename T>
 struct ScatArgs {
   const int4* items;
   const int* wsplit;
   const int* row_of;   // dst-CSR position of each src-CSR position
   const int* dst_of;   // destination vertex of each src-CSR position
-  const int* A;
+  const unsigned long long* emask;  // [De] bit q: edge (dst-CSR position) is the maximum at column q
   const T* gM;
   T* gVRe;
   T* part;
   int Pp, Pe;
 };
 
-// A is read with the same 16-byte-per-lane column split as the values
-template <typename T>
-struct IV;
-template <>
-struct IV<double> {
-  using type = int2;
-};
-template <>
-struct IV<float> {
-  using type = int4;
-};
-
 template <typename T, int NPOW, int NQV>
-__global__ void __launch_bounds__(kT) adj_scatter_kernel(const ScatArgs<T> a) {
-  using IVT = typename IV<T>::type;
+__global__ void ACG_ADJ_BOUNDS adj_scatter_kernel(const ScatArgs<T> a) {
   constexpr int W = AV<T>::W, S = 32 / NPOW, NQ = NQV * W;
   const int Pp = a.Pp, Pe = a.Pe, lane = threadIdx.x & 31, slot = lane / NPOW, qc = lane % NPOW;
   const int gw = (blockIdx.x * kT + threadIdx.x) >> 5;
@@ -387,25 +388,18 @@ __global__ void __launch_bounds__(kT) adj_scatter_kernel(const ScatArgs<T> a) {
         e[u] = ok ? __ldg(a.row_of + j) : -1;
         vd[u] = ok ? __ldg(a.dst_of + j) : 0;
       }
-      IVT av[kU][NQV];
+      unsigned long long mk[kU];
 #pragma unroll
-      for (int u = 0; u < kU; ++u)
-#pragma unroll
-        for (int k = 0; k < NQV; ++k) {
-          const int qv = qc + NPOW * k;
-          if (e[u] >= 0 && qv * W < Pe)
-            av[u][k] = __ldg(reinterpret_cast<const IVT*>(a.A + (size_t)vd[u] * Pp) + qv);
-        }
+      for (int u = 0; u < kU; ++u) mk[u] = e[u] >= 0 ? __ldg(a.emask + e[u]) : 0ull;
 #pragma unroll
       for (int u = 0; u < kU; ++u) {
-        if (e[u] < 0) continue;
+        if (mk[u] == 0ull) continue;
 #pragma unroll
         for (int k = 0; k < NQV; ++k) {
-          if ((qc + NPOW * k) * W >= Pe) continue;
 #pragma unroll
           for (int w = 0; w < W; ++w) {
             const int q = (qc + NPOW * k) * W + w;
-            if (q < Pe && reinterpret_cast<const int*>(&av[u][k])[w] == e[u])
+            if (q < Pe && ((mk[u] >> q) & 1ull))
               acc[k * W + w] += a.gM[(size_t)vd[u] * Pp + q];
           }
         }
@@ -462,6 +456,7 @@ struct StepAArgs {
   const T* M;         // [Dn][Pp] edge maxima of state t-1
   const int* A;       // [Dn][Pp] their first maximal destination-CSR positions
   T* gdE;             // accumulated [De][Pp]
+  unsigned long long* emask;  // [De] out: the columns each edge is the maximum of (nonzero gradient)
   const T* dEmin;
   const double* glob; // statistics of state t-1
   const int* pat;
@@ -544,7 +539,11 @@ __global__ void __launch_bounds__(kT) adj_stepA_kernel(const StepAArgs<T> a) {
       a.gbR[i] = gb;
       a.gM[i] = gm;
       // the maximum's -dE term: each (edge, column) is the maximum of one vertex
-      if (gm != T(0)) a.gdE[(size_t)__ldg(a.A + i) * Pp + q] -= gm;
+      if (gm != T(0)) {
+        const int e = __ldg(a.A + i);
+        a.gdE[(size_t)e * Pp + q] -= gm;
+        atomicOr(a.emask + e, 1ull << q);
+      }
       a.gdEmin[i] -= gb;
       sa[k][0] += sR ? 0.0 : (double)gR;
       sa[k][1] += sF ? 0.0 : (double)gF;
@@ -1352,7 +1351,7 @@ struct Adj {
   }
 
   acg_status scatter() {
-    ScatArgs<T> a{P->sw.items, P->sw.wsplit, D->pos_in_dst, D->scsr.other, W->A, (const T*)W->gM,
+    ScatArgs<T> a{P->sw.items, P->sw.wsplit, D->pos_in_dst, D->scsr.other, W->emask, (const T*)W->gM,
                   (T*)W->gVRe, (T*)W->pscat, Pp, Pe};
     ACG_TRY(fill(W->gVRe, vrow(), T(0)));  // sources without out-edges
     bool done = false;
@@ -1381,8 +1380,9 @@ struct Adj {
     const double* g;
     state(t - 1, t0, &f, &r, &mh, &ml, &g);
     if (Pe > 0) ACG_TRY(argmax(r));
+    if (De > 0) ACG_CUDA_TRY(cudaMemsetAsync(W->emask, 0, sizeof(unsigned long long) * (size_t)De, s));
     StepAArgs<T> sa{(const T*)W->gMU, first ? nullptr : (const T*)W->gFd,
-                    first ? nullptr : (const T*)W->gRd, f, r, (const T*)W->Mx, W->A, (T*)W->gdE, (const T*)P->dEmin, g,
+                    first ? nullptr : (const T*)W->gRd, f, r, (const T*)W->Mx, W->A, (T*)W->gdE, W->emask, (const T*)P->dEmin, g,
                     P->pat, (T*)W->gbR, (T*)W->gM, (T*)W->gdEmin, (T*)W->gCV, W->part,
                     W->part + (size_t)4 * Pe * vblocks, W->parti, Dn, Pn, Pe, Pp};
     const size_t smA = sizeof(T) * kW * 64 * 2 + sizeof(double) * kW * 6 * std::max(1, Pe) +
@@ -1701,6 +1701,7 @@ acg_status adj_alloc(acg_plan* P, int every, cudaStream_t s) {
   for (void** b : {&W->gFd, &W->gRd, &W->gbR, &W->gM, &W->gVRe, &W->Mx, &W->gdEmin, &W->gB})
     ACG_TRY(adj_buf(W, vrow, b, s));
   ACG_TRY(adj_buf(W, Dn * Pp * sizeof(int), (void**)&W->A, s));
+  ACG_TRY(adj_buf(W, De * sizeof(unsigned long long), (void**)&W->emask, s));
   ACG_TRY(adj_buf(W, De * Pp * eb, &W->gdE, s));
   ACG_TRY(adj_buf(W, Dn * Pqc * eb, &W->gRb, s));
   ACG_TRY(adj_buf(W, Dn * Pqc * eb, &W->gFb, s));

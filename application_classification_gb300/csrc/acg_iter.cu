@@ -559,7 +559,10 @@ vertex_update_kernel(const VertexUpdArgs<T> a) {
 // indices (in-edges of p ascending, then out-edges ascending -- the order of
 // the tile form); the new Y, Z from MU_raw[dst_q], MU_raw[src_q].  Vertices
 // without in-edges have M rows of -inf (set once, never written by phase A).
-constexpr int kVps = 4;  // vertices per stage
+#ifndef ACG_VTX_VPS
+#define ACG_VTX_VPS 4
+#endif
+constexpr int kVps = ACG_VTX_VPS;  // vertices per stage
 constexpr int kVw = kBT / 32;
 
 template <typename T, int QPL, int PPL>
@@ -616,8 +619,13 @@ __device__ __forceinline__ void st_n(T* p, const T (&x)[N]) {
   }
 }
 
+// Two blocks per SM bounds the registers at 128 (RMAT-22 vertex phase 1.76 ms;
+// no bound: 1.90 ms; one block: 2.65 ms)
+#ifndef ACG_VTX_MINB
+#define ACG_VTX_MINB 2
+#endif
 template <typename T, int QPL, int PPL>
-__global__ void __launch_bounds__(kBT)
+__global__ void __launch_bounds__(kBT, ACG_VTX_MINB)
 vertex_warp_kernel(const VertexUpdArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int Pe = a.Pe, Pn = a.Pn, Pp = a.Pp, Pnp = a.Pnp, Dn = a.Dn, maxdeg = a.maxdeg;
