@@ -48,8 +48,10 @@ struct AdjWork {
   // work buffers (element type per precision)
   void *gMU = nullptr, *gMU2 = nullptr;            // [Dn][Pn]
   void *gFd = nullptr, *gRd = nullptr;             // [Dn][Pp]
-  void *gbR = nullptr, *gM = nullptr, *gVRe = nullptr, *Mx = nullptr;  // [Dn][Pp]
-  int* A = nullptr;                                // [Dn][Pp] argmax positions
+  void *gbR = nullptr, *gM = nullptr, *gVRe = nullptr;  // [Dn][Pp]
+  std::vector<void*> sm;                           // segment slots: edge maxima of states t0 ..
+  std::vector<int*> sa;                            //   and their argmax positions ([Dn][Pp])
+  int seg_t0 = 0;                                  // first state of the segment being processed
   unsigned long long* emask = nullptr;             // [De] columns each edge is the maximum of
   void *gdEmin = nullptr, *gB = nullptr;           // [Dn][Pp]
   void* gCV = nullptr;                             // [Dn][Pn]
@@ -225,129 +227,6 @@ template <typename T>
 __global__ void fill_t_kernel(T* __restrict__ p, size_t n, T v) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     p[i] = v;
-}
-
-// ------------------------------------------------------- edge-phase argmax
-// M[v][q] = max over in-edges of Z[s_e][q] - dE[e][q] (as the edge phase
-// computes it) and A[v][q] = its first maximal destination-CSR position.
-template <typename T>
-struct ArgArgs {
-  const int4* items;
-  const int* wsplit;
-  const int* src_of;
-  const T* dE;
-  const T* Z;
-  T* M;
-  int* A;
-  T* pval;
-  int* ppos;
-  int Pp;
-};
-
-template <typename T, int NPOW, int NQV>
-__global__ void ACG_ADJ_BOUNDS adj_argmax_kernel(const ArgArgs<T> a) {
-  using VT = typename AV<T>::type;
-  constexpr int W = AV<T>::W, S = 32 / NPOW, NQ = NQV * W;
-  const int Pp = a.Pp, lane = threadIdx.x & 31, slot = lane / NPOW, qc = lane % NPOW;
-  const int gw = (blockIdx.x * kT + threadIdx.x) >> 5;
-  for (int it = a.wsplit[gw]; it < a.wsplit[gw + 1]; ++it) {
-    const int4 item = a.items[it];
-    T best[NQ];
-    int pos[NQ];
-#pragma unroll
-    for (int k = 0; k < NQ; ++k) {
-      best[k] = neg_inf<T>();
-      pos[k] = -1;
-    }
-    // kU edges per lane in flight: their source rows, then both loads, then
-    // the comparisons in increasing position (the first maximum is kept)
-    for (int base = item.y; base < item.z; base += S * kU) {
-      int src[kU];
-#pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        const int e = base + slot + S * u;
-        src[u] = e < item.z ? __ldg(a.src_of + e) : -1;
-      }
-      VT z[kU][NQV], d[kU][NQV];
-#pragma unroll
-      for (int u = 0; u < kU; ++u)
-#pragma unroll
-        for (int k = 0; k < NQV; ++k) {
-          const int qv = qc + NPOW * k;
-          if (src[u] >= 0 && qv * W < Pp) {
-            z[u][k] = __ldg(reinterpret_cast<const VT*>(a.Z + (size_t)src[u] * Pp) + qv);
-            d[u][k] = __ldg(reinterpret_cast<const VT*>(a.dE + (size_t)(base + slot + S * u) * Pp) + qv);
-          }
-        }
-#pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        if (src[u] < 0) continue;
-        const int e = base + slot + S * u;
-#pragma unroll
-        for (int k = 0; k < NQV; ++k) {
-          if ((qc + NPOW * k) * W >= Pp) continue;
-#pragma unroll
-          for (int w = 0; w < W; ++w) {
-            const T v = ag<T>(z[u][k], w) - ag<T>(d[u][k], w);
-            if (pos[k * W + w] < 0 || v > best[k * W + w]) {
-              best[k * W + w] = v;
-              pos[k * W + w] = e;
-            }
-          }
-        }
-      }
-    }
-#pragma unroll
-    for (int o = NPOW; o < 32; o <<= 1)
-#pragma unroll
-      for (int k = 0; k < NQ; ++k) {
-        const T ob = __shfl_xor_sync(0xffffffffu, best[k], o);
-        const int op = __shfl_xor_sync(0xffffffffu, pos[k], o);
-        if (op >= 0 && (pos[k] < 0 || ob > best[k] || (ob == best[k] && op < pos[k]))) {
-          best[k] = ob;
-          pos[k] = op;
-        }
-      }
-    if (slot == 0) {
-      T* mrow = item.w >= 0 ? a.pval + (size_t)item.w * Pp : a.M + (size_t)item.x * Pp;
-      int* arow = item.w >= 0 ? a.ppos + (size_t)item.w * Pp : a.A + (size_t)item.x * Pp;
-#pragma unroll
-      for (int k = 0; k < NQV; ++k)
-#pragma unroll
-        for (int w = 0; w < W; ++w) {
-          const int q = (qc + NPOW * k) * W + w;
-          if (q < Pp) {
-            mrow[q] = best[k * W + w];
-            arow[q] = pos[k * W + w];
-          }
-        }
-    }
-    __syncwarp();
-  }
-}
-
-// One warp per heavy vertex: its chunks in order (earlier chunks hold smaller
-// positions, so a strictly larger value is needed to move the argmax).
-template <typename T>
-__global__ void adj_argmax_combine_kernel(const T* __restrict__ pval, const int* __restrict__ ppos,
-                                          const int* __restrict__ hbase, const int* __restrict__ hcount,
-                                          const int* __restrict__ hvert, int nheavy, int Pp,
-                                          T* __restrict__ M, int* __restrict__ A) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (warp >= nheavy) return;
-  for (int q = lane; q < Pp; q += 32) {
-    T b = neg_inf<T>();
-    int bi = -1;
-    for (int c = 0; c < hcount[warp]; ++c) {
-      const size_t r = (size_t)(hbase[warp] + c) * Pp + q;
-      if (ppos[r] >= 0 && (bi < 0 || pval[r] > b)) {
-        b = pval[r];
-        bi = ppos[r];
-      }
-    }
-    M[(size_t)hvert[warp] * Pp + q] = b;
-    A[(size_t)hvert[warp] * Pp + q] = bi;
-  }
 }
 
 // --------------------------------------------- gradient through the maxima
@@ -1329,27 +1208,6 @@ struct Adj {
     }
   }
 
-  acg_status argmax(const T* Z) {
-    ArgArgs<T> a{P->ew.items, P->ew.wsplit, D->dcsr.other, (const T*)P->dE, Z, (T*)W->Mx, W->A,
-                 (T*)W->pval, W->ppos, Pp};
-    bool done = false;
-#define ADJ_ARG(NP_, NQ_)                                                       \
-    if (!done && P->ws.npow == NP_ && P->ws.nqv == NQ_) {                       \
-      adj_argmax_kernel<T, NP_, NQ_><<<P->edge_blocks, kT, 0, s>>>(a);          \
-      done = true;                                                              \
-    }
-    ADJ_SHAPES(ADJ_ARG)
-#undef ADJ_ARG
-    ACG_LAUNCH_CHECK();
-    if (P->ew.nheavy > 0) {
-      adj_argmax_combine_kernel<T><<<ceil_div(P->ew.nheavy, 8), 256, 0, s>>>(
-          (const T*)W->pval, W->ppos, P->ew.hbase, P->ew.hcount, P->ew.hvert, P->ew.nheavy, Pp,
-          (T*)W->Mx, W->A);
-      ACG_LAUNCH_CHECK();
-    }
-    return ACG_OK;
-  }
-
   acg_status scatter() {
     ScatArgs<T> a{P->sw.items, P->sw.wsplit, D->pos_in_dst, D->scsr.other, W->emask, (const T*)W->gM,
                   (T*)W->gVRe, (T*)W->pscat, Pp, Pe};
@@ -1379,10 +1237,20 @@ struct Adj {
     const T *f, *r, *mh, *ml;
     const double* g;
     state(t - 1, t0, &f, &r, &mh, &ml, &g);
-    if (Pe > 0) ACG_TRY(argmax(r));
+    // the edge maxima of state t - 1 and their argmax, recorded by the edge
+    // phase of iteration t (in the recorded forward or the segment recompute)
+    const T* M;
+    const int* A;
+    if (W->ck.has_am(t - 1)) {
+      M = (const T*)W->ck.m[t - 1];
+      A = W->ck.a[t - 1];
+    } else {
+      M = (const T*)W->sm[t - 1 - t0];
+      A = W->sa[t - 1 - t0];
+    }
     if (De > 0) ACG_CUDA_TRY(cudaMemsetAsync(W->emask, 0, sizeof(unsigned long long) * (size_t)De, s));
     StepAArgs<T> sa{(const T*)W->gMU, first ? nullptr : (const T*)W->gFd,
-                    first ? nullptr : (const T*)W->gRd, f, r, (const T*)W->Mx, W->A, (T*)W->gdE, W->emask, (const T*)P->dEmin, g,
+                    first ? nullptr : (const T*)W->gRd, f, r, M, A, (T*)W->gdE, W->emask, (const T*)P->dEmin, g,
                     P->pat, (T*)W->gbR, (T*)W->gM, (T*)W->gdEmin, (T*)W->gCV, W->part,
                     W->part + (size_t)4 * Pe * vblocks, W->parti, Dn, Pn, Pe, Pp};
     const size_t smA = sizeof(T) * kW * 64 * 2 + sizeof(double) * kW * 6 * std::max(1, Pe) +
@@ -1432,7 +1300,6 @@ struct Adj {
     ACG_TRY(fill(W->gB, vrow(), T(0)));
     ACG_TRY(fill(W->gCV, prow(), T(0)));
     ACG_TRY(fill(W->gdE, (size_t)De * Pp, T(0)));
-    ACG_TRY(fill(W->Mx, vrow(), neg_inf_h()));  // vertices without in-edges
     // the gradient into MU(T): mu = MU(T) - S(T)
     ACG_TRY(col_sums(gmu, Pn, Pn, Dn, 0));
     {
@@ -1454,6 +1321,7 @@ struct Adj {
       const int t0 = W->ck_t[c], t1 = W->ck_t[c + 1];
       if (t1 - t0 > 1) {  // recompute the states strictly between the checkpoints
         seg.resize(T_ + 1);
+        seg.ppos = W->ppos;
         for (int t = t0 + 1; t < t1; ++t) {
           const int i = t - t0 - 1;
           seg.f[t] = W->sf[i];
@@ -1461,6 +1329,8 @@ struct Adj {
           seg.mh[t] = W->smh[i];
           seg.ml[t] = W->sml[i];
           seg.glob[t] = W->sglob[i];
+          seg.m[t - 1] = W->sm[i];  // state t - 1 (t0 .. t1 - 2) from iteration t's edge phase
+          seg.a[t - 1] = W->sa[i];
         }
         ACG_TRY(restore(t0));
         P->rec = &seg;
@@ -1672,7 +1542,12 @@ acg_status adj_alloc(acg_plan* P, int every, cudaStream_t s) {
   const size_t Pqc = std::max(1, P->Pqc);
   const size_t vrow = Dn * Pp * eb, prow = Dn * Pn * eb, gb = sizeof(double) * glob_doubles(P->Pn, P->Pe);
   W->ck.resize(T_ + 1);
+  W->ck.ppos = nullptr;  // set below (W->ppos)
   for (int t : W->ck_t) {
+    if (t >= 1) {  // the edge maxima of state t - 1, from iteration t of the recorded match
+      ACG_TRY(adj_buf(W, vrow, &W->ck.m[t - 1], s));
+      ACG_TRY(adj_buf(W, Dn * Pp * sizeof(int), (void**)&W->ck.a[t - 1], s));
+    }
     if (t < T_ || t == 0) {  // the last state needs only MU_raw and its statistics
       ACG_TRY(adj_buf(W, vrow, &W->ck.f[t], s));
       ACG_TRY(adj_buf(W, vrow, &W->ck.r[t], s));
@@ -1687,7 +1562,11 @@ acg_status adj_alloc(acg_plan* P, int every, cudaStream_t s) {
   W->smh.assign(nslot, nullptr);
   W->sml.assign(nslot, nullptr);
   W->sglob.assign(nslot, nullptr);
+  W->sm.assign(nslot, nullptr);
+  W->sa.assign(nslot, nullptr);
   for (int i = 0; i < nslot; ++i) {
+    ACG_TRY(adj_buf(W, vrow, &W->sm[i], s));
+    ACG_TRY(adj_buf(W, Dn * Pp * sizeof(int), (void**)&W->sa[i], s));
     ACG_TRY(adj_buf(W, vrow, &W->sf[i], s));
     ACG_TRY(adj_buf(W, vrow, &W->sr[i], s));
     ACG_TRY(adj_buf(W, prow, &W->smh[i], s));
@@ -1698,9 +1577,8 @@ acg_status adj_alloc(acg_plan* P, int every, cudaStream_t s) {
   W->vblocks = nsm * 2;
   const size_t vb = W->vblocks;
   for (void** b : {&W->gMU, &W->gMU2, &W->gCV}) ACG_TRY(adj_buf(W, prow, b, s));
-  for (void** b : {&W->gFd, &W->gRd, &W->gbR, &W->gM, &W->gVRe, &W->Mx, &W->gdEmin, &W->gB})
+  for (void** b : {&W->gFd, &W->gRd, &W->gbR, &W->gM, &W->gVRe, &W->gdEmin, &W->gB})
     ACG_TRY(adj_buf(W, vrow, b, s));
-  ACG_TRY(adj_buf(W, Dn * Pp * sizeof(int), (void**)&W->A, s));
   ACG_TRY(adj_buf(W, De * sizeof(unsigned long long), (void**)&W->emask, s));
   ACG_TRY(adj_buf(W, De * Pp * eb, &W->gdE, s));
   ACG_TRY(adj_buf(W, Dn * Pqc * eb, &W->gRb, s));
@@ -1708,6 +1586,7 @@ acg_status adj_alloc(acg_plan* P, int every, cudaStream_t s) {
   const size_t enp = P->ew.npartial, snp = P->sw.npartial;
   ACG_TRY(adj_buf(W, enp * Pp * eb, &W->pval, s));
   ACG_TRY(adj_buf(W, enp * Pp * sizeof(int), (void**)&W->ppos, s));
+  W->ck.ppos = W->ppos;
   ACG_TRY(adj_buf(W, snp * Pp * eb, &W->pscat, s));
   ACG_TRY(adj_buf(W, snp * 2 * Pp * eb, &W->pstat, s));
   ACG_TRY(adj_buf(W, snp * 3 * Pp * sizeof(int), (void**)&W->pstati, s));

@@ -222,9 +222,22 @@ acg_status iterate(acg_plan* P, int t, double* mu_out, cudaStream_t s) {
     EdgeMaxArgs<T> ea{P->ew.items, P->ew.nitems, P->ew.wsplit, D->dcsr.other,
                       (const T*)P->dE, (const T*)P->vr[(t - 1) & 1], (T*)P->M,
                       (T*)P->part_iter, Pp};
+    const bool am = P->rec && P->rec->has_am(t - 1);  // record M and its argmax of state t - 1
+    if (am) {
+      ea.argpos = P->rec->a[t - 1];
+      ea.ppos = P->rec->ppos;
+    }
     ACG_TRY(launch_edge_max<T>(ea, P->ws, P->edge_blocks, s));
-    ACG_TRY(launch_heavy_combine<T>((const T*)P->part_iter, P->ew.hbase, P->ew.hcount,
-                                    P->ew.hvert, P->ew.nheavy, Pp, (T*)P->M, s));
+    if (am) {
+      ACG_TRY(launch_heavy_combine_arg<T>((const T*)P->part_iter, P->rec->ppos, P->ew.hbase,
+                                          P->ew.hcount, P->ew.hvert, P->ew.nheavy, Pp, (T*)P->M,
+                                          P->rec->a[t - 1], s));
+      ACG_CUDA_TRY(cudaMemcpyAsync(P->rec->m[t - 1], P->M, sizeof(T) * (size_t)Dn * Pp,
+                                   cudaMemcpyDeviceToDevice, s));
+    } else {
+      ACG_TRY(launch_heavy_combine<T>((const T*)P->part_iter, P->ew.hbase, P->ew.hcount,
+                                      P->ew.hvert, P->ew.nheavy, Pp, (T*)P->M, s));
+    }
     P->launches += 1 + (P->ew.nheavy > 0);
   }
   if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1) + 1], s);

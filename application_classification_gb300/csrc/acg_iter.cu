@@ -78,7 +78,9 @@ __host__ __device__ inline size_t a16(size_t b) { return (b + 15) & ~size_t(15);
 #ifndef ACG_EDGE_MINB
 #define ACG_EDGE_MINB 1
 #endif
-template <typename T, int NPOW, int NQV>
+// ARG: also the first maximal dst-CSR position of each maximum (adjoint
+// recording): ties go to the smaller position.
+template <typename T, int NPOW, int NQV, bool ARG>
 __global__ void __launch_bounds__(kAT, ACG_EDGE_MINB)
 edge_max_kernel(const EdgeMaxArgs<T> a) {
   using VT = typename VecT<T>::type;
@@ -107,8 +109,13 @@ edge_max_kernel(const EdgeMaxArgs<T> a) {
     sidx[u] = e < item.z ? __ldg(a.src_of + e) : 0;
   }
   T acc[NQ];
+  int pos[ARG ? NQ : 1];
 #pragma unroll
   for (int k = 0; k < NQ; ++k) acc[k] = neg_inf<T>();
+  if constexpr (ARG) {
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) pos[k] = -1;
+  }
   for (;;) {
     // rows of this step
     VT x[kU][NQV], y[kU][NQV];
@@ -143,17 +150,48 @@ edge_max_kernel(const EdgeMaxArgs<T> a) {
       sidx[u] = (more && e < nend) ? __ldg(a.src_of + e) : 0;
     }
 #pragma unroll
-    for (int u = 0; u < kU; ++u)
+    for (int u = 0; u < kU; ++u) {
+      if constexpr (ARG) {
+        const int e = base + slot + S * u;
+        if (e < item.z) {
 #pragma unroll
-      for (int k = 0; k < NQV; ++k)
+          for (int k = 0; k < NQV; ++k)
 #pragma unroll
-        for (int w = 0; w < W; ++w)
-          acc[k * W + w] = fmax(acc[k * W + w], vg<T>(x[u][k], w) - vg<T>(y[u][k], w));
+            for (int w = 0; w < W; ++w) {
+              const T v = vg<T>(x[u][k], w) - vg<T>(y[u][k], w);
+              if (pos[k * W + w] < 0 || v > acc[k * W + w]) {
+                acc[k * W + w] = v;
+                pos[k * W + w] = e;
+              }
+            }
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < NQV; ++k)
+#pragma unroll
+          for (int w = 0; w < W; ++w)
+            acc[k * W + w] = fmax(acc[k * W + w], vg<T>(x[u][k], w) - vg<T>(y[u][k], w));
+      }
+    }
     if (item_done) {
+      if constexpr (ARG) {
 #pragma unroll
-      for (int o = NPOW; o < 32; o <<= 1)
+        for (int o = NPOW; o < 32; o <<= 1)
 #pragma unroll
-        for (int k = 0; k < NQ; ++k) acc[k] = fmax(acc[k], __shfl_xor_sync(0xffffffffu, acc[k], o));
+          for (int k = 0; k < NQ; ++k) {
+            const T ob = __shfl_xor_sync(0xffffffffu, acc[k], o);
+            const int op = __shfl_xor_sync(0xffffffffu, pos[k], o);
+            if (op >= 0 && (pos[k] < 0 || ob > acc[k] || (ob == acc[k] && op < pos[k]))) {
+              acc[k] = ob;
+              pos[k] = op;
+            }
+          }
+      } else {
+#pragma unroll
+        for (int o = NPOW; o < 32; o <<= 1)
+#pragma unroll
+          for (int k = 0; k < NQ; ++k) acc[k] = fmax(acc[k], __shfl_xor_sync(0xffffffffu, acc[k], o));
+      }
       if (slot == 0) {
         T* row = item.w >= 0 ? a.partial + (size_t)item.w * Pp : a.M + (size_t)item.x * Pp;
 #pragma unroll
@@ -164,11 +202,20 @@ edge_max_kernel(const EdgeMaxArgs<T> a) {
 #pragma unroll
             for (int w = 0; w < W; ++w) vs<T>(o, w, acc[k * W + w]);
             reinterpret_cast<VT*>(row)[qv] = o;
+            if constexpr (ARG) {
+              int* prow = item.w >= 0 ? a.ppos + (size_t)item.w * Pp : a.argpos + (size_t)item.x * Pp;
+#pragma unroll
+              for (int w = 0; w < W; ++w) prow[qv * W + w] = pos[k * W + w];
+            }
           }
         }
       }
 #pragma unroll
       for (int k = 0; k < NQ; ++k) acc[k] = neg_inf<T>();
+      if constexpr (ARG) {
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) pos[k] = -1;
+      }
       if (!more) break;
       ++it;
       item = item_next;
@@ -200,6 +247,32 @@ heavy_combine_kernel(const T* __restrict__ partial, const int* __restrict__ hbas
     }
     for (; r < cnt; ++r) m = fmax(m, p0[(size_t)r * Pp + q]);
     row[q] = m;
+  }
+}
+
+// The same with the chunks' argmax positions (chunks in order: an earlier
+// chunk keeps a tie).
+template <typename T>
+__global__ void __launch_bounds__(256)
+heavy_combine_arg_kernel(const T* __restrict__ partial, const int* __restrict__ ppos,
+                         const int* __restrict__ hbase, const int* __restrict__ hcount,
+                         const int* __restrict__ hvert, int nheavy, int Pp, T* __restrict__ M,
+                         int* __restrict__ A) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= nheavy) return;
+  for (int q = lane; q < Pp; q += 32) {
+    T m = neg_inf<T>();
+    int bi = -1;
+    for (int c = 0; c < hcount[warp]; ++c) {
+      const size_t r = (size_t)(hbase[warp] + c) * Pp + q;
+      if (ppos[r] >= 0 && (bi < 0 || partial[r] > m)) {
+        m = partial[r];
+        bi = ppos[r];
+      }
+    }
+    M[(size_t)hvert[warp] * Pp + q] = m;
+    A[(size_t)hvert[warp] * Pp + q] = bi;
   }
 }
 
@@ -939,7 +1012,10 @@ WarpShape choose_warp_shape(int elem_bytes, int pp) {
 
 #define ACG_EDGE_LAUNCH(NP_, NQ_)                                           \
   if (ws.npow == NP_ && ws.nqv == NQ_) {                                    \
-    edge_max_kernel<T, NP_, NQ_><<<blocks, kAT, 0, s>>>(a);                 \
+    if (a.argpos)                                                           \
+      edge_max_kernel<T, NP_, NQ_, true><<<blocks, kAT, 0, s>>>(a);         \
+    else                                                                    \
+      edge_max_kernel<T, NP_, NQ_, false><<<blocks, kAT, 0, s>>>(a);        \
     ACG_LAUNCH_CHECK();                                                     \
     return ACG_OK;                                                          \
   }
@@ -953,7 +1029,7 @@ acg_status launch_edge_max(const EdgeMaxArgs<T>& a, WarpShape ws, int blocks, cu
 
 #define ACG_EDGE_OCC(NP_, NQ_)                                                        \
   if (ws.npow == NP_ && ws.nqv == NQ_) {                                             \
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, edge_max_kernel<T, NP_, NQ_>, \
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, edge_max_kernel<T, NP_, NQ_, false>, \
                                                       kAT, 0) != cudaSuccess)        \
       nb = 1;                                                                        \
   }
@@ -963,6 +1039,17 @@ int edge_max_blocks_per_sm(WarpShape ws) {
   int nb = 1;
   ACG_EDGE_SHAPES(ACG_EDGE_OCC)
   return nb < 1 ? 1 : nb;
+}
+
+template <typename T>
+acg_status launch_heavy_combine_arg(const T* partial, const int* ppos, const int* hbase,
+                                    const int* hcount, const int* hvert, int nheavy, int Pp, T* M,
+                                    int* A, cudaStream_t s) {
+  if (nheavy == 0) return ACG_OK;
+  heavy_combine_arg_kernel<T><<<ceil_div(nheavy, 8), 256, 0, s>>>(partial, ppos, hbase, hcount, hvert,
+                                                                   nheavy, Pp, M, A);
+  ACG_LAUNCH_CHECK();
+  return ACG_OK;
 }
 
 template <typename T>
@@ -1073,6 +1160,8 @@ template acg_status launch_edge_max<double>(const EdgeMaxArgs<double>&, WarpShap
 template acg_status launch_edge_max<float>(const EdgeMaxArgs<float>&, WarpShape, int, cudaStream_t);
 template acg_status launch_heavy_combine<double>(const double*, const int*, const int*, const int*, int, int, double*, cudaStream_t);
 template acg_status launch_heavy_combine<float>(const float*, const int*, const int*, const int*, int, int, float*, cudaStream_t);
+template acg_status launch_heavy_combine_arg<double>(const double*, const int*, const int*, const int*, const int*, int, int, double*, int*, cudaStream_t);
+template acg_status launch_heavy_combine_arg<float>(const float*, const int*, const int*, const int*, const int*, int, int, float*, int*, cudaStream_t);
 template acg_status launch_vertex_update<double>(const VertexUpdArgs<double>&, int, cudaStream_t);
 template acg_status launch_vertex_update<float>(const VertexUpdArgs<float>&, int, cudaStream_t);
 template int edge_max_blocks_per_sm<double>(WarpShape);

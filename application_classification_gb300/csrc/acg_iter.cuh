@@ -21,6 +21,10 @@ struct EdgeMaxArgs {
   T* M;                // [Dn][Pp] out: max over in-edges of VR' - dE
   T* partial;          // [npartial][Pp]
   int Pp;
+  // Recording for the adjoint (null otherwise): the first maximal dst-CSR
+  // position of each maximum ([Dn][Pp]; ppos: [npartial][Pp] for the chunks)
+  int* argpos = nullptr;
+  int* ppos = nullptr;
 };
 
 // Column statistics of one iteration (FP64), double-buffered across iterations:
@@ -79,6 +83,11 @@ acg_status launch_edge_max(const EdgeMaxArgs<T>& a, WarpShape ws, int blocks, cu
 template <typename T>
 acg_status launch_heavy_combine(const T* partial, const int* hbase, const int* hcount,
                                 const int* hvert, int nheavy, int Pp, T* M, cudaStream_t s);
+// The same with the argmax positions of the chunks (earlier chunks win ties).
+template <typename T>
+acg_status launch_heavy_combine_arg(const T* partial, const int* ppos, const int* hbase,
+                                    const int* hcount, const int* hvert, int nheavy, int Pp, T* M,
+                                    int* A, cudaStream_t s);
 template <typename T>
 acg_status launch_vertex_update(const VertexUpdArgs<T>& a, int blocks, cudaStream_t s);
 template <typename T>

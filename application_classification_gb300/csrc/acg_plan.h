@@ -46,17 +46,25 @@ namespace acg {
 // t = after iteration t): f = VF' - cR and r = VR' - cF ([Dn][Pp]), MU_raw as
 // hi + lo ([Dn][Pn]) and the iteration's statistics ([glob_doubles]); null
 // where state t is not recorded.
+// Also, per state s, the edge maxima M of state s ([Dn][Pp]) and their first
+// maximal dst-CSR positions (the edge phase of iteration s + 1), where a[s]
+// is set; ppos: scratch for the hub chunks' positions.
 struct StateRec {
-  std::vector<void*> f, r, mh, ml;
+  std::vector<void*> f, r, mh, ml, m;
+  std::vector<int*> a;
   std::vector<double*> glob;
+  int* ppos = nullptr;
   void resize(int n) {
     f.assign(n, nullptr);
     r.assign(n, nullptr);
     mh.assign(n, nullptr);
     ml.assign(n, nullptr);
+    m.assign(n, nullptr);
+    a.assign(n, nullptr);
     glob.assign(n, nullptr);
   }
   bool has(int t) const { return t >= 0 && t < (int)f.size() && mh[t] != nullptr; }
+  bool has_am(int s) const { return s >= 0 && s < (int)a.size() && a[s] != nullptr; }
 };
 struct AdjWork;  // the adjoint's checkpoints and work buffers (acg_adjoint.cu)
 }  // namespace acg
