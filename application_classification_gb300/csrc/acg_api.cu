@@ -132,8 +132,178 @@ acg_status check_graph(const acg_graph* g, const char* what, bool need_feats) {
 
 }  // namespace
 
+namespace {
+
+constexpr int kWorkOver = 3;  // per-item cost in load steps (item load, combine, store)
+
+// Per vertex: its cost in load steps (0 without edges), summed into *total.
+__global__ void work_cost_kernel(const int* __restrict__ off, int n, int step,
+                                 unsigned long long* __restrict__ total) {
+  __shared__ unsigned long long red[8];
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long c = 0;
+  if (v < n) {
+    const int deg = off[v + 1] - off[v];
+    if (deg > 0) c = (unsigned long long)((deg + step - 1) / step + kWorkOver);
+  }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    atomicAdd(total, t);  // integer: the same in any order
+  }
+}
+
+// Per vertex: its item count, partial-row count and hub flag for a chunk size.
+__global__ void work_count_kernel(const int* __restrict__ off, int n, int chunk,
+                                  uint32_t* __restrict__ nit, uint32_t* __restrict__ npart,
+                                  uint32_t* __restrict__ hub) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  const int deg = off[v + 1] - off[v];
+  const uint32_t k = deg > chunk ? (uint32_t)((deg + chunk - 1) / chunk) : (deg > 0 ? 1u : 0u);
+  nit[v] = k;
+  npart[v] = deg > chunk ? k : 0u;
+  hub[v] = deg > chunk ? 1u : 0u;
+}
+
+// Per vertex: its items (in order) with their costs, and its hub record.
+__global__ void work_items_kernel(const int* __restrict__ off, int n, int chunk, int step,
+                                  const uint32_t* __restrict__ ioff, const uint32_t* __restrict__ poff,
+                                  const uint32_t* __restrict__ hoff, int4* __restrict__ items,
+                                  uint32_t* __restrict__ cost, int* __restrict__ hbase,
+                                  int* __restrict__ hcount, int* __restrict__ hvert) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  const int b = off[v], e = off[v + 1], deg = e - b;
+  if (deg == 0) return;
+  const uint32_t i0 = ioff[v];
+  if (deg > chunk) {
+    const int k = (deg + chunk - 1) / chunk;
+    const int p0 = (int)poff[v], h = (int)hoff[v];
+    hbase[h] = p0;
+    hcount[h] = k;
+    hvert[h] = v;
+    for (int j = 0; j < k; ++j) {
+      const int a = b + j * chunk, z = min(e, a + chunk);
+      items[i0 + j] = make_int4(v, a, z, p0 + j);
+      cost[i0 + j] = (uint32_t)((z - a + step - 1) / step + kWorkOver);
+    }
+  } else {
+    items[i0] = make_int4(v, b, e, -1);
+    cost[i0] = (uint32_t)((deg + step - 1) / step + kWorkOver);
+  }
+}
+
+// split[w] (0 < w < nwarps) = 1 + the first item whose inclusive cost prefix
+// reaches target * w (nitems if none), target = the items' total cost / nwarps;
+// split[0] = 0, split[nwarps] = nitems.
+__global__ void work_split_kernel(const uint32_t* __restrict__ excl, const uint32_t* __restrict__ cost,
+                                  int nitems, int nwarps, int* __restrict__ split) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w > nwarps) return;
+  if (w == 0) {
+    split[0] = 0;
+    return;
+  }
+  if (w == nwarps) {
+    split[w] = nitems;
+    return;
+  }
+  if (nitems == 0) {
+    split[w] = 0;
+    return;
+  }
+  const double target = ((double)excl[nitems - 1] + (double)cost[nitems - 1]) / nwarps;
+  const double goal = target * w;
+  int lo = 0, hi = nitems;  // first i with excl[i] + cost[i] >= goal
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if ((double)excl[mid] + (double)cost[mid] >= goal) hi = mid;
+    else lo = mid + 1;
+  }
+  split[w] = lo < nitems ? lo + 1 : nitems;
+}
+
+}  // namespace
+
+// The work split, built on the device: per-vertex costs and their total give
+// the chunk size; per-vertex item counts, scanned, place the items (vertex
+// order, chunks in order) and the hub records; a binary search of the scanned
+// item costs gives each warp boundary.  The same items and boundaries as
+// build_warp_work_host, without copying the offsets to the host.
 acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* out,
-                           std::vector<DevBuf>* owned, cudaStream_t s) {
+                                std::vector<DevBuf>* owned, cudaStream_t s) {
+  const int n = c.n;
+  if (n == 0 || nwarps < 1) return build_warp_work_host(c, nwarps, step, out, owned, s);
+  std::vector<DevBuf> tmp;
+  auto fail = [&](acg_status st) {
+    dev_free_all(&tmp);
+    return st;
+  };
+  unsigned long long* total = nullptr;
+  uint32_t *nit = nullptr, *npart = nullptr, *hub = nullptr;
+  acg_status st = dev_alloc(&tmp, sizeof(unsigned long long) + 3 * sizeof(uint32_t), (void**)&total, s);
+  if (st == ACG_OK) st = dev_alloc(&tmp, sizeof(uint32_t) * ((size_t)n + 1), (void**)&nit, s);
+  if (st == ACG_OK) st = dev_alloc(&tmp, sizeof(uint32_t) * ((size_t)n + 1), (void**)&npart, s);
+  if (st == ACG_OK) st = dev_alloc(&tmp, sizeof(uint32_t) * ((size_t)n + 1), (void**)&hub, s);
+  if (st != ACG_OK) return fail(st);
+  work_cost_kernel<<<ceil_div(n, 256), 256, 0, s>>>(c.off, n, step, total);
+  if (cudaGetLastError() != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "work cost launch failed"));
+  unsigned long long htotal = 0;
+  ACG_CUDA_TRY(cudaMemcpyAsync(&htotal, total, sizeof(htotal), cudaMemcpyDeviceToHost, s));
+  ACG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (htotal >= 0x7fffffffull) {  // the 32-bit scans could overflow: build on the host
+    dev_free_all(&tmp);
+    return build_warp_work_host(c, nwarps, step, out, owned, s);
+  }
+  const double per_warp = (double)htotal / std::max(1, nwarps);
+  const long long cs = std::max(4LL, (long long)(per_warp / 4));  // chunk, in steps
+  const int chunk = (int)std::min<long long>(1LL << 24, cs * step);
+  work_count_kernel<<<ceil_div(n, 256), 256, 0, s>>>(c.off, n, chunk, nit, npart, hub);
+  if (cudaGetLastError() != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "work count launch failed"));
+  // counts -> offsets (the n-th entry, zero, becomes the total)
+  ACG_TRY(scan_exclusive_u32(nit, nit, (size_t)n + 1, s));
+  ACG_TRY(scan_exclusive_u32(npart, npart, (size_t)n + 1, s));
+  ACG_TRY(scan_exclusive_u32(hub, hub, (size_t)n + 1, s));
+  uint32_t tot[3] = {0, 0, 0};
+  ACG_CUDA_TRY(cudaMemcpyAsync(&tot[0], nit + n, 4, cudaMemcpyDeviceToHost, s));
+  ACG_CUDA_TRY(cudaMemcpyAsync(&tot[1], npart + n, 4, cudaMemcpyDeviceToHost, s));
+  ACG_CUDA_TRY(cudaMemcpyAsync(&tot[2], hub + n, 4, cudaMemcpyDeviceToHost, s));
+  ACG_CUDA_TRY(cudaStreamSynchronize(s));
+  const int nitems = (int)tot[0], npartial = (int)tot[1], nheavy = (int)tot[2];
+  WarpWork& W = *out;
+  W = WarpWork{};
+  W.nitems = nitems;
+  W.nwarps = nwarps;
+  W.chunk = chunk;
+  W.nheavy = nheavy;
+  W.npartial = npartial;
+  ACG_TRY(dev_alloc(owned, sizeof(int4) * std::max(1, nitems), (void**)&W.items, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * ((size_t)nwarps + 1), (void**)&W.wsplit, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * std::max(1, nheavy), (void**)&W.hbase, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * std::max(1, nheavy), (void**)&W.hcount, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * std::max(1, nheavy), (void**)&W.hvert, s));
+  uint32_t *cost = nullptr, *excl = nullptr;  // per item (more items than vertices with hubs)
+  st = dev_alloc(&tmp, sizeof(uint32_t) * ((size_t)nitems + 1), (void**)&cost, s);
+  if (st == ACG_OK) st = dev_alloc(&tmp, sizeof(uint32_t) * ((size_t)nitems + 1), (void**)&excl, s);
+  if (st != ACG_OK) return fail(st);
+  work_items_kernel<<<ceil_div(n, 256), 256, 0, s>>>(c.off, n, chunk, step, nit, npart, hub, W.items, cost,
+                                                     W.hbase, W.hcount, W.hvert);
+  if (cudaGetLastError() != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "work items launch failed"));
+  // exclusive prefix of the item costs; boundaries
+  ACG_TRY(scan_exclusive_u32(cost, excl, (size_t)nitems, s));
+  work_split_kernel<<<ceil_div(nwarps + 1, 256), 256, 0, s>>>(excl, cost, nitems, nwarps, W.wsplit);
+  if (cudaGetLastError() != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "work split launch failed"));
+  ACG_CUDA_TRY(cudaStreamSynchronize(s));
+  dev_free_all(&tmp);
+  return ACG_OK;
+}
+
+acg_status acg::build_warp_work_host(const Csr& c, int nwarps, int step, WarpWork* out,
+                                     std::vector<DevBuf>* owned, cudaStream_t s) {
   const int n = c.n;
   std::vector<int> off((size_t)n + 1);
   ACG_CUDA_TRY(cudaMemcpyAsync(off.data(), c.off, sizeof(int) * ((size_t)n + 1),
@@ -687,20 +857,18 @@ acg_status acg_data_create(const acg_graph* g, void* stream, acg_data** out) {
   const int m = D->De, n = D->Dn;
   uint32_t *s32 = nullptr, *d32 = nullptr;
   int* bad = nullptr;
+  std::vector<DevBuf> tmp;  // temporaries (zero-filled)
   auto fail = [&](acg_status st) {
-    if (s32) cudaFree(s32);
-    if (d32) cudaFree(d32);
-    if (bad) cudaFree(bad);
+    dev_free_all(&tmp);
     dev_free_all(&D->owned);
     return st;
   };
-  if (cudaMalloc(&s32, sizeof(uint32_t) * (size_t)(m ? m : 1)) != cudaSuccess ||
-      cudaMalloc(&d32, sizeof(uint32_t) * (size_t)(m ? m : 1)) != cudaSuccess ||
-      cudaMalloc(&bad, sizeof(int)) != cudaSuccess) {
-    cudaGetLastError();
-    return fail(set_error(ACG_ERR_OUT_OF_MEMORY, "acg_data_create: temporary allocation failed"));
+  {
+    acg_status at = dev_alloc(&tmp, sizeof(uint32_t) * (size_t)(m ? m : 1), (void**)&s32, s);
+    if (at == ACG_OK) at = dev_alloc(&tmp, sizeof(uint32_t) * (size_t)(m ? m : 1), (void**)&d32, s);
+    if (at == ACG_OK) at = dev_alloc(&tmp, sizeof(int), (void**)&bad, s);
+    if (at != ACG_OK) return fail(at);
   }
-  cudaMemsetAsync(bad, 0, sizeof(int), s);
   if (m > 0) {
     validate_edges_kernel<<<ceil_div(m, 256), 256, 0, s>>>(g->srcs, g->dsts, m, (unsigned long long)n, s32, d32, bad);
     if (cudaGetLastError() != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "validate launch failed"));
@@ -724,9 +892,7 @@ acg_status acg_data_create(const acg_graph* g, void* stream, acg_data** out) {
   if (st == ACG_OK && cudaStreamSynchronize(s) != cudaSuccess)
     st = set_error(ACG_ERR_CUDA, "acg_data_create: %s", cudaGetErrorString(cudaGetLastError()));
   if (st != ACG_OK) return fail(st);
-  cudaFree(s32);
-  cudaFree(d32);
-  cudaFree(bad);
+  dev_free_all(&tmp);
   *out = D.release();
   return ACG_OK;
 }

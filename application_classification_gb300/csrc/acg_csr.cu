@@ -21,10 +21,35 @@
 
 namespace acg {
 
+// The library's memory pool on the current device (stream-ordered, never
+// trimmed: freed blocks stay cached for the next data graph or plan, as a
+// caching allocator does).  Created on first use per device.
+static cudaMemPool_t device_pool() {
+  static cudaMemPool_t pools[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!pools[dev]) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[dev] = pool;
+  }
+  return pools[dev];
+}
+
 acg_status dev_alloc(std::vector<DevBuf>* owned, size_t bytes, void** out, cudaStream_t s) {
   if (bytes == 0) bytes = 16;
   void* p = nullptr;
-  cudaError_t e = cudaMalloc(&p, bytes);
+  cudaMemPool_t pool = device_pool();
+  cudaError_t e = pool ? cudaMallocFromPoolAsync(&p, bytes, pool, s) : cudaMalloc(&p, bytes);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return set_error(ACG_ERR_OUT_OF_MEMORY, "cudaMalloc(%zu) failed: %s", bytes,
@@ -32,7 +57,12 @@ acg_status dev_alloc(std::vector<DevBuf>* owned, size_t bytes, void** out, cudaS
   }
   e = cudaMemsetAsync(p, 0, bytes, s);
   if (e != cudaSuccess) {
-    cudaFree(p);
+    if (pool) {
+      cudaStreamSynchronize(s);
+      cudaFreeAsync(p, s);
+    } else {
+      cudaFree(p);
+    }
     return set_error(ACG_ERR_CUDA, "cudaMemsetAsync failed: %s", cudaGetErrorString(e));
   }
   owned->push_back({p, bytes});
@@ -41,8 +71,13 @@ acg_status dev_alloc(std::vector<DevBuf>* owned, size_t bytes, void** out, cudaS
 }
 
 void dev_free_all(std::vector<DevBuf>* owned) {
+  if (owned->empty()) return;
+  // the buffers may be in use on any stream: wait for the device once, then
+  // hand them back to the pool
+  cudaDeviceSynchronize();
   for (auto& b : *owned)
-    if (b.p) cudaFree(b.p);
+    if (b.p) cudaFreeAsync(b.p, 0);
+  cudaDeviceSynchronize();
   owned->clear();
 }
 

@@ -49,6 +49,9 @@ struct WarpWork {
 // `step` = positions one warp loads per step of its pass (the cost unit).
 acg_status build_warp_work(const Csr& c, int nwarps, int step, WarpWork* out,
                            std::vector<DevBuf>* owned, cudaStream_t s);
+// The same on the host (the fallback when a cost sum would leave 32 bits).
+acg_status build_warp_work_host(const Csr& c, int nwarps, int step, WarpWork* out,
+                                std::vector<DevBuf>* owned, cudaStream_t s);
 
 // ---- primitives (acg_csr.cu)
 // Exclusive scan of n uint32 values (in and out may alias); stream ordered.
