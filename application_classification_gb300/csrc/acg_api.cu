@@ -1024,4 +1024,73 @@ acg_status acg_match_graphs(const acg_graph* data, const acg_graph* pattern,
   return st;
 }
 
+acg_status acg_match_graphs_host(const acg_graph* data, const acg_graph* pattern,
+                                 const acg_options* opt, double* mu_out_host, void* stream) {
+  clear_error();
+  ACG_TRY(check_graph(data, "data", true));
+  ACG_TRY(check_graph(pattern, "pattern", true));
+  if (!mu_out_host && data->num_nodes * pattern->num_nodes > 0)
+    return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_match_graphs_host: mu_out_host is null");
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t ev = nullptr;
+  std::vector<DevBuf> tmp;
+  acg_data* D = nullptr;
+  acg_plan* P = nullptr;
+  acg_status st = ACG_OK;
+  auto cuda_ok = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && st == ACG_OK)
+      st = set_error(ACG_ERR_CUDA, "acg_match_graphs_host: %s: %s", what, cudaGetErrorString(e));
+    return st == ACG_OK;
+  };
+  cuda_ok(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking), "stream");
+  cuda_ok(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+  // device copies of the four arrays of each graph: allocate, then copy the
+  // endpoints (the CSRs need them) on `stream` and the features on the second
+  // stream, which run while the CSRs are built
+  acg_graph dg = *data, pg = *pattern;
+  const size_t m = data->num_edges, n = data->num_nodes;
+  struct Up {
+    const void* h;
+    size_t bytes;
+    bool second;
+    const void** out;
+  };
+  const Up ups[] = {
+      {data->srcs, 8 * m, false, (const void**)&dg.srcs},
+      {data->dsts, 8 * m, false, (const void**)&dg.dsts},
+      {pattern->srcs, 8 * pattern->num_edges, false, (const void**)&pg.srcs},
+      {pattern->dsts, 8 * pattern->num_edges, false, (const void**)&pg.dsts},
+      {pattern->node_feats, 8 * pattern->num_nodes * pattern->node_feat_dim, false, (const void**)&pg.node_feats},
+      {pattern->edge_feats, 8 * pattern->num_edges * pattern->edge_feat_dim, false, (const void**)&pg.edge_feats},
+      {data->node_feats, 8 * n * data->node_feat_dim, true, (const void**)&dg.node_feats},
+      {data->edge_feats, 8 * m * data->edge_feat_dim, true, (const void**)&dg.edge_feats}};
+  void* dptr[8] = {};
+  for (int i = 0; i < 8 && st == ACG_OK; ++i)
+    if (ups[i].h && ups[i].bytes) st = dev_alloc(&tmp, ups[i].bytes, &dptr[i], s);
+  cuda_ok(cudaStreamSynchronize(s), "alloc");  // the allocations exist for both streams
+  for (int i = 0; i < 8 && st == ACG_OK; ++i)
+    if (dptr[i] && cuda_ok(cudaMemcpyAsync(dptr[i], ups[i].h, ups[i].bytes, cudaMemcpyHostToDevice,
+                                           ups[i].second ? s2 : s), "copy"))
+      *ups[i].out = dptr[i];
+  cuda_ok(cudaEventRecord(ev, s2), "event record");
+  double* mu = nullptr;
+  if (st == ACG_OK) st = dev_alloc(&tmp, sizeof(double) * n * pattern->num_nodes, (void**)&mu, s);
+  if (st == ACG_OK) st = acg_data_create(&dg, s, &D);  // reads the endpoints only
+  if (st == ACG_OK) cuda_ok(cudaStreamWaitEvent(s, ev, 0), "wait");
+  if (st == ACG_OK) st = acg_plan_create(D, &pg, opt, s, &P);
+  if (st == ACG_OK) st = acg_match(P, mu, s);
+  if (st == ACG_OK && n * pattern->num_nodes > 0)
+    cuda_ok(cudaMemcpyAsync(mu_out_host, mu, sizeof(double) * n * pattern->num_nodes,
+                            cudaMemcpyDeviceToHost, s), "copy back");
+  if (st == ACG_OK) cuda_ok(cudaStreamSynchronize(s), "synchronise");
+  if (s2) cudaStreamSynchronize(s2);
+  acg_plan_destroy(P);
+  acg_data_destroy(D);
+  dev_free_all(&tmp);
+  if (ev) cudaEventDestroy(ev);
+  if (s2) cudaStreamDestroy(s2);
+  return st;
+}
+
 }  // extern "C"

@@ -207,6 +207,27 @@ def match(data: Graph, pattern: Graph, precision: str = "fp64", num_iters: int =
     return out.cpu().numpy()
 
 
+def match_host(data: Graph, pattern: Graph, precision: str = "fp64", num_iters: int = -1,
+               cnull: bool = False, out: np.ndarray | None = None) -> np.ndarray:
+    """One-shot match from host memory through ``acg_match_graphs_host``: the
+    arrays of ``data`` and ``pattern`` (numpy, or pinned torch tensors wrapped
+    in a :class:`Graph`-like object) are copied by the library, mu comes back in
+    ``out`` (a [Dn][Pn] float64 host array, allocated if None)."""
+    _torch()
+    opt = _lib.Options()
+    _lib.lib().acg_options_default(C.byref(opt))
+    opt.precision = PRECISIONS[precision]
+    opt.num_iters = num_iters
+    opt.cnull = 1 if cnull else 0
+    if out is None:
+        out = np.empty((data.num_nodes, pattern.num_nodes), dtype=np.float64)
+    cd, cp = data.c_graph(), pattern.c_graph()
+    _lib.check(_lib.lib().acg_match_graphs_host(C.byref(cd), C.byref(cp), C.byref(opt),
+                                                C.c_void_p(out.ctypes.data if out.size else 0),
+                                                _stream_ptr(None)), "acg_match_graphs_host")
+    return out
+
+
 class Batch:
     """``acg_batch``: many patterns matched against one :class:`DataGraph`.
 

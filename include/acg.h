@@ -158,6 +158,17 @@ acg_status acg_match_graphs(const acg_graph* data, const acg_graph* pattern,
                             const acg_options* opt, double* mu_out,
                             void* stream);
 
+/* One-shot from HOST buffers: the reference program's flow between reading
+ * the graph files and printing MU -- loadGraph's copies (main.cu:54-62), the
+ * match (main.cu:77-247) and the copy of MU back (main.cu:253) -- with the
+ * graphs' arrays in host memory and mu_out_host [data num_nodes][pattern
+ * num_nodes] in host memory.  The edge endpoints are copied first and the data
+ * graph's CSR orderings are built while the features are still being copied
+ * (on a second stream); pinned host buffers let the copies run asynchronously.
+ * Device memory comes from the library's pool.  Synchronises `stream`. */
+acg_status acg_match_graphs_host(const acg_graph* data, const acg_graph* pattern,
+                                 const acg_options* opt, double* mu_out_host, void* stream);
+
 /* ---------------- many patterns against one data graph ----------------- */
 /* No counterpart in the reference, which matches one pattern per run
  * (main.cu:72-75).  The data graph is prepared once; the patterns are packed

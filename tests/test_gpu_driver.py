@@ -54,3 +54,15 @@ def test_driver_mixed_precision(cuda, tmp_path):
                    check=True, capture_output=True)
     mu = np.fromfile(out, dtype=np.float64).reshape(d.num_nodes, p.num_nodes)
     assert np.abs(mu - ref).max() <= 1e-4
+
+
+def test_match_graphs_host_equals_device_path(cuda):
+    """acg_match_graphs_host (host buffers in and out, the feature copies
+    overlapped with the CSR build) gives the device path's mu bit for bit."""
+    from application_classification_gb300 import graph, matcher
+
+    d, p, _ = graph.workload("rmat10_9_18")
+    for prec in ("fp64", "mixed"):
+        a = matcher.match_host(d, p, prec)
+        b = matcher.match(d, p, prec)
+        assert np.array_equal(a, b), prec
