@@ -8,7 +8,11 @@
 // plus the last).  acg_backward walks the segments between checkpoints from
 // the last: it restores the segment's first state, recomputes its iterations
 // with the same kernels (bit-identical: every reduction order is fixed), and
-// runs the adjoint steps of the segment backwards.  The algebra is that of the
+// runs the adjoint steps of the segment backwards.  The edge maxima of each
+// state and their first maximal in-edge are recorded by the edge phase that
+// computes them (the argmax form of edge_max_kernel): in the recorded match for
+// the state before each checkpoint, in the recompute for the others.  The
+// algebra is that of the
 // restructured iteration (the header of acg_bp.cu), unshifted; the numpy model
 // tests/adjoint_model.py states every step and is checked against torch
 // autograd.  Conventions, matching the forward kernels' arithmetic:
@@ -17,8 +21,9 @@
 //     vertex; a segmented maximum (minimum) over a vertex's edges to its first
 //     maximal (minimal) edge in CSR order, i.e. the smallest original edge id;
 //   * log-sum-exps send it through their softmax weights.
-// Every accumulation has a fixed order (per-lane sequences, fixed shuffle
-// trees, blocks in order): the gradients are bit-reproducible.  No atomics.
+// Every sum has a fixed order (per-lane sequences, fixed shuffle trees,
+// blocks in order): the gradients are bit-reproducible.  The one atomic is an
+// integer OR (the per-edge column masks of the maxima), the same in any order.
 //
 // Limits: single-pattern plans of at most 64 padded edge columns and 64
 // pattern vertices (the warp forms), feature dimensions up to 32.
@@ -57,8 +62,7 @@ struct AdjWork {
   void* gCV = nullptr;                             // [Dn][Pn]
   void* gdE = nullptr;                             // [De][Pp]
   void *gRb = nullptr, *gFb = nullptr;             // [Dn][Pqc]
-  void* pval = nullptr;                            // [max partial rows][Pp]
-  int* ppos = nullptr;
+  int* ppos = nullptr;                             // [edge-side partial rows][Pp]: hub chunk positions
   void* pscat = nullptr;                           // [src partial rows][Pp]
   void* pstat = nullptr;                           // [src partial rows][4 Pp]
   int* pstati = nullptr;                           // [src partial rows][2 Pp]
@@ -316,11 +320,8 @@ __global__ void adj_sum_combine_kernel(const T* __restrict__ part, const int* __
 }
 
 // --------------------------------------------------------- vertex steps
-// Per-lane pattern columns as in the forward's warp form: lane l owns edge
+// Lanes own pattern columns as in the forward's warp form: lane l owns edge
 // columns q = l * QPL + k and pattern vertices p = l + 32 j.
-struct PatCols {
-  int qd[2], qs[2];
-};
 
 // Step A (per vertex): the gradients into this iteration's messages, the max
 // selections, and column sums: gaR, gaF (into the fills), GbR, GbF (into
@@ -1439,7 +1440,6 @@ struct Adj {
     return ACG_OK;
   }
 
-  static T neg_inf_h() { return -std::numeric_limits<T>::infinity(); }
 
   // vertex == true: dV (rows = data vertices, columns = pattern vertices,
   // gradient W->gMU); else dE (rows in destination-CSR order, W->gdE).
@@ -1584,7 +1584,6 @@ acg_status adj_alloc(acg_plan* P, int every, cudaStream_t s) {
   ACG_TRY(adj_buf(W, Dn * Pqc * eb, &W->gRb, s));
   ACG_TRY(adj_buf(W, Dn * Pqc * eb, &W->gFb, s));
   const size_t enp = P->ew.npartial, snp = P->sw.npartial;
-  ACG_TRY(adj_buf(W, enp * Pp * eb, &W->pval, s));
   ACG_TRY(adj_buf(W, enp * Pp * sizeof(int), (void**)&W->ppos, s));
   W->ck.ppos = W->ppos;
   ACG_TRY(adj_buf(W, snp * Pp * eb, &W->pscat, s));

@@ -239,7 +239,8 @@ acg_status acg_initial_mu_noalloc(const double* data_node_feats, uint64_t num_no
  * pattern [Pn][node feat dim], [Pe][edge feat dim]), recomputing the
  * iterations between checkpoints.  Maxima pass their gradient to the first
  * maximal element (smallest data vertex; smallest edge id within a vertex's
- * edges); log-sum-exps through their softmax.  Deterministic: no atomics.
+ * edges); log-sum-exps through their softmax.  Deterministic: every sum has
+ * a fixed order (the one atomic is an integer OR).
  * Limits: single plans of at most 64 pattern vertices and 64 pattern edges
  * (padded), feature dimensions <= 32 (else ACG_ERR_UNSUPPORTED).  The
  * checkpoints stay with the plan until it is destroyed or re-recorded.
