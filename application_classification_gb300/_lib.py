@@ -122,6 +122,7 @@ SIGNATURES: dict[str, tuple] = {
     "acg_plan_stats": (i32, [vp, _P(Stats)]),
     "acg_match_graphs": (i32, [_P(Graph), _P(Graph), _P(Options), vp, vp]),
     "acg_match_graphs_host": (i32, [_P(Graph), _P(Graph), _P(Options), vp, vp]),
+    "acg_release_cached_memory": (i32, []),
     "acg_initial_mu_noalloc": (i32, [vp, u64, u64, vp, u64, vp, vp]),
     "acg_batch_create": (i32, [vp, vp, i32, _P(Options), vp, _P(vp)]),
     "acg_batch_match": (i32, [vp, vp, vp]),

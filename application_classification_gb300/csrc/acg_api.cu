@@ -1024,6 +1024,13 @@ acg_status acg_match_graphs(const acg_graph* data, const acg_graph* pattern,
   return st;
 }
 
+acg_status acg_release_cached_memory(void) {
+  clear_error();
+  cudaDeviceSynchronize();
+  release_pools();
+  return ACG_OK;
+}
+
 acg_status acg_match_graphs_host(const acg_graph* data, const acg_graph* pattern,
                                  const acg_options* opt, double* mu_out_host, void* stream) {
   clear_error();

@@ -12,6 +12,8 @@
 // later floating-point reduction order (and so every result) deterministic.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include <algorithm>
 #include <cstdint>
 #include <vector>
@@ -24,10 +26,14 @@ namespace acg {
 // The library's memory pool on the current device (stream-ordered, never
 // trimmed: freed blocks stay cached for the next data graph or plan, as a
 // caching allocator does).  Created on first use per device.
+static cudaMemPool_t g_pools[64] = {};
+static std::mutex g_pool_mutex;
+
 static cudaMemPool_t device_pool() {
-  static cudaMemPool_t pools[64] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(g_pool_mutex);
+  cudaMemPool_t* pools = g_pools;
   if (!pools[dev]) {
     cudaMemPoolProps props{};
     props.allocType = cudaMemAllocationTypePinned;
@@ -68,6 +74,12 @@ acg_status dev_alloc(std::vector<DevBuf>* owned, size_t bytes, void** out, cudaS
   owned->push_back({p, bytes});
   *out = p;
   return ACG_OK;
+}
+
+void release_pools() {
+  std::lock_guard<std::mutex> lock(g_pool_mutex);
+  for (cudaMemPool_t p : g_pools)
+    if (p) cudaMemPoolTrimTo(p, 0);
 }
 
 void dev_free_all(std::vector<DevBuf>* owned) {

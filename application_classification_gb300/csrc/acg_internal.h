@@ -67,6 +67,8 @@ acg_status build_csr(const uint32_t* key, const uint32_t* other, int n, int m, C
 // Allocate `bytes` (>= 1) of device memory, zero it, record it in `owned`.
 acg_status dev_alloc(std::vector<DevBuf>* owned, size_t bytes, void** out, cudaStream_t s);
 void dev_free_all(std::vector<DevBuf>* owned);
+// Return the pools' cached free memory to the driver (acg_release_cached_memory).
+void release_pools();
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 

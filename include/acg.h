@@ -251,6 +251,15 @@ acg_status acg_backward(acg_plan* plan, const double* grad_mu, double* grad_data
                         double* grad_data_edge_feats, double* grad_pattern_node_feats,
                         double* grad_pattern_edge_feats, void* stream);
 
+/* ---------------- memory ----------------------------------------------- */
+/* Device memory of data graphs, plans, batches and the adjoint comes from a
+ * per-device stream-ordered pool that keeps freed blocks cached for the next
+ * object (as a caching allocator does), so the process holds its high-water
+ * mark until exit.  This returns the cached free blocks to the driver (memory
+ * still in use by live objects is not touched).  No counterpart in the
+ * reference. */
+acg_status acg_release_cached_memory(void);
+
 /* ---------------- errors ----------------------------------------------- */
 const char* acg_status_string(acg_status s);
 /* Message of the last failing call on this host thread ("" if none). */

@@ -66,3 +66,18 @@ def test_match_graphs_host_equals_device_path(cuda):
         a = matcher.match_host(d, p, prec)
         b = matcher.match(d, p, prec)
         assert np.array_equal(a, b), prec
+
+
+def test_release_cached_memory(cuda):
+    """Objects freed to the library's pool can be handed back to the driver;
+    matching works again afterwards."""
+    import torch
+    from application_classification_gb300 import _lib, graph, matcher
+
+    d, p, _ = graph.workload("rmat10_9_18")
+    first = matcher.match(d, p, "mixed")
+    _lib.check(_lib.lib().acg_release_cached_memory(), "acg_release_cached_memory")
+    free_after, _ = torch.cuda.mem_get_info()
+    again = matcher.match(d, p, "mixed")
+    assert np.array_equal(first, again)
+    assert free_after > 0
