@@ -12,6 +12,7 @@
 // later floating-point reduction order (and so every result) deterministic.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
 #include <mutex>
 
 #include <algorithm>
@@ -25,11 +26,22 @@ namespace acg {
 
 // The library's memory pool on the current device (stream-ordered, never
 // trimmed: freed blocks stay cached for the next data graph or plan, as a
-// caching allocator does).  Created on first use per device.
+// caching allocator does).  Created on first use per device.  ACG_MEMPOOL=0
+// in the environment selects plain cudaMalloc / cudaFree instead (profilers
+// that save and restore device memory between kernel replays expect it).
 static cudaMemPool_t g_pools[64] = {};
 static std::mutex g_pool_mutex;
 
+static bool pool_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("ACG_MEMPOOL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 static cudaMemPool_t device_pool() {
+  if (!pool_enabled()) return nullptr;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
   std::lock_guard<std::mutex> lock(g_pool_mutex);
@@ -87,14 +99,35 @@ void dev_free_all(std::vector<DevBuf>* owned) {
   // the buffers may be in use on any stream: wait for the device once, then
   // hand them back to the pool
   cudaDeviceSynchronize();
+  const bool pool = pool_enabled();
   for (auto& b : *owned)
-    if (b.p) cudaFreeAsync(b.p, 0);
+    if (b.p) {
+      if (pool)
+        cudaFreeAsync(b.p, 0);
+      else
+        cudaFree(b.p);
+    }
   cudaDeviceSynchronize();
   owned->clear();
 }
 
 // ---------------------------------------------------------------- scan
 namespace {
+
+// Short-lived scratch of the CSR build: the device's default stream-ordered
+// pool, or plain cudaMalloc when ACG_MEMPOOL=0.
+cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
+  return pool_enabled() ? cudaMallocAsync(p, bytes, s) : cudaMalloc(p, bytes);
+}
+
+void scratch_free(void* p, cudaStream_t s) {
+  if (pool_enabled()) {
+    cudaFreeAsync(p, s);
+  } else {
+    cudaStreamSynchronize(s);
+    cudaFree(p);
+  }
+}
 
 constexpr int kScanThreads = 1024;
 constexpr int kScanPerThread = 4;
@@ -159,7 +192,7 @@ acg_status scan_exclusive_u32(const uint32_t* in, uint32_t* out, size_t n, cudaS
     return ACG_OK;
   }
   uint32_t* sums = nullptr;
-  ACG_CUDA_TRY(cudaMallocAsync((void**)&sums, nb * sizeof(uint32_t), s));
+  ACG_CUDA_TRY(scratch_alloc((void**)&sums, nb * sizeof(uint32_t), s));
   scan_tile_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, sums);
   ACG_LAUNCH_CHECK();
   acg_status st = scan_exclusive_u32(sums, sums, nb, s);
@@ -167,7 +200,7 @@ acg_status scan_exclusive_u32(const uint32_t* in, uint32_t* out, size_t n, cudaS
     scan_add_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, n, sums);
     if (cudaGetLastError() != cudaSuccess) st = set_error(ACG_ERR_CUDA, "scan_add launch failed");
   }
-  cudaFreeAsync(sums, s);
+  scratch_free(sums, s);
   return st;
 }
 
@@ -242,7 +275,7 @@ acg_status radix_sort_pairs_u32(uint32_t* keys, uint32_t* vals, uint32_t* keys_t
   const int ntiles = (int)((n + kSortTile - 1) / kSortTile);
   const size_t hn = (size_t)ntiles * 256;
   uint32_t* hist = nullptr;
-  ACG_CUDA_TRY(cudaMallocAsync((void**)&hist, hn * sizeof(uint32_t), s));
+  ACG_CUDA_TRY(scratch_alloc((void**)&hist, hn * sizeof(uint32_t), s));
   uint32_t *ka = keys, *va = vals, *kb = keys_tmp, *vb = vals_tmp;
   acg_status st = ACG_OK;
   const unsigned blocks = (unsigned)((ntiles + kSortWarps - 1) / kSortWarps);
@@ -266,7 +299,7 @@ acg_status radix_sort_pairs_u32(uint32_t* keys, uint32_t* vals, uint32_t* keys_t
     cudaMemcpyAsync(keys, ka, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
     cudaMemcpyAsync(vals, va, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
   }
-  cudaFreeAsync(hist, s);
+  scratch_free(hist, s);
   return st;
 }
 
@@ -306,9 +339,9 @@ acg_status build_csr(const uint32_t* key, const uint32_t* other, int n, int m, C
   ACG_TRY(dev_alloc(owned, sizeof(int) * (size_t)m, (void**)&out->other, s));
   const size_t mm = m > 0 ? (size_t)m : 1;
   uint32_t *k = nullptr, *k2 = nullptr, *v2 = nullptr;
-  ACG_CUDA_TRY(cudaMallocAsync((void**)&k, mm * sizeof(uint32_t), s));
-  ACG_CUDA_TRY(cudaMallocAsync((void**)&k2, mm * sizeof(uint32_t), s));
-  ACG_CUDA_TRY(cudaMallocAsync((void**)&v2, mm * sizeof(uint32_t), s));
+  ACG_CUDA_TRY(scratch_alloc((void**)&k, mm * sizeof(uint32_t), s));
+  ACG_CUDA_TRY(scratch_alloc((void**)&k2, mm * sizeof(uint32_t), s));
+  ACG_CUDA_TRY(scratch_alloc((void**)&v2, mm * sizeof(uint32_t), s));
   acg_status st = ACG_OK;
   uint32_t* vals = reinterpret_cast<uint32_t*>(out->eid);
   if (m > 0) {
@@ -323,9 +356,9 @@ acg_status build_csr(const uint32_t* key, const uint32_t* other, int n, int m, C
     if (m > 0) gather_other_kernel<<<ceil_div(m, 256), 256, 0, s>>>(vals, other, m, out->other);
     if (cudaGetLastError() != cudaSuccess) st = set_error(ACG_ERR_CUDA, "csr launch failed");
   }
-  cudaFreeAsync(k, s);
-  cudaFreeAsync(k2, s);
-  cudaFreeAsync(v2, s);
+  scratch_free(k, s);
+  scratch_free(k2, s);
+  scratch_free(v2, s);
   return st;
 }
 

@@ -257,7 +257,9 @@ acg_status acg_backward(acg_plan* plan, const double* grad_mu, double* grad_data
  * object (as a caching allocator does), so the process holds its high-water
  * mark until exit.  This returns the cached free blocks to the driver (memory
  * still in use by live objects is not touched).  No counterpart in the
- * reference. */
+ * reference.  ACG_MEMPOOL=0 in the environment (read once, at the first
+ * allocation) selects plain cudaMalloc / cudaFree instead; results are the
+ * same bytes either way. */
 acg_status acg_release_cached_memory(void);
 
 /* ---------------- errors ----------------------------------------------- */

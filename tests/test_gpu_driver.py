@@ -81,3 +81,19 @@ def test_release_cached_memory(cuda):
     again = matcher.match(d, p, "mixed")
     assert np.array_equal(first, again)
     assert free_after > 0
+
+
+def test_plain_allocator_gives_identical_output(cuda, tmp_path):
+    """ACG_MEMPOOL=0 (plain cudaMalloc instead of the stream-ordered pool)
+    changes where buffers live, not what is computed: the bytes are equal."""
+    import os
+
+    d, p, ref, dp, pp = _golden_paths(tmp_path, "rmat9")
+    outs = []
+    for flag in ("1", "0"):
+        out = tmp_path / f"mu{flag}.bin"
+        env = dict(os.environ, ACG_MEMPOOL=flag)
+        subprocess.run([EXE, "--precision", "mixed", "--binary", "--out", str(out), str(dp),
+                        str(pp)], check=True, capture_output=True, env=env)
+        outs.append(out.read_bytes())
+    assert outs[0] == outs[1]
