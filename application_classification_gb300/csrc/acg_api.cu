@@ -425,7 +425,8 @@ acg_status iterate(acg_plan* P, int t, double* mu_out, cudaStream_t s) {
     va.rec_ml = (T*)P->rec->ml[t];
   }
   ACG_TRY(launch_vertex_update<T>(va, P->vert_blocks, s));
-  ACG_TRY(launch_finalize(P->bpart, P->vert_blocks, StatSpec{2 * Pe, 2 * Pe + Pn}, P->gi[t & 1], s));
+  ACG_TRY(launch_finalize(P->bpart, P->vert_blocks,
+                          StatSpec{2 * Pe, 2 * Pe + Pn, P->prec != ACG_PREC_FP64}, P->gi[t & 1], s));
   ACG_TRY(launch_capture_s(P->gi[t & 1] + 4 * Pe, P->iters_p, t, P->S_final, Pn, s));
   if (rec)
     ACG_CUDA_TRY(cudaMemcpyAsync(P->rec->glob[t], P->gi[t & 1], sizeof(double) * glob_doubles(Pn, Pe),

@@ -148,25 +148,33 @@ stat_finalize_kernel(const double* __restrict__ bpart, int nblocks, StatSpec spe
       out[o] = r;
     }
   } else {
+    // two passes: the largest m of the non-empty partials, then the sum of
+    // s_b exp(m_b - m) -- one independent exponential per partial; the sum
+    // is taken in a fixed order (threads' strides, xor tree, warps in order)
     const int sl = spec.nmax + 2 * (o - spec.nmax);
-    double m = -CUDART_INF, s = 0.0;
+    const double* pm = bpart + (size_t)sl * nblocks;
+    const double* ps = bpart + (size_t)(sl + 1) * nblocks;
+    double m = -CUDART_INF;
     for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
-      lse_merge(m, s, bpart[(size_t)sl * nblocks + b], bpart[(size_t)(sl + 1) * nblocks + b]);
+      if (lse_nonempty(pm[b], ps[b])) m = fmax(m, pm[b]);
 #pragma unroll
-    for (int k = 16; k >= 1; k >>= 1) {
-      const double m2 = shfl_xor_d(m, k), s2 = shfl_xor_d(s, k);
-      lse_merge(m, s, m2, s2);
-    }
-    if (lane == 0) {
-      sm[w] = m;
-      ss[w] = s;
-    }
+    for (int k = 16; k >= 1; k >>= 1) m = fmax(m, shfl_xor_d(m, k));
+    if (lane == 0) sm[w] = m;
+    __syncthreads();
+    m = sm[0];
+    for (int k = 1; k < 8; ++k) m = fmax(m, sm[k]);
+    double s = 0.0;
+    if (m > -CUDART_INF)
+      for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+        if (lse_nonempty(pm[b], ps[b])) s += ps[b] * merge_exp(pm[b] - m, spec.f32 != 0);
+#pragma unroll
+    for (int k = 16; k >= 1; k >>= 1) s += shfl_xor_d(s, k);
+    if (lane == 0) ss[w] = s;
     __syncthreads();
     if (threadIdx.x == 0) {
-      LseD r;
-      r.init();
-      for (int k = 0; k < 8; ++k) r.merge(sm[k], ss[k]);
-      out[o] = r.value();
+      double t = 0.0;
+      for (int k = 0; k < 8; ++k) t += ss[k];
+      out[o] = (m > -CUDART_INF && t > 0.0) ? m + log(t) : -CUDART_INF;
     }
   }
 }

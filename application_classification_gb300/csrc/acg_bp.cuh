@@ -21,6 +21,7 @@ __host__ __device__ inline int pattern_ints(int pn, int pe) { return 4 * pe + 2 
 struct StatSpec {
   int nmax;
   int nlse;
+  int f32 = 0;  // merge with the FP32 exponential (statistics of FP32 kernels)
   __host__ __device__ int slots() const { return nmax + 2 * nlse; }
   __host__ __device__ int outs() const { return nmax + nlse; }
 };

@@ -172,12 +172,26 @@ __device__ __forceinline__ void lse_merge(double& m, double& s, double m2, doubl
   s = a.s;
 }
 
+// exp(d) for d <= 0, the factor that rescales a partial sum when partial
+// log-sum-exps are merged.  FP64 for FP64 statistics; the FP32 exponential
+// (relative error ~1e-7, that of the FP32 partial sums it scales) for the
+// statistics of FP32 kernels -- FP64 transcendentals are slow on this GPU.
+__device__ __forceinline__ double merge_exp(double d, bool f32) {
+  return f32 ? (double)expf((float)d) : exp(d);
+}
+// A partial (m, s) that holds no term: m = -inf or s = 0.
+__device__ __forceinline__ bool lse_nonempty(double m, double s) {
+  return m > -CUDART_INF && s != 0.0;
+}
+
 // Per-block statistics written as partials [slot][column]: `nmax` maxima, then
 // `nlse` log-sum-exps as (m, s) pairs.  red[w * slots + slot] holds warp w's
 // value; warps are combined in order, so the result does not depend on timing.
+// Each log-sum-exp is merged in two passes (the largest m, then the sum of
+// s_w exp(m_w - m)): one independent exponential per partial, no chain.
 __device__ __forceinline__ void write_block_partials(const double* red, int nwarps, int nmax,
                                                      int nlse, double* bpart, int ncols,
-                                                     int col) {
+                                                     int col, bool f32 = false) {
   const int slots = nmax + 2 * nlse;
   for (int j = threadIdx.x; j < nmax + nlse; j += blockDim.x) {
     if (j < nmax) {
@@ -187,7 +201,16 @@ __device__ __forceinline__ void write_block_partials(const double* red, int nwar
     } else {
       const int sm = nmax + 2 * (j - nmax);
       double m = -CUDART_INF, s = 0.0;
-      for (int w = 0; w < nwarps; ++w) lse_merge(m, s, red[w * slots + sm], red[w * slots + sm + 1]);
+      for (int w = 0; w < nwarps; ++w) {
+        const double m2 = red[w * slots + sm], s2 = red[w * slots + sm + 1];
+        if (lse_nonempty(m2, s2)) m = fmax(m, m2);
+      }
+      if (m > -CUDART_INF) {
+        for (int w = 0; w < nwarps; ++w) {
+          const double m2 = red[w * slots + sm], s2 = red[w * slots + sm + 1];
+          if (lse_nonempty(m2, s2)) s += s2 * merge_exp(m2 - m, f32);
+        }
+      }
       bpart[(size_t)sm * ncols + col] = m;
       bpart[(size_t)(sm + 1) * ncols + col] = s;
     }

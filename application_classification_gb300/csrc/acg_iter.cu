@@ -971,7 +971,7 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
     }
   }
   __syncthreads();
-  write_block_partials(red, kVw, nmax, nlse, a.bpart, gridDim.x, blockIdx.x);
+  write_block_partials(red, kVw, nmax, nlse, a.bpart, gridDim.x, blockIdx.x, sizeof(T) == 4);
 }
 
 __global__ void capture_s_kernel(const double* __restrict__ S, const int* __restrict__ iters_p,
