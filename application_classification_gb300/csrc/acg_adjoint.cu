@@ -749,6 +749,7 @@ struct QuirkArgs {
   int* ppos;           // [npartial][2 Pqc]: position, covered
   long long De;
   int Pp, Pqc, qcov;
+  int nranges;         // item ranges; warp w does ranges w, w + warps, ...
 };
 
 template <typename T, int NPOW, int NQV>
@@ -774,7 +775,9 @@ __global__ void __launch_bounds__(kT) adj_quirk_dst_kernel(const QuirkArgs<T> a)
       gl[k] = a.cols[q];
     }
   }
-  for (int it = a.wsplit[gw]; it < a.wsplit[gw + 1]; ++it) {
+  const int nw = (int)gridDim.x * (kT / 32);
+  for (int r = gw; r < a.nranges; r += nw)
+  for (int it = a.wsplit[r]; it < a.wsplit[r + 1]; ++it) {
     const int4 item = a.items[it];
     T best[NQ];
     int pos[NQ], cov[NQ];
@@ -1379,7 +1382,8 @@ struct Adj {
     // quirk rows over in-edges (covered columns), then the source side
     if (De > 0 && P->qcov > 0) {
       QuirkArgs<T> a{P->ew.items, P->ew.wsplit, D->dcsr.eid, (const T*)P->dE, (const T*)W->gFb, P->ge,
-                     P->qlim_col, W->cols, (T*)W->gdE, (T*)W->pq, W->pqi, (long long)De, Pp, Pqc, P->qcov};
+                     P->qlim_col, W->cols, (T*)W->gdE, (T*)W->pq, W->pqi, (long long)De, Pp, Pqc, P->qcov,
+                     P->ew.nparts};
       bool done = false;
 #define ADJ_Q(NP_, NQ_)                                                         \
       if (!done && P->qws.npow == NP_ && P->qws.nqv == NQ_) {                   \

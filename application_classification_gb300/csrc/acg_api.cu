@@ -235,9 +235,10 @@ __global__ void work_split_kernel(const uint32_t* __restrict__ excl, const uint3
 // item costs gives each warp boundary.  The same items and boundaries as
 // build_warp_work_host, without copying the offsets to the host.
 acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* out,
-                                std::vector<DevBuf>* owned, cudaStream_t s) {
+                                std::vector<DevBuf>* owned, cudaStream_t s, int max_ranges,
+                                int chunk_div) {
   const int n = c.n;
-  if (n == 0 || nwarps < 1) return build_warp_work_host(c, nwarps, step, out, owned, s);
+  if (n == 0 || nwarps < 1) return build_warp_work_host(c, nwarps, step, out, owned, s, max_ranges, chunk_div);
   std::vector<DevBuf> tmp;
   auto fail = [&](acg_status st) {
     dev_free_all(&tmp);
@@ -257,10 +258,11 @@ acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* ou
   ACG_CUDA_TRY(cudaStreamSynchronize(s));
   if (htotal >= 0x7fffffffull) {  // the 32-bit scans could overflow: build on the host
     dev_free_all(&tmp);
-    return build_warp_work_host(c, nwarps, step, out, owned, s);
+    return build_warp_work_host(c, nwarps, step, out, owned, s, max_ranges, chunk_div);
   }
-  const double per_warp = (double)htotal / std::max(1, nwarps);
-  const long long cs = std::max(4LL, (long long)(per_warp / 4));  // chunk, in steps
+  const int nparts = work_parts((double)htotal, nwarps, max_ranges);
+  const double per_part = (double)htotal / nparts;
+  const long long cs = std::max(4LL, (long long)(per_part / chunk_div));  // chunk, in steps
   const int chunk = (int)std::min<long long>(1LL << 24, cs * step);
   work_count_kernel<<<ceil_div(n, 256), 256, 0, s>>>(c.off, n, chunk, nit, npart, hub);
   if (cudaGetLastError() != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "work count launch failed"));
@@ -277,12 +279,12 @@ acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* ou
   WarpWork& W = *out;
   W = WarpWork{};
   W.nitems = nitems;
-  W.nwarps = nwarps;
+  W.nparts = nparts;
   W.chunk = chunk;
   W.nheavy = nheavy;
   W.npartial = npartial;
   ACG_TRY(dev_alloc(owned, sizeof(int4) * std::max(1, nitems), (void**)&W.items, s));
-  ACG_TRY(dev_alloc(owned, sizeof(int) * ((size_t)nwarps + 1), (void**)&W.wsplit, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * ((size_t)nparts + 1), (void**)&W.wsplit, s));
   ACG_TRY(dev_alloc(owned, sizeof(int) * std::max(1, nheavy), (void**)&W.hbase, s));
   ACG_TRY(dev_alloc(owned, sizeof(int) * std::max(1, nheavy), (void**)&W.hcount, s));
   ACG_TRY(dev_alloc(owned, sizeof(int) * std::max(1, nheavy), (void**)&W.hvert, s));
@@ -295,7 +297,7 @@ acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* ou
   if (cudaGetLastError() != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "work items launch failed"));
   // exclusive prefix of the item costs; boundaries
   ACG_TRY(scan_exclusive_u32(cost, excl, (size_t)nitems, s));
-  work_split_kernel<<<ceil_div(nwarps + 1, 256), 256, 0, s>>>(excl, cost, nitems, nwarps, W.wsplit);
+  work_split_kernel<<<ceil_div(nparts + 1, 256), 256, 0, s>>>(excl, cost, nitems, nparts, W.wsplit);
   if (cudaGetLastError() != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "work split launch failed"));
   ACG_CUDA_TRY(cudaStreamSynchronize(s));
   dev_free_all(&tmp);
@@ -303,7 +305,8 @@ acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* ou
 }
 
 acg_status acg::build_warp_work_host(const Csr& c, int nwarps, int step, WarpWork* out,
-                                     std::vector<DevBuf>* owned, cudaStream_t s) {
+                                     std::vector<DevBuf>* owned, cudaStream_t s, int max_ranges,
+                                     int chunk_div) {
   const int n = c.n;
   std::vector<int> off((size_t)n + 1);
   ACG_CUDA_TRY(cudaMemcpyAsync(off.data(), c.off, sizeof(int) * ((size_t)n + 1),
@@ -315,8 +318,8 @@ acg_status acg::build_warp_work_host(const Csr& c, int nwarps, int step, WarpWor
     const int deg = off[v + 1] - off[v];
     if (deg) total += (deg + step - 1) / step + kOver;
   }
-  const double per_warp = total / std::max(1, nwarps);
-  const long long cs = std::max(4LL, (long long)(per_warp / 4));  // chunk, in steps
+  const int nparts = work_parts(total, nwarps, max_ranges);
+  const long long cs = std::max(4LL, (long long)(total / nparts / chunk_div));  // chunk, in steps
   const int chunk = (int)std::min<long long>(1LL << 24, cs * step);
   std::vector<int4> items;
   std::vector<double> cost;
@@ -343,22 +346,22 @@ acg_status acg::build_warp_work_host(const Csr& c, int nwarps, int step, WarpWor
       cost.push_back((deg + step - 1) / step + kOver);
     }
   }
-  std::vector<int> split((size_t)nwarps + 1, (int)items.size());
+  std::vector<int> split((size_t)nparts + 1, (int)items.size());
   split[0] = 0;
   {
     double acc = 0, target = 0;
     for (double x : cost) target += x;
-    target /= std::max(1, nwarps);
+    target /= nparts;
     int w = 1;
-    for (size_t i = 0; i < items.size() && w < nwarps; ++i) {
+    for (size_t i = 0; i < items.size() && w < nparts; ++i) {
       acc += cost[i];
-      while (w < nwarps && acc >= target * w) split[w++] = (int)i + 1;
+      while (w < nparts && acc >= target * w) split[w++] = (int)i + 1;
     }
   }
   WarpWork& W = *out;
   W = WarpWork{};
   W.nitems = (int)items.size();
-  W.nwarps = nwarps;
+  W.nparts = nparts;
   W.chunk = chunk;
   W.nheavy = (int)hv.size();
   W.npartial = npart;
@@ -392,6 +395,8 @@ acg_status iterate(acg_plan* P, int t, double* mu_out, cudaStream_t s) {
     EdgeMaxArgs<T> ea{P->ew.items, P->ew.nitems, P->ew.wsplit, D->dcsr.other,
                       (const T*)P->dE, (const T*)P->vr[(t - 1) & 1], (T*)P->M,
                       (T*)P->part_iter, Pp};
+    ea.nranges = P->ew.nparts;
+    ea.ctr = P->edge_ctr;
     const bool am = P->rec && P->rec->has_am(t - 1);  // record M and its argmax of state t - 1
     if (am) {
       ea.argpos = P->rec->a[t - 1];
@@ -469,7 +474,7 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s, const UnionOut
     ACG_TRY(launch_src_stats_combine<T>(sa, P->sw, s));
     DstQuirkArgs<T> qa{P->ew.items, P->ew.nitems, P->ew.wsplit, D->dcsr.eid, (const T*)P->dE,
                        (T*)P->Fq, (T*)P->part_iter, P->bpart, P->qlim_col, De, lim, Pp,
-                       P->Pqc, P->qcov};
+                       P->Pqc, P->qcov, P->ew.nparts};
     ACG_TRY(launch_dst_quirk<T>(qa, P->qws, P->edge_blocks, s));
     if (P->qcov > 0 && P->ew.nitems > 0) {  // ge[q < Pqc]; the later columns stay -inf
       ACG_TRY(launch_finalize(P->bpart, P->edge_blocks, StatSpec{0, P->Pqc}, P->ge, s));
@@ -615,14 +620,32 @@ acg_status resolve_options(const acg_options* opt, acg_options* o) {
   return ACG_OK;
 }
 
-// The work split for (CSR, warps, step), built once per data graph.
+// At most kEdgeRanges item ranges per launched warp of the edge phase (fewer
+// when a range would fall under kMinRangeSteps load steps): a warp does its
+// own range, then claims others as it finishes.  Heavy-vertex chunks are as
+// long as a range (chunk_div 1): with claimed ranges that leaves no tail, and
+// fewer chunks mean fewer partial rows to write and combine.  RMAT-22 edge
+// phase with fixed counts and quarter-range chunks: 1 range (a static split)
+// 4.05 ms, 4: 3.76, 8: 3.49, 16: 3.41, 64: 3.53; 32 with range-long chunks
+// 3.27 ms.  RMAT-18 wants fewer: 32 ranges of ~5 steps 0.27 ms, 16: 0.13.
+#ifndef ACG_EDGE_RANGES
+#define ACG_EDGE_RANGES 32
+#endif
+constexpr int kEdgeRanges = ACG_EDGE_RANGES;
+#ifndef ACG_EDGE_CHUNK_DIV
+#define ACG_EDGE_CHUNK_DIV 1
+#endif
+constexpr int kEdgeChunkDiv = ACG_EDGE_CHUNK_DIV;
+
+// The work split for (CSR, parts, step, chunk divisor), built once per data graph.
 static acg_status get_work(acg_data* D, int which, int nwarps, int step, WarpWork* out,
-                           cudaStream_t s) {
-  const auto key = std::make_tuple(which, nwarps, step);
+                           cudaStream_t s, int max_ranges = 1, int chunk_div = 4) {
+  const auto key = std::make_tuple(which, nwarps, step, max_ranges, chunk_div);
   auto it = D->work.find(key);
   if (it == D->work.end()) {
     WarpWork w;
-    ACG_TRY(build_warp_work(which == 0 ? D->dcsr : D->scsr, nwarps, step, &w, &D->owned, s));
+    ACG_TRY(build_warp_work(which == 0 ? D->dcsr : D->scsr, nwarps, step, &w, &D->owned, s,
+                            max_ranges, chunk_div));
     it = D->work.emplace(key, w).first;
   }
   *out = it->second;
@@ -703,7 +726,10 @@ acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& 
     const int fit = eb == 8 ? edge_max_blocks_per_sm<double>(P->ws) : edge_max_blocks_per_sm<float>(P->ws);
     P->edge_blocks = D->num_sms * (o.edge_blocks_per_sm > 0 ? std::min(fit, o.edge_blocks_per_sm) : fit);
   }
-  st = get_work(D, 0, P->edge_blocks * 8, edge_step(P->ws), &P->ew, s);
+  // item ranges for the launched warps: each warp's own, then claimed
+  st = get_work(D, 0, P->edge_blocks * 8, edge_step(P->ws), &P->ew, s, kEdgeRanges, kEdgeChunkDiv);
+  if (st != ACG_OK) return fail(st);
+  st = dev_alloc(&P->owned, 2 * sizeof(int), (void**)&P->edge_ctr, s);
   if (st != ACG_OK) return fail(st);
   // source-side static pass: one wave of resident blocks over the source CSR
   {

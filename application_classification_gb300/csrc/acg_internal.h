@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <algorithm>
 #include <vector>
 
 #include "acg.h"
@@ -38,8 +39,8 @@ struct Csr {
 struct WarpWork {
   int4* items = nullptr;
   int nitems = 0;
-  int* wsplit = nullptr;   // [nwarps + 1]
-  int nwarps = 0;
+  int* wsplit = nullptr;   // [nparts + 1]
+  int nparts = 0;          // parts of the split: one per warp, or item ranges
   int chunk = 0;           // positions per chunk
   int* hbase = nullptr;
   int* hcount = nullptr;
@@ -47,11 +48,24 @@ struct WarpWork {
   int nheavy = 0, npartial = 0;
 };
 // `step` = positions one warp loads per step of its pass (the cost unit).
+// With max_ranges > 1 the work of each of the nwarps launched warps is cut into
+// R = clamp(its steps / kMinRangeSteps, 1, max_ranges) item ranges (claimed at
+// run time past the first); a chunk is 1 / chunk_div of a part's cost (at least
+// 4 steps).
+constexpr int kMinRangeSteps = 16;
 acg_status build_warp_work(const Csr& c, int nwarps, int step, WarpWork* out,
-                           std::vector<DevBuf>* owned, cudaStream_t s);
+                           std::vector<DevBuf>* owned, cudaStream_t s, int max_ranges = 1,
+                           int chunk_div = 4);
 // The same on the host (the fallback when a cost sum would leave 32 bits).
 acg_status build_warp_work_host(const Csr& c, int nwarps, int step, WarpWork* out,
-                                std::vector<DevBuf>* owned, cudaStream_t s);
+                                std::vector<DevBuf>* owned, cudaStream_t s, int max_ranges = 1,
+                                int chunk_div = 4);
+// Parts of a split for nwarps warps whose total cost is `total` steps.
+inline int work_parts(double total, int nwarps, int max_ranges) {
+  if (max_ranges <= 1 || nwarps < 1) return std::max(1, nwarps);
+  const double r = total / nwarps / kMinRangeSteps;
+  return nwarps * (r < 1.0 ? 1 : (r > max_ranges ? max_ranges : (int)r));
+}
 
 // ---- primitives (acg_csr.cu)
 // Exclusive scan of n uint32 values (in and out may alias); stream ordered.

@@ -80,20 +80,16 @@ __host__ __device__ inline size_t a16(size_t b) { return (b + 15) & ~size_t(15);
 #endif
 // ARG: also the first maximal dst-CSR position of each maximum (adjoint
 // recording): ties go to the smaller position.
+// One range of a warp's items, [it, it_end).
 template <typename T, int NPOW, int NQV, bool ARG>
-__global__ void __launch_bounds__(kAT, ACG_EDGE_MINB)
-edge_max_kernel(const EdgeMaxArgs<T> a) {
+__device__ __forceinline__ void edge_max_range(const EdgeMaxArgs<T>& a, int it, const int it_end,
+                                               const int slot, const int qc) {
   using VT = typename VecT<T>::type;
   constexpr int W = VecT<T>::W;
   constexpr int S = 32 / NPOW;
   constexpr int NQ = NQV * W;
   constexpr int STEP = S * kU;
   const int Pp = a.Pp;
-  const int lane = threadIdx.x & 31;
-  const int slot = lane / NPOW, qc = lane % NPOW;
-  const int gw = (blockIdx.x * kAT + threadIdx.x) >> 5;
-  const int it_end = __ldg(a.wsplit + gw + 1);
-  int it = __ldg(a.wsplit + gw);
   if (it >= it_end) return;
 
   // Software pipeline over the warp's steps (kU in-edges per slot per step,
@@ -222,6 +218,32 @@ edge_max_kernel(const EdgeMaxArgs<T> a) {
       item_next = it + 1 < it_end ? __ldg(a.items + it + 1) : make_int4(0, 0, 0, -1);
     }
     base = nbase;
+  }
+}
+
+template <typename T, int NPOW, int NQV, bool ARG>
+__global__ void __launch_bounds__(kAT, ACG_EDGE_MINB)
+edge_max_kernel(const EdgeMaxArgs<T> a) {
+  const int lane = threadIdx.x & 31;
+  const int slot = lane / NPOW, qc = lane % NPOW;
+  const int nw = (int)gridDim.x * (kAT / 32);
+  const int gw = (blockIdx.x * kAT + threadIdx.x) >> 5;
+  // The warp's own range first, then claimed ones (the claim of the next is in
+  // flight while this one runs): warps that finish early keep taking work, so
+  // the SMs stay full until the last ranges instead of waiting on the slowest
+  // warp of a static split.
+  for (int r = gw; r < a.nranges;) {
+    int rn = a.nranges;
+    if (a.ctr && lane == 0) rn = nw + atomicAdd(a.ctr, 1);
+    edge_max_range<T, NPOW, NQV, ARG>(a, __ldg(a.wsplit + r), __ldg(a.wsplit + r + 1), slot, qc);
+    r = __shfl_sync(0xffffffffu, rn, 0);
+  }
+  if (a.ctr && lane == 0) {
+    __threadfence();  // this warp's claims come before its finish count
+    if (atomicAdd(a.ctr + 1, 1) == nw - 1) {  // every warp has made its last claim
+      a.ctr[0] = 0;
+      a.ctr[1] = 0;
+    }
   }
 }
 

@@ -14,7 +14,7 @@ template <typename T>
 struct EdgeMaxArgs {
   const int4* items;
   int nitems;
-  const int* wsplit;   // [warps + 1]: warp w does items [wsplit[w], wsplit[w+1])
+  const int* wsplit;   // [nranges + 1]: range r is items [wsplit[r], wsplit[r+1])
   const int* src_of;   // [De] source vertex of each dst-CSR position
   const T* dE;         // [De][Pp]
   const T* vr_in;      // [Dn][Pp]
@@ -25,6 +25,12 @@ struct EdgeMaxArgs {
   // position of each maximum ([Dn][Pp]; ppos: [npartial][Pp] for the chunks)
   int* argpos = nullptr;
   int* ppos = nullptr;
+  // Item ranges: warp w first does range w; with `ctr` (two zeroed ints: the
+  // next range past the warps' first ones, and the warps finished) further
+  // ranges are claimed from the counter, and the last warp to finish resets
+  // both.  Without it nranges must equal the launched warps.
+  int nranges = 0;
+  int* ctr = nullptr;
 };
 
 // Column statistics of one iteration (FP64), double-buffered across iterations:

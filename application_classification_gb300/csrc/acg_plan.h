@@ -37,7 +37,7 @@ struct acg_data {
   int ke32 = 0;
   // warp work splits, shared by every plan on this graph: key = (0 dst / 1 src
   // CSR, warps, positions per step)
-  std::map<std::tuple<int, int, int>, acg::WarpWork> work;
+  std::map<std::tuple<int, int, int, int, int>, acg::WarpWork> work;
   std::vector<acg::DevBuf> owned;
 };
 
@@ -119,6 +119,7 @@ struct acg_plan {
   int64_t launches = 0;
   bool ran = false;
   bool cdist_tc = false;       // edge cost matrix on the tensor cores
+  int* edge_ctr = nullptr;     // [2] the edge phase's range claims and finished warps
   int* dev_err = nullptr;      // set by a device-side bounded wait that gave up
   double* cnull = nullptr;     // [Pe] C-null term, then [2 Pe] dE column stats (option cnull)
   double* cnull_part = nullptr;  // [3 Pe][cnull_blocks] block partials

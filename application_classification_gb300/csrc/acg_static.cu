@@ -302,8 +302,7 @@ dst_quirk_kernel(const DstQuirkArgs<T> a) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int slot = lane / NPOW, qc = lane % NPOW;
   const int gw = (blockIdx.x * kST + threadIdx.x) >> 5;
-  const int it_end = __ldg(a.wsplit + gw + 1);
-  int it = __ldg(a.wsplit + gw);
+  const int nw = (int)gridDim.x * (kST / 32);
   T qx[NQ];
   long long qlim[NQ];
   // LSE of -dE over the covered elements of each column (the reference's
@@ -316,7 +315,10 @@ dst_quirk_kernel(const DstQuirkArgs<T> a) {
     const int q = (qc + NPOW * (k / W)) * W + k % W;
     qlim[k] = q < qcov ? __ldg(a.qlim_col + q) : 0;
   }
-  if (it < it_end) {
+  for (int r = gw; r < a.nranges; r += nw) {
+    const int it_end = __ldg(a.wsplit + r + 1);
+    int it = __ldg(a.wsplit + r);
+    if (it >= it_end) continue;
     int4 item = __ldg(a.items + it);
     int base = item.y;
     for (;;) {

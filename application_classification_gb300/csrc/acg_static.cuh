@@ -66,6 +66,8 @@ struct DstQuirkArgs {
   const long long* qlim_col;  // [Pp] as for the source side
   long long De, lim;
   int Pp, Pqc, qcov;
+  int nranges = 0;     // item ranges (wsplit has nranges + 1 entries); warp w
+                       // does ranges w, w + warps, ...
 };
 template <typename T>
 acg_status launch_dst_quirk(const DstQuirkArgs<T>& a, WarpShape ws, int blocks, cudaStream_t s);
