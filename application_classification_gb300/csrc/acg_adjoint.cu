@@ -250,6 +250,7 @@ struct ScatArgs {
   T* gVRe;
   T* part;
   int Pp, Pe;
+  int nranges;         // item ranges; warp w does ranges w, w + warps, ...
 };
 
 template <typename T, int NPOW, int NQV>
@@ -257,7 +258,9 @@ __global__ void ACG_ADJ_BOUNDS adj_scatter_kernel(const ScatArgs<T> a) {
   constexpr int W = AV<T>::W, S = 32 / NPOW, NQ = NQV * W;
   const int Pp = a.Pp, Pe = a.Pe, lane = threadIdx.x & 31, slot = lane / NPOW, qc = lane % NPOW;
   const int gw = (blockIdx.x * kT + threadIdx.x) >> 5;
-  for (int it = a.wsplit[gw]; it < a.wsplit[gw + 1]; ++it) {
+  const int nw = (int)gridDim.x * (kT / 32);
+  for (int r = gw; r < a.nranges; r += nw)
+  for (int it = a.wsplit[r]; it < a.wsplit[r + 1]; ++it) {
     const int4 item = a.items[it];
     T acc[NQ];
 #pragma unroll
@@ -881,6 +884,7 @@ struct SrcBackArgs {
   T* pval;             // [npartial][2 Pp]: min value | quirk max value
   int* ppos;           // [npartial][3 Pp]: min position | quirk position | covered
   int Pp, Pe, Pqc, qcov;
+  int nranges;         // item ranges; warp w does ranges w, w + warps, ...
 };
 
 template <typename T, int NPOW, int NQV>
@@ -894,7 +898,9 @@ __global__ void __launch_bounds__(kT) adj_src_back_kernel(const SrcBackArgs<T> a
     const int q = (qc + NPOW * (k / W)) * W + k % W;
     qlim[k] = q < a.qcov ? a.qlim_col[q] : 0;
   }
-  for (int it = a.wsplit[gw]; it < a.wsplit[gw + 1]; ++it) {
+  const int nw = (int)gridDim.x * (kT / 32);
+  for (int r = gw; r < a.nranges; r += nw)
+  for (int it = a.wsplit[r]; it < a.wsplit[r + 1]; ++it) {
     const int4 item = a.items[it];
     const size_t vrow = (size_t)item.x * Pp;
     T mn[NQ], bq[NQ], Bv[NQ], gBv[NQ];
@@ -1214,7 +1220,7 @@ struct Adj {
 
   acg_status scatter() {
     ScatArgs<T> a{P->sw.items, P->sw.wsplit, D->pos_in_dst, D->scsr.other, W->emask, (const T*)W->gM,
-                  (T*)W->gVRe, (T*)W->pscat, Pp, Pe};
+                  (T*)W->gVRe, (T*)W->pscat, Pp, Pe, P->sw.nparts};
     ACG_TRY(fill(W->gVRe, vrow(), T(0)));  // sources without out-edges
     bool done = false;
 #define ADJ_SC(NP_, NQ_)                                                        \
@@ -1403,7 +1409,8 @@ struct Adj {
     if (De > 0 && Pe > 0) {
       SrcBackArgs<T> a{P->sw.items, P->sw.wsplit, D->pos_in_dst, D->scsr.eid, (const T*)P->dE,
                        (const T*)P->B, (const T*)W->gB, (const T*)W->gdEmin, (const T*)W->gRb,
-                       P->qlim_col, (T*)W->gdE, (T*)W->pstat, W->pstati, Pp, Pe, Pqc, P->qcov};
+                       P->qlim_col, (T*)W->gdE, (T*)W->pstat, W->pstati, Pp, Pe, Pqc, P->qcov,
+                       P->sw.nparts};
       bool done = false;
 #define ADJ_S(NP_, NQ_)                                                         \
       if (!done && P->ws.npow == NP_ && P->ws.nqv == NQ_) {                     \

@@ -396,7 +396,7 @@ acg_status iterate(acg_plan* P, int t, double* mu_out, cudaStream_t s) {
                       (const T*)P->dE, (const T*)P->vr[(t - 1) & 1], (T*)P->M,
                       (T*)P->part_iter, Pp};
     ea.nranges = P->ew.nparts;
-    ea.ctr = P->edge_ctr;
+    ea.ctr = P->range_ctr;
     const bool am = P->rec && P->rec->has_am(t - 1);  // record M and its argmax of state t - 1
     if (am) {
       ea.argpos = P->rec->a[t - 1];
@@ -470,6 +470,8 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s, const UnionOut
     SrcStatsArgs<T> sa{P->sw.items, P->sw.nitems, P->sw.wsplit, D->pos_in_dst, D->scsr.eid,
                        (const T*)P->dE, (T*)P->dEmin, (T*)P->B, (T*)P->Rq,
                        (T*)P->part_src, P->qlim_col, De, lim, Pp, P->Pqc, P->qcov};
+    sa.nranges = P->sw.nparts;
+    sa.ctr = P->range_ctr;
     ACG_TRY(launch_src_stats<T>(sa, P->ws, P->src_blocks, s));
     ACG_TRY(launch_src_stats_combine<T>(sa, P->sw, s));
     DstQuirkArgs<T> qa{P->ew.items, P->ew.nitems, P->ew.wsplit, D->dcsr.eid, (const T*)P->dE,
@@ -729,14 +731,14 @@ acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& 
   // item ranges for the launched warps: each warp's own, then claimed
   st = get_work(D, 0, P->edge_blocks * 8, edge_step(P->ws), &P->ew, s, kEdgeRanges, kEdgeChunkDiv);
   if (st != ACG_OK) return fail(st);
-  st = dev_alloc(&P->owned, 2 * sizeof(int), (void**)&P->edge_ctr, s);
+  st = dev_alloc(&P->owned, 2 * sizeof(int), (void**)&P->range_ctr, s);
   if (st != ACG_OK) return fail(st);
   // source-side static pass: one wave of resident blocks over the source CSR
   {
     const int fit = eb == 8 ? src_stats_blocks_per_sm<double>(P->ws) : src_stats_blocks_per_sm<float>(P->ws);
     P->src_blocks = D->num_sms * (o.edge_blocks_per_sm > 0 ? std::min(fit, o.edge_blocks_per_sm) : fit);
   }
-  st = get_work(D, 1, P->src_blocks * 8, edge_step(P->ws), &P->sw, s);
+  st = get_work(D, 1, P->src_blocks * 8, edge_step(P->ws), &P->sw, s, kEdgeRanges, kEdgeChunkDiv);
   if (st != ACG_OK) return fail(st);
   P->Pqc = std::max(W, (P->qcov + W - 1) / W * W);
   P->qws = choose_warp_shape(eb, P->Pqc);

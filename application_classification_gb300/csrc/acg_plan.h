@@ -119,7 +119,9 @@ struct acg_plan {
   int64_t launches = 0;
   bool ran = false;
   bool cdist_tc = false;       // edge cost matrix on the tensor cores
-  int* edge_ctr = nullptr;     // [2] the edge phase's range claims and finished warps
+  int* range_ctr = nullptr;    // [2] range claims and finished warps of the range-split
+                               // kernels (one at a time on the plan's stream; each
+                               // launch leaves both at zero)
   int* dev_err = nullptr;      // set by a device-side bounded wait that gave up
   double* cnull = nullptr;     // [Pe] C-null term, then [2 Pe] dE column stats (option cnull)
   double* cnull_part = nullptr;  // [3 Pe][cnull_blocks] block partials

@@ -83,20 +83,16 @@ __device__ __forceinline__ T exp_ref_limit() { return sizeof(T) == 4 ? T(60) : T
 #else
 #define ACG_SRC_BOUNDS __launch_bounds__(kST)
 #endif
+// One range of a warp's items, [it, it_end).
 template <typename T, int NPOW, int NQV>
-__global__ void ACG_SRC_BOUNDS
-src_stats_kernel(const SrcStatsArgs<T> a) {
+__device__ __forceinline__ void src_stats_range(const SrcStatsArgs<T>& a, int it, const int it_end,
+                                                const int slot, const int qc) {
   using VT = typename SV<T>::type;
   constexpr int W = SV<T>::W;
   constexpr int S = 32 / NPOW;
   constexpr int NQ = NQV * W;
   constexpr int STEP = S * kSU;
   const int Pp = a.Pp, Pqc = a.Pqc, qcov = a.qcov;
-  const int lane = threadIdx.x & 31;
-  const int slot = lane / NPOW, qc = lane % NPOW;
-  const int gw = (blockIdx.x * kST + threadIdx.x) >> 5;
-  const int it_end = __ldg(a.wsplit + gw + 1);
-  int it = __ldg(a.wsplit + gw);
   if (it >= it_end) return;
 
   int4 item = __ldg(a.items + it);
@@ -257,6 +253,29 @@ src_stats_kernel(const SrcStatsArgs<T> a) {
       item_next = it + 1 < it_end ? __ldg(a.items + it + 1) : make_int4(0, 0, 0, -1);
     }
     base = nbase;
+  }
+}
+
+// The warp's own range first, then claimed ones (as edge_max_kernel).
+template <typename T, int NPOW, int NQV>
+__global__ void ACG_SRC_BOUNDS
+src_stats_kernel(const SrcStatsArgs<T> a) {
+  const int lane = threadIdx.x & 31;
+  const int slot = lane / NPOW, qc = lane % NPOW;
+  const int nw = (int)gridDim.x * (kST / 32);
+  const int gw = (blockIdx.x * kST + threadIdx.x) >> 5;
+  for (int r = gw; r < a.nranges;) {
+    int rn = a.nranges;
+    if (a.ctr && lane == 0) rn = nw + atomicAdd(a.ctr, 1);
+    src_stats_range<T, NPOW, NQV>(a, __ldg(a.wsplit + r), __ldg(a.wsplit + r + 1), slot, qc);
+    r = __shfl_sync(0xffffffffu, rn, 0);
+  }
+  if (a.ctr && lane == 0) {
+    __threadfence();  // this warp's claims come before its finish count
+    if (atomicAdd(a.ctr + 1, 1) == nw - 1) {  // every warp has made its last claim
+      a.ctr[0] = 0;
+      a.ctr[1] = 0;
+    }
   }
 }
 

@@ -42,6 +42,10 @@ struct SrcStatsArgs {
   const long long* qlim_col;  // [Pp] column q covers original edge ids < qlim_col[q]
   long long De, lim;
   int Pp, Pqc, qcov;
+  // item ranges, as the edge phase's: warp w first does range w, then claims
+  // ranges from ctr (two zeroed ints, reset by the last warp to finish)
+  int nranges = 0;
+  int* ctr = nullptr;
 };
 template <typename T>
 acg_status launch_src_stats(const SrcStatsArgs<T>& a, WarpShape ws, int blocks, cudaStream_t s);
