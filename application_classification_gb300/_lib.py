@@ -87,6 +87,9 @@ class Stats(C.Structure):
         ("ms_vertex_phase", C.c_double),
         ("launches", i64),
         ("num_iters", i64),
+        ("edge_warps", i64),
+        ("edge_ranges", i64),
+        ("edge_heavy_vertices", i64),
     ]
 
 

@@ -1024,6 +1024,9 @@ acg_status acg_plan_stats(acg_plan* P, acg_stats* out) {
   out->bytes_iters = (out->bytes_edge_phase + out->bytes_vertex_phase) * P->iters;
   out->launches = P->launches;
   out->num_iters = P->iters;
+  out->edge_warps = (int64_t)P->edge_blocks * 8;
+  out->edge_ranges = P->ew.nparts;
+  out->edge_heavy_vertices = P->ew.nheavy;
   if (P->kernel_timing) {
     double se = 0, sv = 0;
     for (int t = 0; t < P->iters; ++t) {

@@ -119,6 +119,12 @@ typedef struct acg_stats {
   double ms_vertex_phase; /* vertex phases (kernel + statistics), summed */
   int64_t launches;       /* kernels launched by the last acg_match */
   int64_t num_iters;
+  /* The edge phase's work split: launched warps, item ranges (the first
+     edge_warps are the warps' own, the rest are claimed at run time) and
+     vertices split into chunks that reduce through partial rows. */
+  int64_t edge_warps;
+  int64_t edge_ranges;
+  int64_t edge_heavy_vertices;
 } acg_stats;
 
 /* ---------------- data graph ------------------------------------------- */

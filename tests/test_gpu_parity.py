@@ -74,6 +74,49 @@ def test_num_iters(cuda, iters, prec):
     assert np.abs(mu - ref).max() <= tol
 
 
+def _hub_graph(seed=0):
+    """RMAT-14 (16/32 planted pattern) plus one vertex with 6,000 out-edges and
+    6,000 in-edges: its in-edges are split into chunks that reduce through
+    partial rows."""
+    d, p, _ = graph.workload("rmat14_16_32")
+    rng = np.random.default_rng(seed)
+    n = d.num_nodes
+    hub = 7
+    s = np.concatenate([np.asarray(d.srcs, np.int64), np.full(6000, hub), rng.integers(0, n, 6000)])
+    t = np.concatenate([np.asarray(d.dsts, np.int64), rng.integers(0, n, 6000), np.full(6000, hub)])
+    ef = np.concatenate([np.asarray(d.edge_feats), rng.normal(size=(12000, d.edge_feats.shape[1]))])
+    return graph.Graph(np.asarray(d.node_feats), ef, s, t), p
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_claimed_ranges_vs_oracle(cuda, prec):
+    """One resident block per SM gives every warp four times the work, so the
+    edge phase and the source-side pass cut it into several item ranges per
+    warp and claim them at run time (the counter's reset is exercised by the
+    second match); hubs go through chunks and partial rows.  The result matches
+    the oracle and repeats bit for bit."""
+    d, p = _hub_graph()
+    ref = oracle.match(d, p)
+    dg = matcher.DataGraph(d)
+    pl = matcher.Plan(dg, p, prec, edge_blocks_per_sm=1)
+    a = pl.run().cpu().numpy()
+    st = pl.stats()
+    assert st["edge_ranges"] >= 2 * st["edge_warps"] > 0
+    assert st["edge_heavy_vertices"] >= 1
+    b = pl.run().cpu().numpy()
+    assert np.array_equal(a, b)
+    if prec == "fp64":
+        assert np.abs(a - ref).max() <= FP64_REL * max(1.0, np.abs(ref).max())
+        assert _argmax_same(a, ref)
+    else:
+        assert np.abs(a - ref).max() <= MIXED_ABS
+        assert _argmax_same(a, ref, tol=1e-5)
+    # the default launch shape (one range per warp at this size) agrees too
+    c = matcher.Plan(dg, p, prec).run().cpu().numpy()
+    tol = FP64_REL * max(1.0, np.abs(ref).max()) if prec == "fp64" else MIXED_ABS
+    assert np.abs(c - a).max() <= tol
+
+
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_deterministic(cuda, prec):
     """Two matches on one plan are bit-identical (fixed reduction order)."""
