@@ -299,8 +299,8 @@ acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* ou
   ACG_TRY(scan_exclusive_u32(cost, excl, (size_t)nitems, s));
   work_split_kernel<<<ceil_div(nparts + 1, 256), 256, 0, s>>>(excl, cost, nitems, nparts, W.wsplit);
   if (cudaGetLastError() != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "work split launch failed"));
+  dev_free_on(&tmp, s);
   ACG_CUDA_TRY(cudaStreamSynchronize(s));
-  dev_free_all(&tmp);
   return ACG_OK;
 }
 
@@ -921,7 +921,7 @@ acg_status acg_data_create(const acg_graph* g, void* stream, acg_data** out) {
   if (st == ACG_OK && cudaStreamSynchronize(s) != cudaSuccess)
     st = set_error(ACG_ERR_CUDA, "acg_data_create: %s", cudaGetErrorString(cudaGetLastError()));
   if (st != ACG_OK) return fail(st);
-  dev_free_all(&tmp);
+  dev_free_on(&tmp, s);
   *out = D.release();
   return ACG_OK;
 }
@@ -1116,8 +1116,22 @@ acg_status acg_match_graphs_host(const acg_graph* data, const acg_graph* pattern
   double* mu = nullptr;
   if (st == ACG_OK) st = dev_alloc(&tmp, sizeof(double) * n * pattern->num_nodes, (void**)&mu, s);
   if (st == ACG_OK) st = acg_data_create(&dg, s, &D);  // reads the endpoints only
-  if (st == ACG_OK) cuda_ok(cudaStreamWaitEvent(s, ev, 0), "wait");
+  // Mixed precision reads the data features only through their FP32 copies:
+  // those are made on the second stream once the features and the CSRs are
+  // there, while the plan is built on `stream` (the host link, ~210 GB/s, is
+  // the critical path).  FP64 plans wait for the features first.
+  const bool mixed = opt && opt->precision == ACG_PREC_MIXED;
+  if (st == ACG_OK && mixed) {
+    cudaEvent_t csr = nullptr;
+    if (cuda_ok(cudaEventCreateWithFlags(&csr, cudaEventDisableTiming), "event") &&
+        cuda_ok(cudaEventRecord(csr, s), "event record") && cuda_ok(cudaStreamWaitEvent(s2, csr, 0), "wait"))
+      st = ensure_f32(D, s2);
+    if (csr) cudaEventDestroy(csr);
+    cuda_ok(cudaEventRecord(ev, s2), "event record");
+  }
+  if (st == ACG_OK && !mixed) cuda_ok(cudaStreamWaitEvent(s, ev, 0), "wait");
   if (st == ACG_OK) st = acg_plan_create(D, &pg, opt, s, &P);
+  if (st == ACG_OK && mixed) cuda_ok(cudaStreamWaitEvent(s, ev, 0), "wait");
   if (st == ACG_OK) st = acg_match(P, mu, s);
   if (st == ACG_OK && n * pattern->num_nodes > 0)
     cuda_ok(cudaMemcpyAsync(mu_out_host, mu, sizeof(double) * n * pattern->num_nodes,

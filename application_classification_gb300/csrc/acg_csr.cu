@@ -111,6 +111,19 @@ void dev_free_all(std::vector<DevBuf>* owned) {
   owned->clear();
 }
 
+void dev_free_on(std::vector<DevBuf>* owned, cudaStream_t s) {
+  if (owned->empty()) return;
+  if (pool_enabled()) {
+    for (auto& b : *owned)
+      if (b.p) cudaFreeAsync(b.p, s);
+  } else {
+    cudaStreamSynchronize(s);
+    for (auto& b : *owned)
+      if (b.p) cudaFree(b.p);
+  }
+  owned->clear();
+}
+
 // ---------------------------------------------------------------- scan
 namespace {
 

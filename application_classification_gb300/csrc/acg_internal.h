@@ -81,6 +81,9 @@ acg_status build_csr(const uint32_t* key, const uint32_t* other, int n, int m, C
 // Allocate `bytes` (>= 1) of device memory, zero it, record it in `owned`.
 acg_status dev_alloc(std::vector<DevBuf>* owned, size_t bytes, void** out, cudaStream_t s);
 void dev_free_all(std::vector<DevBuf>* owned);
+// Free buffers used only on stream s, in stream order: no device-wide wait, so
+// work on other streams (a feature upload) keeps running.
+void dev_free_on(std::vector<DevBuf>* owned, cudaStream_t s);
 // Return the pools' cached free memory to the driver (acg_release_cached_memory).
 void release_pools();
 
