@@ -7,10 +7,18 @@
 //   vertex's).  The 32 lanes are (edge slot, 16-byte column) pairs: NPOW lanes
 //   cover one [Pp] row, S = 32 / NPOW in-edges are loaded per instruction and
 //   kU instructions are issued back to back, so each warp keeps S * kU pairs of
-//   (streamed dE row, gathered VR' row) in flight.  Each warp walks a
-//   contiguous item range of near-equal cost (load steps plus a per-item
-//   overhead), computed on the host.  A chunk writes a partial row;
+//   (streamed dE row, gathered VR' row) in flight.  The items are cut into
+//   contiguous ranges of near-equal cost (load steps plus a per-item
+//   overhead; built on the device once per data graph), up to 32 per launched
+//   warp: a warp walks its own range, then claims further ranges from a
+//   counter as it finishes, so the SMs stay full until the last ranges.  Every
+//   item is written by exactly one warp, whichever it is, so the result does
+//   not depend on the order of the claims.  A chunk writes a partial row;
 //   heavy_combine_kernel takes the max of a heavy vertex's partial rows.
+//
+// Phase B, vertex_warp_kernel (patterns up to 64 x 64) -- one warp per
+//   contiguous vertex range, rows staged per warp with cp.async; see its own
+//   comment.  The block-tile form below it serves larger patterns.
 //
 // Phase B, vertex_update_kernel -- everything per vertex, streamed with
 //   coalesced 16-byte accesses: FMax, RMax, MU_raw (compensated sum), the next
