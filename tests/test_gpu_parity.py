@@ -117,6 +117,23 @@ def test_claimed_ranges_vs_oracle(cuda, prec):
     assert np.abs(c - a).max() <= tol
 
 
+def test_claimed_ranges_in_batch_graph(cuda):
+    """The batch's CUDA graph replays the claimed-range kernels: every replay
+    starts from a counter the previous launch left at zero, so two runs are
+    bit-identical and each member matches its single-plan result."""
+    d, p = _hub_graph()
+    _, p2, _, _ = graph.plant(d, 5, 8, 0.05, seed=11)
+    dg = matcher.DataGraph(d)
+    b = matcher.Batch(dg, [p, p2], "mixed", edge_blocks_per_sm=1)
+    r1 = [x.cpu().numpy() for x in b.run()]
+    r2 = [x.cpu().numpy() for x in b.run()]
+    for x, y in zip(r1, r2):
+        assert np.array_equal(x, y)
+    for x, pat in zip(r1, (p, p2)):
+        single = matcher.Plan(dg, pat, "mixed", edge_blocks_per_sm=1).run().cpu().numpy()
+        assert np.abs(x - single).max() <= 5e-5
+
+
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_deterministic(cuda, prec):
     """Two matches on one plan are bit-identical (fixed reduction order)."""
