@@ -174,7 +174,8 @@ __global__ void work_items_kernel(const int* __restrict__ off, int n, int chunk,
                                   const uint32_t* __restrict__ ioff, const uint32_t* __restrict__ poff,
                                   const uint32_t* __restrict__ hoff, int4* __restrict__ items,
                                   uint32_t* __restrict__ cost, int* __restrict__ hbase,
-                                  int* __restrict__ hcount, int* __restrict__ hvert) {
+                                  int* __restrict__ hcount, int* __restrict__ hvert,
+                                  int* __restrict__ pheavy) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
   const int b = off[v], e = off[v + 1], deg = e - b;
@@ -189,6 +190,7 @@ __global__ void work_items_kernel(const int* __restrict__ off, int n, int chunk,
     for (int j = 0; j < k; ++j) {
       const int a = b + j * chunk, z = min(e, a + chunk);
       items[i0 + j] = make_int4(v, a, z, p0 + j);
+      pheavy[p0 + j] = h;
       cost[i0 + j] = (uint32_t)((z - a + step - 1) / step + kWorkOver);
     }
   } else {
@@ -288,12 +290,13 @@ acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* ou
   ACG_TRY(dev_alloc(owned, sizeof(int) * std::max(1, nheavy), (void**)&W.hbase, s));
   ACG_TRY(dev_alloc(owned, sizeof(int) * std::max(1, nheavy), (void**)&W.hcount, s));
   ACG_TRY(dev_alloc(owned, sizeof(int) * std::max(1, nheavy), (void**)&W.hvert, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * std::max(1, npartial), (void**)&W.pheavy, s));
   uint32_t *cost = nullptr, *excl = nullptr;  // per item (more items than vertices with hubs)
   st = dev_alloc(&tmp, sizeof(uint32_t) * ((size_t)nitems + 1), (void**)&cost, s);
   if (st == ACG_OK) st = dev_alloc(&tmp, sizeof(uint32_t) * ((size_t)nitems + 1), (void**)&excl, s);
   if (st != ACG_OK) return fail(st);
   work_items_kernel<<<ceil_div(n, 256), 256, 0, s>>>(c.off, n, chunk, step, nit, npart, hub, W.items, cost,
-                                                     W.hbase, W.hcount, W.hvert);
+                                                     W.hbase, W.hcount, W.hvert, W.pheavy);
   if (cudaGetLastError() != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "work items launch failed"));
   // exclusive prefix of the item costs; boundaries
   ACG_TRY(scan_exclusive_u32(cost, excl, (size_t)nitems, s));
@@ -323,7 +326,7 @@ acg_status acg::build_warp_work_host(const Csr& c, int nwarps, int step, WarpWor
   const int chunk = (int)std::min<long long>(1LL << 24, cs * step);
   std::vector<int4> items;
   std::vector<double> cost;
-  std::vector<int> hb, hc, hv;
+  std::vector<int> hb, hc, hv, ph;
   items.reserve((size_t)n / 2 + 16);
   cost.reserve((size_t)n / 2 + 16);
   int npart = 0;
@@ -338,6 +341,7 @@ acg_status acg::build_warp_work_host(const Csr& c, int nwarps, int step, WarpWor
       for (int j = 0; j < k; ++j) {
         const int a = off[v] + j * chunk, b = std::min(off[v + 1], a + chunk);
         items.push_back(make_int4(v, a, b, npart + j));
+        ph.push_back((int)hv.size() - 1);
         cost.push_back((b - a + step - 1) / step + kOver);
       }
       npart += k;
@@ -370,6 +374,7 @@ acg_status acg::build_warp_work_host(const Csr& c, int nwarps, int step, WarpWor
   ACG_TRY(dev_alloc(owned, sizeof(int) * std::max<size_t>(1, hv.size()), (void**)&W.hbase, s));
   ACG_TRY(dev_alloc(owned, sizeof(int) * std::max<size_t>(1, hv.size()), (void**)&W.hcount, s));
   ACG_TRY(dev_alloc(owned, sizeof(int) * std::max<size_t>(1, hv.size()), (void**)&W.hvert, s));
+  ACG_TRY(dev_alloc(owned, sizeof(int) * std::max<size_t>(1, ph.size()), (void**)&W.pheavy, s));
   if (!items.empty())
     ACG_CUDA_TRY(cudaMemcpyAsync(W.items, items.data(), sizeof(int4) * items.size(),
                                  cudaMemcpyHostToDevice, s));
@@ -379,6 +384,7 @@ acg_status acg::build_warp_work_host(const Csr& c, int nwarps, int step, WarpWor
     ACG_CUDA_TRY(cudaMemcpyAsync(W.hbase, hb.data(), sizeof(int) * hb.size(), cudaMemcpyHostToDevice, s));
     ACG_CUDA_TRY(cudaMemcpyAsync(W.hcount, hc.data(), sizeof(int) * hc.size(), cudaMemcpyHostToDevice, s));
     ACG_CUDA_TRY(cudaMemcpyAsync(W.hvert, hv.data(), sizeof(int) * hv.size(), cudaMemcpyHostToDevice, s));
+    ACG_CUDA_TRY(cudaMemcpyAsync(W.pheavy, ph.data(), sizeof(int) * ph.size(), cudaMemcpyHostToDevice, s));
   }
   ACG_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die here
   return ACG_OK;
@@ -397,11 +403,19 @@ acg_status iterate(acg_plan* P, int t, double* mu_out, cudaStream_t s) {
                       (T*)P->part_iter, Pp};
     ea.nranges = P->ew.nparts;
     ea.ctr = P->range_ctr;
+    ea.pheavy = P->ew.pheavy;
+    ea.hbase = P->ew.hbase;
+    ea.hcount = P->ew.hcount;
+    ea.hvert = P->ew.hvert;
+    ea.hcnt = P->heavy_ctr;
     const bool am = P->rec && P->rec->has_am(t - 1);  // record M and its argmax of state t - 1
     if (am) {
       ea.argpos = P->rec->a[t - 1];
       ea.ppos = P->rec->ppos;
     }
+    // FP32 without argmax: the hubs are combined inside the edge kernel
+    const bool inside = sizeof(T) == 4 && !am;
+    if (!inside) ea.hcnt = nullptr;
     ACG_TRY(launch_edge_max<T>(ea, P->ws, P->edge_blocks, s));
     if (am) {
       ACG_TRY(launch_heavy_combine_arg<T>((const T*)P->part_iter, P->rec->ppos, P->ew.hbase,
@@ -409,11 +423,11 @@ acg_status iterate(acg_plan* P, int t, double* mu_out, cudaStream_t s) {
                                           P->rec->a[t - 1], s));
       ACG_CUDA_TRY(cudaMemcpyAsync(P->rec->m[t - 1], P->M, sizeof(T) * (size_t)Dn * Pp,
                                    cudaMemcpyDeviceToDevice, s));
-    } else {
+    } else if (!inside) {
       ACG_TRY(launch_heavy_combine<T>((const T*)P->part_iter, P->ew.hbase, P->ew.hcount,
                                       P->ew.hvert, P->ew.nheavy, Pp, (T*)P->M, s));
     }
-    P->launches += 1 + (P->ew.nheavy > 0);
+    P->launches += 1 + (!inside && P->ew.nheavy > 0);
   }
   if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1) + 1], s);
   VertexUpdArgs<T> va{D->dcsr.off, (const T*)P->M, (T*)P->vf, (T*)P->vr[t & 1],
@@ -732,6 +746,8 @@ acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& 
   st = get_work(D, 0, P->edge_blocks * 8, edge_step(P->ws), &P->ew, s, kEdgeRanges, kEdgeChunkDiv);
   if (st != ACG_OK) return fail(st);
   st = dev_alloc(&P->owned, 2 * sizeof(int), (void**)&P->range_ctr, s);
+  if (st == ACG_OK)
+    st = dev_alloc(&P->owned, sizeof(int) * (size_t)std::max(1, P->ew.nheavy), (void**)&P->heavy_ctr, s);
   if (st != ACG_OK) return fail(st);
   // source-side static pass: one wave of resident blocks over the source CSR
   {

@@ -45,6 +45,7 @@ struct WarpWork {
   int* hbase = nullptr;
   int* hcount = nullptr;
   int* hvert = nullptr;
+  int* pheavy = nullptr;   // [npartial] heavy vertex index of each partial row
   int nheavy = 0, npartial = 0;
 };
 // `step` = positions one warp loads per step of its pass (the cost unit).

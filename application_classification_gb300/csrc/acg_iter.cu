@@ -88,6 +88,20 @@ __host__ __device__ inline size_t a16(size_t b) { return (b + 15) & ~size_t(15);
 #endif
 // ARG: also the first maximal dst-CSR position of each maximum (adjoint
 // recording): ties go to the smaller position.
+// The max of heavy vertex h's cnt partial rows into its M row; one warp, lanes
+// over columns.  The rows were written by other warps of this launch: read
+// through L2.
+template <typename T>
+__device__ __forceinline__ void heavy_finish(const T* partial, T* M, size_t b0, size_t out, int cnt,
+                                             int Pp) {
+  const int lane = threadIdx.x & 31;
+  for (int q = lane; q < Pp; q += 32) {
+    T m = neg_inf<T>();
+    for (int r = 0; r < cnt; ++r) m = fmax(m, __ldcg(partial + b0 + (size_t)r * Pp + q));
+    M[out + q] = m;
+  }
+}
+
 // One range of a warp's items, [it, it_end).
 template <typename T, int NPOW, int NQV, bool ARG>
 __device__ __forceinline__ void edge_max_range(const EdgeMaxArgs<T>& a, int it, const int it_end,
@@ -212,6 +226,24 @@ __device__ __forceinline__ void edge_max_range(const EdgeMaxArgs<T>& a, int it, 
               for (int w = 0; w < W; ++w) prow[qv * W + w] = pos[k * W + w];
             }
           }
+        }
+      }
+      // (FP32 without argmax only: in the other forms the finisher would cost
+      // the edge loop registers, 64 -> 72..94; they keep heavy_combine)
+      if (sizeof(T) == 4 && !ARG && item.w >= 0 && a.hcnt) {
+        // a chunk: its rows are fenced before the count; the warp that
+        // completes the heavy vertex's last chunk fences again and combines
+        __threadfence();
+        __syncwarp();
+        const int h = __ldg(a.pheavy + item.w);
+        const int cnt = __ldg(a.hcount + h);
+        int last = 0;
+        if ((threadIdx.x & 31) == 0) last = atomicAdd(a.hcnt + h, 1) == cnt - 1;
+        if (__shfl_sync(0xffffffffu, last, 0)) {
+          __threadfence();
+          heavy_finish<T>(a.partial, a.M, (size_t)__ldg(a.hbase + h) * Pp,
+                          (size_t)__ldg(a.hvert + h) * Pp, cnt, Pp);
+          if ((threadIdx.x & 31) == 0) a.hcnt[h] = 0;  // ready for the next launch
         }
       }
 #pragma unroll
@@ -1071,6 +1103,7 @@ int edge_max_blocks_per_sm(WarpShape ws) {
   return nb < 1 ? 1 : nb;
 }
 
+
 template <typename T>
 acg_status launch_heavy_combine_arg(const T* partial, const int* ppos, const int* hbase,
                                     const int* hcount, const int* hvert, int nheavy, int Pp, T* M,
@@ -1081,7 +1114,6 @@ acg_status launch_heavy_combine_arg(const T* partial, const int* ppos, const int
   ACG_LAUNCH_CHECK();
   return ACG_OK;
 }
-
 template <typename T>
 acg_status launch_heavy_combine(const T* partial, const int* hbase, const int* hcount,
                                 const int* hvert, int nheavy, int Pp, T* M, cudaStream_t s) {
@@ -1188,10 +1220,10 @@ int vertex_update_blocks_per_sm(int pn, int pe, int pp) {
 
 template acg_status launch_edge_max<double>(const EdgeMaxArgs<double>&, WarpShape, int, cudaStream_t);
 template acg_status launch_edge_max<float>(const EdgeMaxArgs<float>&, WarpShape, int, cudaStream_t);
-template acg_status launch_heavy_combine<double>(const double*, const int*, const int*, const int*, int, int, double*, cudaStream_t);
-template acg_status launch_heavy_combine<float>(const float*, const int*, const int*, const int*, int, int, float*, cudaStream_t);
 template acg_status launch_heavy_combine_arg<double>(const double*, const int*, const int*, const int*, const int*, int, int, double*, int*, cudaStream_t);
 template acg_status launch_heavy_combine_arg<float>(const float*, const int*, const int*, const int*, const int*, int, int, float*, int*, cudaStream_t);
+template acg_status launch_heavy_combine<double>(const double*, const int*, const int*, const int*, int, int, double*, cudaStream_t);
+template acg_status launch_heavy_combine<float>(const float*, const int*, const int*, const int*, int, int, float*, cudaStream_t);
 template acg_status launch_vertex_update<double>(const VertexUpdArgs<double>&, int, cudaStream_t);
 template acg_status launch_vertex_update<float>(const VertexUpdArgs<float>&, int, cudaStream_t);
 template int edge_max_blocks_per_sm<double>(WarpShape);

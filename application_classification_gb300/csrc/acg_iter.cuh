@@ -31,6 +31,15 @@ struct EdgeMaxArgs {
   // both.  Without it nranges must equal the launched warps.
   int nranges = 0;
   int* ctr = nullptr;
+  // Heavy vertices combined in the kernel (FP32 without argmax, with hcnt,
+  // [nheavy] zeroed counters): the warp that completes a heavy vertex's last
+  // chunk takes the max of its partial rows into M and resets the counter.
+  // Otherwise heavy_combine(_arg)_kernel does it after the launch.
+  const int* pheavy = nullptr;  // [npartial] heavy index of each partial row
+  const int* hbase = nullptr;
+  const int* hcount = nullptr;
+  const int* hvert = nullptr;
+  int* hcnt = nullptr;
 };
 
 // Column statistics of one iteration (FP64), double-buffered across iterations:

@@ -119,6 +119,7 @@ struct acg_plan {
   int64_t launches = 0;
   bool ran = false;
   bool cdist_tc = false;       // edge cost matrix on the tensor cores
+  int* heavy_ctr = nullptr;    // [nheavy] chunks of each heavy vertex done in this edge phase
   int* range_ctr = nullptr;    // [2] range claims and finished warps of the range-split
                                // kernels (one at a time on the plan's stream; each
                                // launch leaves both at zero)
