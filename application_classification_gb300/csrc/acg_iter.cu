@@ -323,18 +323,35 @@ heavy_combine_arg_kernel(const T* __restrict__ partial, const int* __restrict__ 
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= nheavy) return;
+  const size_t b0 = (size_t)hbase[warp] * Pp, out = (size_t)hvert[warp] * Pp;
+  const int cnt = hcount[warp];
   for (int q = lane; q < Pp; q += 32) {
     T m = neg_inf<T>();
     int bi = -1;
-    for (int c = 0; c < hcount[warp]; ++c) {
-      const size_t r = (size_t)(hbase[warp] + c) * Pp + q;
-      if (ppos[r] >= 0 && (bi < 0 || partial[r] > m)) {
-        m = partial[r];
-        bi = ppos[r];
+    auto take = [&](T x, int px) {
+      if (px >= 0 && (bi < 0 || x > m)) {
+        m = x;
+        bi = px;
       }
+    };
+    int c = 0;
+    for (; c + 4 <= cnt; c += 4) {  // four rows in flight, applied in order
+      const size_t r = b0 + (size_t)c * Pp + q;
+      const T x0 = partial[r], x1 = partial[r + Pp], x2 = partial[r + 2 * (size_t)Pp],
+              x3 = partial[r + 3 * (size_t)Pp];
+      const int p0 = ppos[r], p1 = ppos[r + Pp], p2 = ppos[r + 2 * (size_t)Pp],
+                p3 = ppos[r + 3 * (size_t)Pp];
+      take(x0, p0);
+      take(x1, p1);
+      take(x2, p2);
+      take(x3, p3);
     }
-    M[(size_t)hvert[warp] * Pp + q] = m;
-    A[(size_t)hvert[warp] * Pp + q] = bi;
+    for (; c < cnt; ++c) {
+      const size_t r = b0 + (size_t)c * Pp + q;
+      take(partial[r], ppos[r]);
+    }
+    M[out + q] = m;
+    A[out + q] = bi;
   }
 }
 
