@@ -250,7 +250,9 @@ struct ScatArgs {
   T* gVRe;
   T* part;
   int Pp, Pe;
-  int nranges;         // item ranges; warp w does ranges w, w + warps, ...
+  int nranges;         // item ranges: warp w does range w, then claims from ctr
+  int* ctr;            // (two zeroed ints, reset by the last warp; null: ranges
+                       // w, w + warps, ...)
 };
 
 template <typename T, int NPOW, int NQV>
@@ -259,7 +261,9 @@ __global__ void ACG_ADJ_BOUNDS adj_scatter_kernel(const ScatArgs<T> a) {
   const int Pp = a.Pp, Pe = a.Pe, lane = threadIdx.x & 31, slot = lane / NPOW, qc = lane % NPOW;
   const int gw = (blockIdx.x * kT + threadIdx.x) >> 5;
   const int nw = (int)gridDim.x * (kT / 32);
-  for (int r = gw; r < a.nranges; r += nw)
+  for (int r = gw; r < a.nranges;) {
+  int rn = r + nw;  // the next range: claimed (in flight while this one runs) or strided
+  if (a.ctr && lane == 0) rn = nw + atomicAdd(a.ctr, 1);
   for (int it = a.wsplit[r]; it < a.wsplit[r + 1]; ++it) {
     const int4 item = a.items[it];
     T acc[NQ];
@@ -306,6 +310,15 @@ __global__ void ACG_ADJ_BOUNDS adj_scatter_kernel(const ScatArgs<T> a) {
         }
     }
     __syncwarp();
+  }
+  r = a.ctr ? __shfl_sync(0xffffffffu, rn, 0) : rn;
+  }
+  if (a.ctr && lane == 0) {
+    __threadfence();  // this warp's claims come before its finish count
+    if (atomicAdd(a.ctr + 1, 1) == nw - 1) {  // every warp has made its last claim
+      a.ctr[0] = 0;
+      a.ctr[1] = 0;
+    }
   }
 }
 
@@ -1220,7 +1233,7 @@ struct Adj {
 
   acg_status scatter() {
     ScatArgs<T> a{P->sw.items, P->sw.wsplit, D->pos_in_dst, D->scsr.other, W->emask, (const T*)W->gM,
-                  (T*)W->gVRe, (T*)W->pscat, Pp, Pe, P->sw.nparts};
+                  (T*)W->gVRe, (T*)W->pscat, Pp, Pe, P->sw.nparts, P->range_ctr};
     ACG_TRY(fill(W->gVRe, vrow(), T(0)));  // sources without out-edges
     bool done = false;
 #define ADJ_SC(NP_, NQ_)                                                        \
