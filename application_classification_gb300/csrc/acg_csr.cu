@@ -352,9 +352,18 @@ acg_status build_csr(const uint32_t* key, const uint32_t* other, int n, int m, C
   ACG_TRY(dev_alloc(owned, sizeof(int) * (size_t)m, (void**)&out->other, s));
   const size_t mm = m > 0 ? (size_t)m : 1;
   uint32_t *k = nullptr, *k2 = nullptr, *v2 = nullptr;
-  ACG_CUDA_TRY(scratch_alloc((void**)&k, mm * sizeof(uint32_t), s));
-  ACG_CUDA_TRY(scratch_alloc((void**)&k2, mm * sizeof(uint32_t), s));
-  ACG_CUDA_TRY(scratch_alloc((void**)&v2, mm * sizeof(uint32_t), s));
+  {
+    cudaError_t e = scratch_alloc((void**)&k, mm * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = scratch_alloc((void**)&k2, mm * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = scratch_alloc((void**)&v2, mm * sizeof(uint32_t), s);
+    if (e != cudaSuccess) {  // free what was taken; the CSR's own buffers are in `owned`
+      cudaGetLastError();
+      for (uint32_t* p : {k, k2, v2})
+        if (p) scratch_free(p, s);
+      return set_error(ACG_ERR_OUT_OF_MEMORY, "build_csr: scratch of %zu bytes: %s",
+                       mm * sizeof(uint32_t), cudaGetErrorString(e));
+    }
+  }
   acg_status st = ACG_OK;
   uint32_t* vals = reinterpret_cast<uint32_t*>(out->eid);
   if (m > 0) {
