@@ -204,13 +204,15 @@ def ncu_traffic(workload: str, precision: str):
 
 # ----------------------------------------------------------- CPU baseline
 def cpu_sample(workload: str, threads: int | None = None):
-    """Time the CPU oracle on the bounded sample; returns (ms per full match, info)."""
-    from application_classification_gb300 import graph
+    """Time the CPU oracle on the bounded sample; returns (ms per full match, info).
+
+    The sample graph comes from the oracle's own generator (the same bytes as
+    the product's), so this leg never loads the product library."""
     from oracle import oracle
 
     full = _work_units(workload)
     sample = workload_info(workload)[1]
-    d, p, _ = graph.workload(sample)
+    d, p, _ = oracle.workload(sample)
     nt = threads or os.cpu_count() or 1
     _, el_us = oracle.match(d, p, threads=nt, return_elapsed=True)
     units = _units(d.num_nodes, d.num_edges, p.num_nodes, p.num_edges)
@@ -218,8 +220,24 @@ def cpu_sample(workload: str, threads: int | None = None):
     info = {"sample": f"{sample}: {d.num_nodes} vertices / {d.num_edges} edges, pattern "
                       f"{p.num_nodes}/{p.num_edges}; {el_us/1e6:.2f} s measured, scaled by "
                       f"(De+Dn)*Pe*(Pn+1) to the full workload (x{full/units:.1f})",
-            "cores": nt, "sample_s": el_us / 1e6}
+            "cores": nt, "sample_s": el_us / 1e6, "sample_ms_per_unit": el_us / 1e3 / units}
     return ms, info
+
+
+def cpu_validation(ms_per_unit: float, threads: int, name: str = "rmat18"):
+    """One measured oracle match of a larger workload (R-MAT 18, 16/32 pattern:
+    the reference's GPU configuration) beside the sample model's prediction for
+    it, so the extrapolation from the sample is checked, not assumed."""
+    from oracle import oracle
+
+    d, p, _ = oracle.workload(name)
+    _, el_us = oracle.match(d, p, threads=threads, return_elapsed=True)
+    pred = ms_per_unit * _units(d.num_nodes, d.num_edges, p.num_nodes, p.num_edges)
+    meas = el_us / 1e3
+    return {"workload": f"{name}: {d.num_nodes} vertices / {d.num_edges} edges, pattern "
+                        f"{p.num_nodes}/{p.num_edges}",
+            "measured_ms": round(meas, 1), "predicted_ms": round(pred, 1),
+            "model_error": round(pred / meas - 1.0, 3)}
 
 
 def _units(dn, de, pn, pe):
@@ -232,8 +250,8 @@ _SHAPES = {"rmat22": (4194304, 65242331, 32, 64), "rmat18": (262144, 3939126, 16
 
 def _work_units(workload):
     if workload not in _SHAPES:
-        from application_classification_gb300 import graph
-        d, p, _ = graph.workload(workload)
+        from oracle import oracle
+        d, p, _ = oracle.workload(workload)
         _SHAPES[workload] = (d.num_nodes, d.num_edges, p.num_nodes, p.num_edges)
     dn, de, pn, pe = _SHAPES[workload]
     return _units(dn, de, pn, pe)
@@ -411,7 +429,9 @@ def run_ours(args, ws, rank, local):
     if rank == 0 and ws == 1 and not args.no_cpu:
         ms, info = cpu_sample(args.workload)
         result["cpu_baseline"] = {"value": round(ms, 1), "unit": "ms", "cores": info["cores"],
-                                  "kind": "port", "sample": info["sample"]}
+                                  "kind": "port", "sample": info["sample"],
+                                  "validation": cpu_validation(info["sample_ms_per_unit"],
+                                                               info["cores"])}
     if rank == 0:
         print(json.dumps(result), flush=True)
 
@@ -421,12 +441,11 @@ def run_reference(args, ws, rank):
     """The CPU oracle (restatement of the reference program) on a bounded sample."""
     if rank != 0:
         return
-    from application_classification_gb300 import graph
     from oracle import oracle
 
     full = _work_units(args.workload)
     sample = workload_info(args.workload)[1]
-    d, p, _ = graph.workload(sample)
+    d, p, _ = oracle.workload(sample)  # the oracle's generator: no product library here
     nt = os.cpu_count() or 1
     units = _units(d.num_nodes, d.num_edges, p.num_nodes, p.num_edges)
     for _ in range(args.warmup):
@@ -439,6 +458,7 @@ def run_reference(args, ws, rank):
     wall = time.time() - t0
     ms_sample = sum(els) / len(els)
     value = ms_sample * full / units
+    validation = cpu_validation(ms_sample / units, nt)
     print(json.dumps({
         "impl": "reference",
         "metric": "match ms (one whole ApplicationClassification match, "
@@ -451,7 +471,8 @@ def run_reference(args, ws, rank):
         "cpu_baseline": {"value": round(value, 1), "unit": "ms", "cores": nt, "kind": "port",
                          "sample": f"{sample}: {d.num_nodes} vertices / {d.num_edges} edges, "
                                    f"pattern {p.num_nodes}/{p.num_edges}, {ms_sample/1e3:.2f} s per "
-                                   f"sample match, scaled by (De+Dn)*Pe*(Pn+1) x{full/units:.1f}"},
+                                   f"sample match, scaled by (De+Dn)*Pe*(Pn+1) x{full/units:.1f}",
+                         "validation": validation},
         "e2e": {"value": round(value, 1), "unit": "ms", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "wall_s": round(wall, 1),
