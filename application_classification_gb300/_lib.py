@@ -71,7 +71,8 @@ class HostGraph(C.Structure):
 class Options(C.Structure):
     _fields_ = [("precision", i32), ("num_iters", i32), ("kernel_timing", i32),
                 ("edge_blocks_per_sm", i32), ("vertex_blocks_per_sm", i32),
-                ("cnull", i32), ("cdist_kernel", i32), ("autotune", i32)]
+                ("cnull", i32), ("cdist_kernel", i32), ("autotune", i32),
+                ("edge_kernel", i32)]
 
 
 class Stats(C.Structure):

@@ -397,6 +397,16 @@ acg_status iterate(acg_plan* P, int t, double* mu_out, cudaStream_t s) {
   acg_data* D = P->data;
   const int Dn = D->Dn, Pn = P->Pn, Pe = P->Pe, Pp = P->Pp;
   if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1)], s);
+  if constexpr (std::is_same_v<T, float>) {
+    if (Pe > 0 && P->edge_tc && !P->rec) {  // costs recomputed on the tensor cores
+      EdgeTcArgs ta{D->ef32, P->pe, D->dcsr.other, D->dst_of, D->dcsr.off,
+                    (const float*)P->vr[(t - 1) & 1], (float*)P->M, P->et_H, P->et_T, P->et_cnt,
+                    P->dev_err, (long long)D->De, D->Ke, D->ke32, Pe, Pp, P->et_tpc};
+      ACG_TRY(launch_edge_tc(ta, D->num_sms, s));
+      P->launches += 1;
+      goto vertex_phase;
+    }
+  }
   if (Pe > 0) {
     EdgeMaxArgs<T> ea{P->ew.items, P->ew.nitems, P->ew.wsplit, D->dcsr.other,
                       (const T*)P->dE, (const T*)P->vr[(t - 1) & 1], (T*)P->M,
@@ -429,6 +439,7 @@ acg_status iterate(acg_plan* P, int t, double* mu_out, cudaStream_t s) {
     }
     P->launches += 1 + (!inside && P->ew.nheavy > 0);
   }
+vertex_phase:
   if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1) + 1], s);
   VertexUpdArgs<T> va{D->dcsr.off, (const T*)P->M, (T*)P->vf, (T*)P->vr[t & 1],
                       (const T*)P->dEmin, (const T*)P->B, (const T*)P->CV,
@@ -633,6 +644,8 @@ acg_status resolve_options(const acg_options* opt, acg_options* o) {
     return set_error(ACG_ERR_INVALID_ARGUMENT, "autotune must be 0 or 1 (got %d)", o->autotune);
   if (o->cdist_kernel < 0 || o->cdist_kernel > 2)
     return set_error(ACG_ERR_INVALID_ARGUMENT, "cdist_kernel must be 0, 1 or 2 (got %d)", o->cdist_kernel);
+  if (o->edge_kernel < 0 || o->edge_kernel > 2)
+    return set_error(ACG_ERR_INVALID_ARGUMENT, "edge_kernel must be 0, 1 or 2 (got %d)", o->edge_kernel);
   return ACG_OK;
 }
 
@@ -713,6 +726,29 @@ acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& 
       dev_free_all(&P->owned);
       return set_error(ACG_ERR_UNSUPPORTED,
                        "tensor-core cdist: edge feature dim %d, %d pattern edges", D->Ke, Pe);
+    }
+  }
+  // the edge phase recomputing the costs (single plans with the tensor-core
+  // edge cost matrix; a batch shares workspaces and keeps the stored matrix)
+  if (P->prec == ACG_PREC_MIXED && o.edge_kernel == 2) {
+    P->edge_tc = !deferred && P->cdist_tc && Pe > 0 && De > 0 &&
+                 edge_tc_eligible(D->Ke, (D->Ke + 3) / 4 * 4, Pe, Pp);
+    if (!P->edge_tc && o.edge_kernel == 2) {
+      dev_free_all(&P->owned);
+      return set_error(ACG_ERR_UNSUPPORTED,
+                       "edge phase on the tensor cores: edge feature dim %d, %d pattern edges%s", D->Ke,
+                       Pe, deferred ? " (batch)" : "");
+    }
+  }
+  if (P->edge_tc) {
+    P->et_tpc = edge_tc_tiles_per_chunk(De, D->num_sms);
+    const size_t nch = (size_t)edge_tc_chunks(De, P->et_tpc);
+    alloc(sizeof(float) * nch * Pp, (void**)&P->et_H);
+    alloc(sizeof(float) * nch * Pp, (void**)&P->et_T);
+    alloc(sizeof(int) * nch, (void**)&P->et_cnt);
+    if (st == ACG_OK && !D->dst_of) {
+      st = dev_alloc(&D->owned, sizeof(int) * (size_t)De, (void**)&D->dst_of, s);
+      if (st == ACG_OK) st = launch_csr_rows(D->dcsr.off, Dn, D->dst_of, s);
     }
   }
   if (o.cnull) {
@@ -1036,6 +1072,8 @@ acg_status acg_plan_stats(acg_plan* P, acg_stats* out) {
   // mixed precision) read, Y and Z written, the in-degree offsets.
   const double cvb = P->prec == ACG_PREC_MIXED ? 2.0 * eb : eb;
   out->bytes_edge_phase = De * (Pe * eb + 4.0) + 2.0 * Dn * Pe * eb + (double)P->ew.nitems * 16.0;
+  if (P->edge_tc)  // costs recomputed: per in-edge its FP32 features, source and destination
+    out->bytes_edge_phase = De * (P->data->Ke * 4.0 + 8.0) + 2.0 * Dn * Pe * eb;
   out->bytes_vertex_phase = Dn * (4.0 * Pe * eb + Pn * cvb + 2.0 * Pe * eb + 4.0);
   out->bytes_iters = (out->bytes_edge_phase + out->bytes_vertex_phase) * P->iters;
   out->launches = P->launches;

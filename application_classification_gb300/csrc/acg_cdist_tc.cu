@@ -33,14 +33,16 @@
 
 #include "acg_cdist.cuh"
 #include "acg_device.cuh"
+#include "acg_tc.cuh"
 
 namespace acg {
 
 namespace {
 
+using namespace tc;
+
 constexpr int kTT = 256;               // threads per CTA
 constexpr int kTM = 128;               // data rows per tile (the MMA's M)
-constexpr long long kSpin = 1LL << 22;  // try_wait rounds before a wait gives up
 #ifndef ACG_TC_NEAR
 #define ACG_TC_NEAR 8.0f
 #endif
@@ -51,7 +53,6 @@ constexpr int kStg = 20;  // staging row stride (floats): 16 columns + 16 bytes 
 struct TcLayout {
   uint32_t a, b, x0, x1, y, nx, ny, mean, bar, tslot, total;
 };
-__host__ __device__ inline uint32_t al128(uint32_t v) { return (v + 127u) & ~127u; }
 __host__ __device__ inline TcLayout tc_layout(int K, int kstride, int Pp, int N) {
   TcLayout L;
   (void)K;
@@ -73,91 +74,6 @@ __host__ __device__ inline TcLayout tc_layout(int K, int kstride, int Pp, int N)
   L.total = o;
   return L;
 }
-
-// Byte offset of element (row, k) of a K-major operand with `rows` rows in the
-// no-swizzle canonical layout: core matrices of 8 rows x 16 bytes (4 TF32),
-// stored [k / 4][row / 8][row % 8][k % 4].  Adjacent core matrices along K are
-// rows/8 * 128 bytes apart (the descriptor's leading byte offset), along M/N
-// 128 bytes apart (its stride byte offset).
-__device__ __forceinline__ uint32_t kmaj_off(int row, int k, int rows) {
-  return (uint32_t)(((k >> 2) * (rows >> 3) + (row >> 3)) * 128 + (row & 7) * 16 + (k & 3) * 4);
-}
-
-// Shared-memory matrix descriptor: start, leading and stride byte offsets
-// (>> 4), descriptor version 1 (bits 46-47), base offset 0, no swizzle.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
-         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
-}
-
-// Instruction descriptor of kind::tf32: D FP32 (bits 4-5 = 1), A and B TF32
-// (bits 7-9, 10-12 = 2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
-__host__ __device__ inline uint32_t idesc_tf32(int M, int N) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ float tf32_round(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (long long i = 0; i < kSpin; ++i) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-// Bulk copy global -> shared completing on `bar` (which expects `bytes`).
-__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-      "l"(src), "r"(bytes), "r"(bar)
-      : "memory");
-}
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, int acc) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-      : "memory");
-}
-__device__ __forceinline__ void tc_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-               : "memory");
-}
-// 16 consecutive TMEM columns of this warp's 32 lanes (no wait).
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&v)[16]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-      "[%16];"
-      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-        "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-        "=r"(v[15])
-      : "r"(taddr)
-      : "memory");
-}
-__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 struct TcArgs {
   const float* x;   // [nrows][KM] FP32 features (zero past K), in output row order
@@ -196,11 +112,8 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sb + L.tslot),
-                 "r"(a.tcols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    tc_fence_before();
+    tmem_alloc(sb + L.tslot, (uint32_t)a.tcols);
+    fence_before();
   }
   // the centre m (mean pattern feature vector, zero past K) and the FP32
   // pattern rows for the exact recompute
@@ -240,7 +153,7 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
   for (int i = tid; i < kTM * KP; i += kTT) sA[i] = 0.f;
   for (int r = tid; r < kTM; r += kTT) snx[r] = 0.f;
   __syncthreads();
-  tc_fence_after();
+  fence_after();
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + L.tslot);
 
   const uint32_t lboA = (kTM / 8) * 128, lboB = (uint32_t)(N / 8) * 128, sbo = 128;
@@ -315,22 +228,22 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
       }
     }
     fence_proxy_async();  // the generic-proxy writes of A' before the MMA reads them
-    tc_fence_before();
+    fence_before();
     __syncthreads();
     if (tid == 0) {
-      tc_fence_after();
+      fence_after();
 #pragma unroll
       for (int st = 0; st < KP / 8; ++st)
-        tc_mma(tmem, smem_desc(sb + L.a + (uint32_t)st * 2 * lboA, lboA, sbo),
+        mma_tf32(tmem, smem_desc(sb + L.a + (uint32_t)st * 2 * lboA, lboA, sbo),
                smem_desc(sb + L.b + (uint32_t)st * 2 * lboB, lboB, sbo), idesc, st > 0);
-      tc_commit(bar[2]);
+      commit(bar[2]);
     }
     pend_mma = true;
     ok = mbar_wait(bar[2], ph[2]);
     if (!__syncthreads_and(ok)) break;
     ph[2] ^= 1u;
     pend_mma = false;
-    tc_fence_after();
+    fence_after();
     // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows) and the
     // 16-column chunks c = w / 4, w / 4 + 2, ...; each chunk goes through the
     // warp's own staging rows (in A', idle until the next split) so that a
@@ -385,12 +298,12 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
       };
       for (int c = warp >> 2; c < N / 16; c += 2) {
         uint32_t v[16];
-        tc_ld16(tmem + ((uint32_t)rw << 16) + (uint32_t)c * 16, v);
-        tc_wait_ld();
+        ld16(tmem + ((uint32_t)rw << 16) + (uint32_t)c * 16, v);
+        wait_ld();
         emit(c, v);
       }
     }
-    tc_fence_before();
+    fence_before();
     __syncthreads();  // TMEM read, this x buffer free
   }
   if (!ok) {
@@ -400,12 +313,11 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
       if (pend[i]) mbar_wait(bar[i], ph[i]);
     if (pend_mma) mbar_wait(bar[2], ph[2]);
   }
-  tc_fence_before();
+  fence_before();
   __syncthreads();
   if (warp == 0) {
-    tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tcols)
-                 : "memory");
+    fence_after();
+    tmem_dealloc(tmem, (uint32_t)a.tcols);
   }
 }
 

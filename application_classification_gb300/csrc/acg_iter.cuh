@@ -85,6 +85,37 @@ struct VertexUpdArgs {
 acg_status launch_capture_s(const double* S, const int* iters_p, int t, double* S_final, int Pn,
                             cudaStream_t s);
 
+// Edge phase of FP32 plans with the costs recomputed on the tensor cores
+// (acg_edge_tc.cu): M[v][q] = max over in-edges e of z[s_e][q] - ||x_e - y_q||,
+// d formed as the tensor-core edge cost matrix forms it.
+struct EdgeTcArgs {
+  const float* x;      // [De][KM] FP32 edge features in dst-CSR order (zero past K)
+  const double* y;     // [P][K] pattern edge features
+  const int* src_of;   // [De] source vertex of each dst-CSR position
+  const int* dst_of;   // [De] destination vertex of each dst-CSR position
+  const int* off;      // [Dn + 1] dst-CSR offsets
+  const float* z;      // [Dn][Pp] gathered by source
+  float* M;            // [Dn][Pp] out (rows of vertices without in-edges untouched)
+  float* H;            // [nchunks][Pp] partial rows: head / through pieces of a chunk
+  float* T;            // [nchunks][Pp] partial rows: tail pieces
+  int* cnt;            // [nchunks] arrival counts, zero before and after a launch
+  int* err;            // set to 1 when a bounded wait gave up
+  long long De;
+  int K, KM, P, Pp;
+  int tpc;             // tiles of 128 in-edges per chunk
+  // set by launch_edge_tc
+  int N = 0, tcols = 0, ntiles = 0, nchunks = 0;
+};
+bool edge_tc_eligible(int K, int kstride, int P, int Pp);
+size_t edge_tc_smem(int kstride, int Pp);
+int edge_tc_tiles_per_chunk(long long De, int num_sms);
+inline int edge_tc_chunks(long long De, int tpc) {
+  return (int)(((De + 127) / 128 + tpc - 1) / tpc);
+}
+acg_status launch_edge_tc(const EdgeTcArgs& a, int num_sms, cudaStream_t s);
+// dst_of[i] = v for every position i in [off[v], off[v+1]).
+acg_status launch_csr_rows(const int* off, int n, int* dst_of, cudaStream_t s);
+
 struct WarpShape {
   int npow;  // lanes covering one [Pp] row (power of two <= 32)
   int nqv;   // 16-byte vectors per lane per row

@@ -35,6 +35,7 @@ struct acg_data {
   float* nf32 = nullptr;
   float* ef32 = nullptr;
   int ke32 = 0;
+  int* dst_of = nullptr;      // [De] destination of each dst-CSR position (built on first use)
   // warp work splits, shared by every plan on this graph: key = (0 dst / 1 src
   // CSR, warps, positions per step)
   std::map<std::tuple<int, int, int, int, int>, acg::WarpWork> work;
@@ -119,6 +120,11 @@ struct acg_plan {
   int64_t launches = 0;
   bool ran = false;
   bool cdist_tc = false;       // edge cost matrix on the tensor cores
+  bool edge_tc = false;        // edge phase recomputes the costs on the tensor cores
+  int et_tpc = 0;              // its tiles per chunk, chunk pieces and counts
+  float* et_H = nullptr;
+  float* et_T = nullptr;
+  int* et_cnt = nullptr;
   int* heavy_ctr = nullptr;    // [nheavy] chunks of each heavy vertex done in this edge phase
   int* range_ctr = nullptr;    // [2] range claims and finished warps of the range-split
                                // kernels (one at a time on the plan's stream; each

@@ -25,6 +25,9 @@ from .graph import Graph
 PRECISIONS = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
 # acg_options.cdist_kernel: the mixed path's edge cost matrix
 CDIST_KERNELS = {"auto": 0, "simt": 1, "tensor": 2}
+# acg_options.edge_kernel: the mixed path's edge phase (costs recomputed on the
+# tensor cores, or read from the stored edge cost matrix)
+EDGE_KERNELS = {"auto": 0, "stored": 1, "fused": 2}
 
 
 def _torch():
@@ -111,7 +114,8 @@ class Plan:
 
     def __init__(self, data: DataGraph, pattern, precision: str = "fp64", num_iters: int = -1,
                  stream=None, kernel_timing: bool = False, edge_blocks_per_sm: int = 0,
-                 vertex_blocks_per_sm: int = 0, cnull: bool = False, cdist_kernel: str = "auto"):
+                 vertex_blocks_per_sm: int = 0, cnull: bool = False, cdist_kernel: str = "auto",
+                 edge_kernel: str = "auto"):
         self.data = data
         self.pat = pattern if isinstance(pattern, DeviceGraph) else DeviceGraph(pattern)
         self._c = self.pat.c_graph()
@@ -126,6 +130,7 @@ class Plan:
         opt.vertex_blocks_per_sm = int(vertex_blocks_per_sm)
         opt.cnull = 1 if cnull else 0
         opt.cdist_kernel = CDIST_KERNELS[cdist_kernel]
+        opt.edge_kernel = EDGE_KERNELS[edge_kernel]
         self.precision = precision
         self.handle = C.c_void_p()
         _lib.check(_lib.lib().acg_plan_create(data.handle, C.byref(self._c), C.byref(opt),

@@ -93,6 +93,16 @@ typedef struct acg_options {
   int32_t autotune;   /* acg_batch_create only: 1 = measure before grouping
                          (see acg_batch_create); 0 (default) = greedy packing
                          with the default launch shapes */
+  int32_t edge_kernel; /* the edge phase of the mixed-precision iterations:
+                          0 (default) and 1 read the stored edge cost matrix;
+                          2 recompute each in-edge's costs on the tensor cores
+                          inside the phase (acg_edge_tc.cu: the arithmetic of
+                          the stored matrix, so the same values, without
+                          reading it) or ACG_ERR_UNSUPPORTED when the shape
+                          does not allow it (plans with the tensor-core edge
+                          cost matrix, edge feature dim <= 24, <= 64 padded
+                          pattern edges).  FP64 plans, batches and recorded
+                          matches (acg_match_record) read the stored matrix. */
 } acg_options;
 
 /* Fill `opt` with the defaults (FP64, num_iters = -1). */

@@ -129,7 +129,8 @@ def test_claimed_ranges_vs_oracle(cuda, prec):
     d, p = _hub_graph()
     ref = oracle.match(d, p)
     dg = matcher.DataGraph(d)
-    pl = matcher.Plan(dg, p, prec, edge_blocks_per_sm=1)
+    kern = {"edge_kernel": "stored"} if prec == "mixed" else {}
+    pl = matcher.Plan(dg, p, prec, edge_blocks_per_sm=1, **kern)
     a = pl.run().cpu().numpy()
     st = pl.stats()
     assert st["edge_ranges"] >= 2 * st["edge_warps"] > 0
@@ -143,7 +144,7 @@ def test_claimed_ranges_vs_oracle(cuda, prec):
         assert np.abs(a - ref).max() <= MIXED_ABS
         assert _argmax_same(a, ref, tol=1e-5)
     # the default launch shape (one range per warp at this size) agrees too
-    c = matcher.Plan(dg, p, prec).run().cpu().numpy()
+    c = matcher.Plan(dg, p, prec, **kern).run().cpu().numpy()
     tol = FP64_REL * max(1.0, np.abs(ref).max()) if prec == "fp64" else MIXED_ABS
     assert np.abs(c - a).max() <= tol
 
