@@ -127,6 +127,8 @@ SIGNATURES: dict[str, tuple] = {
     "acg_match_graphs": (i32, [_P(Graph), _P(Graph), _P(Options), vp, vp]),
     "acg_match_graphs_host": (i32, [_P(Graph), _P(Graph), _P(Options), vp, vp]),
     "acg_release_cached_memory": (i32, []),
+    "acg_inject_alloc_failure": (i32, [i64]),
+    "acg_device_memory_in_use": (i32, [_P(i64)]),
     "acg_initial_mu_noalloc": (i32, [vp, u64, u64, vp, u64, vp, vp]),
     "acg_batch_create": (i32, [vp, vp, i32, _P(Options), vp, _P(vp)]),
     "acg_batch_match": (i32, [vp, vp, vp]),

@@ -173,7 +173,7 @@ __global__ void work_count_kernel(const int* __restrict__ off, int n, int chunk,
 __global__ void work_items_kernel(const int* __restrict__ off, int n, int chunk, int step,
                                   const uint32_t* __restrict__ ioff, const uint32_t* __restrict__ poff,
                                   const uint32_t* __restrict__ hoff, int4* __restrict__ items,
-                                  uint32_t* __restrict__ cost, int* __restrict__ hbase,
+                                  unsigned long long* __restrict__ cost, int* __restrict__ hbase,
                                   int* __restrict__ hcount, int* __restrict__ hvert,
                                   int* __restrict__ pheavy) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
@@ -191,19 +191,20 @@ __global__ void work_items_kernel(const int* __restrict__ off, int n, int chunk,
       const int a = b + j * chunk, z = min(e, a + chunk);
       items[i0 + j] = make_int4(v, a, z, p0 + j);
       pheavy[p0 + j] = h;
-      cost[i0 + j] = (uint32_t)((z - a + step - 1) / step + kWorkOver);
+      cost[i0 + j] = (unsigned long long)((z - a + step - 1) / step + kWorkOver);
     }
   } else {
     items[i0] = make_int4(v, b, e, -1);
-    cost[i0] = (uint32_t)((deg + step - 1) / step + kWorkOver);
+    cost[i0] = (unsigned long long)((deg + step - 1) / step + kWorkOver);
   }
 }
 
 // split[w] (0 < w < nwarps) = 1 + the first item whose inclusive cost prefix
 // reaches target * w (nitems if none), target = the items' total cost / nwarps;
 // split[0] = 0, split[nwarps] = nitems.
-__global__ void work_split_kernel(const uint32_t* __restrict__ excl, const uint32_t* __restrict__ cost,
-                                  int nitems, int nwarps, int* __restrict__ split) {
+__global__ void work_split_kernel(const unsigned long long* __restrict__ excl,
+                                  const unsigned long long* __restrict__ cost, int nitems, int nwarps,
+                                  int* __restrict__ split) {
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w > nwarps) return;
   if (w == 0) {
@@ -233,15 +234,33 @@ __global__ void work_split_kernel(const uint32_t* __restrict__ excl, const uint3
 
 // The work split, built on the device: per-vertex costs and their total give
 // the chunk size; per-vertex item counts, scanned, place the items (vertex
-// order, chunks in order) and the hub records; a binary search of the scanned
-// item costs gives each warp boundary.  The same items and boundaries as
-// build_warp_work_host, without copying the offsets to the host.
+// order, chunks in order) and the hub records; a binary search of the 64-bit
+// scanned item costs gives each part's boundary.  Items of a vertex are its
+// in-edge positions (one item), or chunks of `chunk` positions for a heavy
+// vertex; a part is a run of items of near-equal total cost.
 acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* out,
                                 std::vector<DevBuf>* owned, cudaStream_t s, int max_ranges,
                                 int chunk_div) {
   const int n = c.n;
-  if (n == 0 || nwarps < 1) return build_warp_work_host(c, nwarps, step, out, owned, s, max_ranges, chunk_div);
+  if (nwarps < 1) return set_error(ACG_ERR_INVALID_ARGUMENT, "work split: %d warps", nwarps);
+  if (n == 0) {  // no items: every part is empty
+    WarpWork& W = *out;
+    W = WarpWork{};
+    W.nparts = nwarps;
+    W.chunk = 4 * step;
+    ACG_TRY(dev_alloc(owned, sizeof(int4), (void**)&W.items, s));
+    ACG_TRY(dev_alloc(owned, sizeof(int) * ((size_t)nwarps + 1), (void**)&W.wsplit, s));
+    ACG_TRY(dev_alloc(owned, sizeof(int), (void**)&W.hbase, s));
+    ACG_TRY(dev_alloc(owned, sizeof(int), (void**)&W.hcount, s));
+    ACG_TRY(dev_alloc(owned, sizeof(int), (void**)&W.hvert, s));
+    ACG_TRY(dev_alloc(owned, sizeof(int), (void**)&W.pheavy, s));
+    return ACG_OK;  // dev_alloc zero-fills: wsplit is all zeros
+  }
   std::vector<DevBuf> tmp;
+  struct TmpGuard {  // the temporaries go back on every exit path
+    std::vector<DevBuf>* v;
+    ~TmpGuard() { dev_free_all(v); }
+  } guard{&tmp};
   auto fail = [&](acg_status st) {
     dev_free_all(&tmp);
     return st;
@@ -258,10 +277,6 @@ acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* ou
   unsigned long long htotal = 0;
   ACG_CUDA_TRY(cudaMemcpyAsync(&htotal, total, sizeof(htotal), cudaMemcpyDeviceToHost, s));
   ACG_CUDA_TRY(cudaStreamSynchronize(s));
-  if (htotal >= 0x7fffffffull) {  // the 32-bit scans could overflow: build on the host
-    dev_free_all(&tmp);
-    return build_warp_work_host(c, nwarps, step, out, owned, s, max_ranges, chunk_div);
-  }
   const int nparts = work_parts((double)htotal, nwarps, max_ranges);
   const double per_part = (double)htotal / nparts;
   const long long cs = std::max(4LL, (long long)(per_part / chunk_div));  // chunk, in steps
@@ -291,102 +306,21 @@ acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* ou
   ACG_TRY(dev_alloc(owned, sizeof(int) * std::max(1, nheavy), (void**)&W.hcount, s));
   ACG_TRY(dev_alloc(owned, sizeof(int) * std::max(1, nheavy), (void**)&W.hvert, s));
   ACG_TRY(dev_alloc(owned, sizeof(int) * std::max(1, npartial), (void**)&W.pheavy, s));
-  uint32_t *cost = nullptr, *excl = nullptr;  // per item (more items than vertices with hubs)
-  st = dev_alloc(&tmp, sizeof(uint32_t) * ((size_t)nitems + 1), (void**)&cost, s);
-  if (st == ACG_OK) st = dev_alloc(&tmp, sizeof(uint32_t) * ((size_t)nitems + 1), (void**)&excl, s);
+  // per item (more items than vertices with hubs); the cost prefix in 64 bits
+  // (a total can pass 2^32 on graphs with hundreds of millions of vertices)
+  unsigned long long *cost = nullptr, *excl = nullptr;
+  st = dev_alloc(&tmp, sizeof(unsigned long long) * ((size_t)nitems + 1), (void**)&cost, s);
+  if (st == ACG_OK) st = dev_alloc(&tmp, sizeof(unsigned long long) * ((size_t)nitems + 1), (void**)&excl, s);
   if (st != ACG_OK) return fail(st);
   work_items_kernel<<<ceil_div(n, 256), 256, 0, s>>>(c.off, n, chunk, step, nit, npart, hub, W.items, cost,
                                                      W.hbase, W.hcount, W.hvert, W.pheavy);
   if (cudaGetLastError() != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "work items launch failed"));
   // exclusive prefix of the item costs; boundaries
-  ACG_TRY(scan_exclusive_u32(cost, excl, (size_t)nitems, s));
+  ACG_TRY(scan_exclusive_u64(cost, excl, (size_t)nitems, s));
   work_split_kernel<<<ceil_div(nparts + 1, 256), 256, 0, s>>>(excl, cost, nitems, nparts, W.wsplit);
   if (cudaGetLastError() != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "work split launch failed"));
   dev_free_on(&tmp, s);
   ACG_CUDA_TRY(cudaStreamSynchronize(s));
-  return ACG_OK;
-}
-
-acg_status acg::build_warp_work_host(const Csr& c, int nwarps, int step, WarpWork* out,
-                                     std::vector<DevBuf>* owned, cudaStream_t s, int max_ranges,
-                                     int chunk_div) {
-  const int n = c.n;
-  std::vector<int> off((size_t)n + 1);
-  ACG_CUDA_TRY(cudaMemcpyAsync(off.data(), c.off, sizeof(int) * ((size_t)n + 1),
-                               cudaMemcpyDeviceToHost, s));
-  ACG_CUDA_TRY(cudaStreamSynchronize(s));
-  const double kOver = 3.0;  // per-item cost in steps (item load, combine, store)
-  double total = 0;
-  for (int v = 0; v < n; ++v) {
-    const int deg = off[v + 1] - off[v];
-    if (deg) total += (deg + step - 1) / step + kOver;
-  }
-  const int nparts = work_parts(total, nwarps, max_ranges);
-  const long long cs = std::max(4LL, (long long)(total / nparts / chunk_div));  // chunk, in steps
-  const int chunk = (int)std::min<long long>(1LL << 24, cs * step);
-  std::vector<int4> items;
-  std::vector<double> cost;
-  std::vector<int> hb, hc, hv, ph;
-  items.reserve((size_t)n / 2 + 16);
-  cost.reserve((size_t)n / 2 + 16);
-  int npart = 0;
-  for (int v = 0; v < n; ++v) {
-    const int deg = off[v + 1] - off[v];
-    if (deg == 0) continue;
-    if (deg > chunk) {
-      const int k = (deg + chunk - 1) / chunk;
-      hb.push_back(npart);
-      hc.push_back(k);
-      hv.push_back(v);
-      for (int j = 0; j < k; ++j) {
-        const int a = off[v] + j * chunk, b = std::min(off[v + 1], a + chunk);
-        items.push_back(make_int4(v, a, b, npart + j));
-        ph.push_back((int)hv.size() - 1);
-        cost.push_back((b - a + step - 1) / step + kOver);
-      }
-      npart += k;
-    } else {
-      items.push_back(make_int4(v, off[v], off[v + 1], -1));
-      cost.push_back((deg + step - 1) / step + kOver);
-    }
-  }
-  std::vector<int> split((size_t)nparts + 1, (int)items.size());
-  split[0] = 0;
-  {
-    double acc = 0, target = 0;
-    for (double x : cost) target += x;
-    target /= nparts;
-    int w = 1;
-    for (size_t i = 0; i < items.size() && w < nparts; ++i) {
-      acc += cost[i];
-      while (w < nparts && acc >= target * w) split[w++] = (int)i + 1;
-    }
-  }
-  WarpWork& W = *out;
-  W = WarpWork{};
-  W.nitems = (int)items.size();
-  W.nparts = nparts;
-  W.chunk = chunk;
-  W.nheavy = (int)hv.size();
-  W.npartial = npart;
-  ACG_TRY(dev_alloc(owned, sizeof(int4) * std::max<size_t>(1, items.size()), (void**)&W.items, s));
-  ACG_TRY(dev_alloc(owned, sizeof(int) * split.size(), (void**)&W.wsplit, s));
-  ACG_TRY(dev_alloc(owned, sizeof(int) * std::max<size_t>(1, hv.size()), (void**)&W.hbase, s));
-  ACG_TRY(dev_alloc(owned, sizeof(int) * std::max<size_t>(1, hv.size()), (void**)&W.hcount, s));
-  ACG_TRY(dev_alloc(owned, sizeof(int) * std::max<size_t>(1, hv.size()), (void**)&W.hvert, s));
-  ACG_TRY(dev_alloc(owned, sizeof(int) * std::max<size_t>(1, ph.size()), (void**)&W.pheavy, s));
-  if (!items.empty())
-    ACG_CUDA_TRY(cudaMemcpyAsync(W.items, items.data(), sizeof(int4) * items.size(),
-                                 cudaMemcpyHostToDevice, s));
-  ACG_CUDA_TRY(cudaMemcpyAsync(W.wsplit, split.data(), sizeof(int) * split.size(),
-                               cudaMemcpyHostToDevice, s));
-  if (!hv.empty()) {
-    ACG_CUDA_TRY(cudaMemcpyAsync(W.hbase, hb.data(), sizeof(int) * hb.size(), cudaMemcpyHostToDevice, s));
-    ACG_CUDA_TRY(cudaMemcpyAsync(W.hcount, hc.data(), sizeof(int) * hc.size(), cudaMemcpyHostToDevice, s));
-    ACG_CUDA_TRY(cudaMemcpyAsync(W.hvert, hv.data(), sizeof(int) * hv.size(), cudaMemcpyHostToDevice, s));
-    ACG_CUDA_TRY(cudaMemcpyAsync(W.pheavy, ph.data(), sizeof(int) * ph.size(), cudaMemcpyHostToDevice, s));
-  }
-  ACG_CUDA_TRY(cudaStreamSynchronize(s));  // the host vectors die here
   return ACG_OK;
 }
 
@@ -684,6 +618,17 @@ static acg_status get_work(acg_data* D, int which, int nwarps, int step, WarpWor
 acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& o, cudaStream_t s,
                             bool deferred, acg_plan** out) {
   std::unique_ptr<acg_plan> P(new acg_plan());
+  struct Guard {  // a plan that is not handed out frees what it holds on every exit path
+    acg_plan* p;
+    ~Guard() {
+      if (!p) return;
+      dev_free_all(&p->owned);
+      for (auto& e : p->ev)
+        if (e) cudaEventDestroy(e);
+      for (auto& e : p->kev)
+        if (e) cudaEventDestroy(e);
+    }
+  } guard{P.get()};
   P->data = D;
   P->prec = o.precision;
   P->Pn = spec.Pn;
@@ -875,6 +820,7 @@ acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& 
   }
   if (cudaStreamSynchronize(s) != cudaSuccess)
     return fail(set_error(ACG_ERR_CUDA, "acg_plan_create: %s", cudaGetErrorString(cudaGetLastError())));
+  guard.p = nullptr;
   *out = P.release();
   return ACG_OK;
 }
@@ -1114,6 +1060,22 @@ acg_status acg_release_cached_memory(void) {
   clear_error();
   cudaDeviceSynchronize();
   release_pools();
+  return ACG_OK;
+}
+
+acg_status acg_inject_alloc_failure(int64_t nth) {
+  clear_error();
+  set_alloc_failure((long long)nth);
+  return ACG_OK;
+}
+
+acg_status acg_device_memory_in_use(int64_t* bytes) {
+  clear_error();
+  if (!bytes) return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_device_memory_in_use: null argument");
+  ACG_CUDA_TRY(cudaDeviceSynchronize());  // stream-ordered frees have happened
+  const long long b = device_memory_in_use();
+  if (b < 0) return set_error(ACG_ERR_CUDA, "acg_device_memory_in_use: no device");
+  *bytes = (int64_t)b;
   return ACG_OK;
 }
 

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdlib>
+#include <atomic>
 #include <mutex>
 
 #include <algorithm>
@@ -31,6 +32,35 @@ namespace acg {
 // that save and restore device memory between kernel replays expect it).
 static cudaMemPool_t g_pools[64] = {};
 static std::mutex g_pool_mutex;
+
+// Injected allocation failure (acg_inject_alloc_failure): the value counts
+// down with every device allocation of the library; the one that takes it
+// from 1 to 0 fails as if the device were out of memory.
+static std::atomic<long long> g_fail_nth{0};
+static bool injected_failure() {
+  if (g_fail_nth.load(std::memory_order_relaxed) <= 0) return false;
+  return g_fail_nth.fetch_sub(1) == 1;
+}
+void set_alloc_failure(long long nth) { g_fail_nth.store(nth > 0 ? nth : 0); }
+
+long long device_memory_in_use() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+  long long total = 0;
+  uint64_t used = 0;
+  {
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    if (dev >= 0 && dev < 64 && g_pools[dev] &&
+        cudaMemPoolGetAttribute(g_pools[dev], cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess)
+      total += (long long)used;
+  }
+  cudaMemPool_t def = nullptr;  // the scratch of the CSR build comes from the default pool
+  if (cudaDeviceGetDefaultMemPool(&def, dev) == cudaSuccess &&
+      cudaMemPoolGetAttribute(def, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess)
+    total += (long long)used;
+  cudaGetLastError();
+  return total;
+}
 
 static bool pool_enabled() {
   static const bool on = [] {
@@ -65,6 +95,8 @@ static cudaMemPool_t device_pool() {
 
 acg_status dev_alloc(std::vector<DevBuf>* owned, size_t bytes, void** out, cudaStream_t s) {
   if (bytes == 0) bytes = 16;
+  if (injected_failure())
+    return set_error(ACG_ERR_OUT_OF_MEMORY, "cudaMalloc(%zu) failed: injected failure", bytes);
   void* p = nullptr;
   cudaMemPool_t pool = device_pool();
   cudaError_t e = pool ? cudaMallocFromPoolAsync(&p, bytes, pool, s) : cudaMalloc(&p, bytes);
@@ -130,6 +162,7 @@ namespace {
 // Short-lived scratch of the CSR build: the device's default stream-ordered
 // pool, or plain cudaMalloc when ACG_MEMPOOL=0.
 cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
+  if (injected_failure()) return cudaErrorMemoryAllocation;
   return pool_enabled() ? cudaMallocAsync(p, bytes, s) : cudaMalloc(p, bytes);
 }
 
@@ -147,40 +180,40 @@ constexpr int kScanPerThread = 4;
 constexpr int kScanTile = kScanThreads * kScanPerThread;
 
 // Exclusive scan of one tile per block; writes the tile total to sums[block].
+template <typename T>
 __global__ void __launch_bounds__(kScanThreads)
-scan_tile_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, size_t n,
-                 uint32_t* __restrict__ sums) {
-  __shared__ uint32_t warp_tot[kScanThreads / 32];
+scan_tile_kernel(const T* __restrict__ in, T* __restrict__ out, size_t n, T* __restrict__ sums) {
+  __shared__ T warp_tot[kScanThreads / 32];
   const size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanPerThread;
-  uint32_t v[kScanPerThread];
-  uint32_t t = 0;
+  T v[kScanPerThread];
+  T t = 0;
 #pragma unroll
   for (int k = 0; k < kScanPerThread; ++k) {
-    v[k] = (base + k < n) ? in[base + k] : 0u;
+    v[k] = (base + k < n) ? in[base + k] : T(0);
     t += v[k];
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t inc = t;
+  T inc = t;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    T y = __shfl_up_sync(0xffffffffu, inc, o);
     if (lane >= o) inc += y;
   }
   if (lane == 31) warp_tot[warp] = inc;
   __syncthreads();
   if (warp == 0) {
-    uint32_t w = warp_tot[lane];
-    uint32_t wi = w;
+    T w = warp_tot[lane];
+    T wi = w;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+      T y = __shfl_up_sync(0xffffffffu, wi, o);
       if (lane >= o) wi += y;
     }
     warp_tot[lane] = wi - w;  // exclusive prefix of warp totals
     if (lane == 31 && sums) sums[blockIdx.x] = wi;
   }
   __syncthreads();
-  uint32_t run = warp_tot[warp] + inc - t;
+  T run = warp_tot[warp] + inc - t;
 #pragma unroll
   for (int k = 0; k < kScanPerThread; ++k) {
     if (base + k < n) out[base + k] = run;
@@ -188,33 +221,43 @@ scan_tile_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, si
   }
 }
 
-__global__ void scan_add_kernel(uint32_t* __restrict__ out, size_t n,
-                                const uint32_t* __restrict__ offs) {
+template <typename T>
+__global__ void scan_add_kernel(T* __restrict__ out, size_t n, const T* __restrict__ offs) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] += offs[i / kScanTile];
+}
+
+template <typename T>
+acg_status scan_exclusive(const T* in, T* out, size_t n, cudaStream_t s) {
+  if (n == 0) return ACG_OK;
+  const size_t nb = (n + kScanTile - 1) / kScanTile;
+  if (nb == 1) {
+    scan_tile_kernel<T><<<1, kScanThreads, 0, s>>>(in, out, n, nullptr);
+    ACG_LAUNCH_CHECK();
+    return ACG_OK;
+  }
+  T* sums = nullptr;
+  ACG_CUDA_TRY(scratch_alloc((void**)&sums, nb * sizeof(T), s));
+  scan_tile_kernel<T><<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, sums);
+  ACG_LAUNCH_CHECK();
+  acg_status st = scan_exclusive<T>(sums, sums, nb, s);
+  if (st == ACG_OK) {
+    scan_add_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, n, sums);
+    if (cudaGetLastError() != cudaSuccess) st = set_error(ACG_ERR_CUDA, "scan_add launch failed");
+  }
+  scratch_free(sums, s);
+  return st;
 }
 
 }  // namespace
 
 acg_status scan_exclusive_u32(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s) {
-  if (n == 0) return ACG_OK;
-  const size_t nb = (n + kScanTile - 1) / kScanTile;
-  if (nb == 1) {
-    scan_tile_kernel<<<1, kScanThreads, 0, s>>>(in, out, n, nullptr);
-    ACG_LAUNCH_CHECK();
-    return ACG_OK;
-  }
-  uint32_t* sums = nullptr;
-  ACG_CUDA_TRY(scratch_alloc((void**)&sums, nb * sizeof(uint32_t), s));
-  scan_tile_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(in, out, n, sums);
-  ACG_LAUNCH_CHECK();
-  acg_status st = scan_exclusive_u32(sums, sums, nb, s);
-  if (st == ACG_OK) {
-    scan_add_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, n, sums);
-    if (cudaGetLastError() != cudaSuccess) st = set_error(ACG_ERR_CUDA, "scan_add launch failed");
-  }
-  scratch_free(sums, s);
-  return st;
+  return scan_exclusive<uint32_t>(in, out, n, s);
+}
+
+acg_status scan_exclusive_u64(const unsigned long long* in, unsigned long long* out, size_t n,
+                              cudaStream_t s) {
+  return scan_exclusive<unsigned long long>(in, out, n, s);
 }
 
 // ----------------------------------------------------------- radix sort

@@ -12,8 +12,10 @@
   do {                                                                        \
     cudaError_t acg_e_ = (expr);                                              \
     if (acg_e_ != cudaSuccess)                                                \
-      return acg::set_error(ACG_ERR_CUDA, "%s:%d: %s: %s", __FILE__, __LINE__, \
-                            #expr, cudaGetErrorString(acg_e_));               \
+      return acg::set_error(acg_e_ == cudaErrorMemoryAllocation               \
+                                ? ACG_ERR_OUT_OF_MEMORY : ACG_ERR_CUDA,       \
+                            "%s:%d: %s: %s", __FILE__, __LINE__, #expr,       \
+                            cudaGetErrorString(acg_e_));                      \
   } while (0)
 
 #define ACG_LAUNCH_CHECK()                                                    \

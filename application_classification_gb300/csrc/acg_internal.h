@@ -29,8 +29,8 @@ struct Csr {
   int* other = nullptr;    // [m] the other endpoint at each position
 };
 
-// Work of a warp-per-item segmented pass over one CSR (built on the host from
-// its offsets): item = {vertex, first position, end position, partial row or
+// Work of a warp-per-item segmented pass over one CSR (built on the device
+// from its offsets): item = {vertex, first position, end position, partial row or
 // -1}; warp w does items [wsplit[w], wsplit[w+1]), contiguous and of near-equal
 // cost (load steps + a per-item overhead).  A vertex whose edges would take a
 // large share of one warp's work is split into chunks that reduce into partial
@@ -57,10 +57,6 @@ constexpr int kMinRangeSteps = 16;
 acg_status build_warp_work(const Csr& c, int nwarps, int step, WarpWork* out,
                            std::vector<DevBuf>* owned, cudaStream_t s, int max_ranges = 1,
                            int chunk_div = 4);
-// The same on the host (the fallback when a cost sum would leave 32 bits).
-acg_status build_warp_work_host(const Csr& c, int nwarps, int step, WarpWork* out,
-                                std::vector<DevBuf>* owned, cudaStream_t s, int max_ranges = 1,
-                                int chunk_div = 4);
 // Parts of a split for nwarps warps whose total cost is `total` steps.
 inline int work_parts(double total, int nwarps, int max_ranges) {
   if (max_ranges <= 1 || nwarps < 1) return std::max(1, nwarps);
@@ -71,6 +67,8 @@ inline int work_parts(double total, int nwarps, int max_ranges) {
 // ---- primitives (acg_csr.cu)
 // Exclusive scan of n uint32 values (in and out may alias); stream ordered.
 acg_status scan_exclusive_u32(const uint32_t* in, uint32_t* out, size_t n, cudaStream_t s);
+acg_status scan_exclusive_u64(const unsigned long long* in, unsigned long long* out, size_t n,
+                              cudaStream_t s);
 // Stable LSD radix sort of (key, value) pairs on the low `bits` key bits.
 // Sorted result ends in keys/vals; keys_tmp/vals_tmp are scratch of size n.
 acg_status radix_sort_pairs_u32(uint32_t* keys, uint32_t* vals, uint32_t* keys_tmp,
@@ -87,6 +85,10 @@ void dev_free_all(std::vector<DevBuf>* owned);
 void dev_free_on(std::vector<DevBuf>* owned, cudaStream_t s);
 // Return the pools' cached free memory to the driver (acg_release_cached_memory).
 void release_pools();
+// The nth device allocation from now fails (nth <= 0: none); acg_inject_alloc_failure.
+void set_alloc_failure(long long nth);
+// Bytes in use in the library's pool and the device's default pool (-1 on error).
+long long device_memory_in_use();
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 

@@ -16,10 +16,14 @@
 // stand-in), so the address is looked up once per device with
 // cudaGetSymbolAddress, with that device current, on the first call made on it.
 // That first call therefore does a runtime query: make it before any stream
-// capture begins.  Every call uses the same array: calls whose kernels overlap
-// on the GPU (two streams, two threads) race on it and must be serialised by
-// the caller.  Nothing in the array needs to start at zero: each call writes
-// every partial it later reads.
+// capture begins.  The address is kept per device together with the identity
+// of the CUDA context it was looked up in; after cudaDeviceReset (which
+// unloads the module and the array with it) the device's next context has
+// another identity, so the next call looks the address up again -- that call,
+// too, must come before any capture.  Every call uses the same array: calls
+// whose kernels overlap on the GPU (two streams, two threads) race on it and
+// must be serialised by the caller.  Nothing in the array needs to start at
+// zero: each call writes every partial it later reads.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -44,6 +48,36 @@ static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 double* g_scratch_ptr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};  // context the address belongs to
+
+// Unique id of the current CUDA context (0 if none or unknown), from the
+// driver's cuCtxGetCurrent / cuCtxGetId, found through the runtime's entry
+// point query so that no driver library is linked.  A host-side query: it
+// enqueues nothing and is allowed while a stream is captured.
+unsigned long long current_context_id() {
+  using GetCurrent = int (*)(void**);
+  using GetId = int (*)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+    cudaGetLastError();
+  });
+  if (!get_current || !get_id) return 0;
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
 
 // Distance in the difference form, summed over the feature index in order
 // (ac.hxx:33-56), the same arithmetic as the main cdist kernel's FP64 path.
@@ -115,6 +149,12 @@ extern "C" acg_status acg_initial_mu_noalloc(const double* data_node_feats, uint
                                              uint64_t feat_dim, const double* pattern_node_feats,
                                              uint64_t pattern_nodes, double* mu_out, void* stream) {
   acg::clear_error();
+  // an error left by earlier work on this thread is reported as such, not as
+  // a failure of this call's launches
+  if (const cudaError_t pend = cudaGetLastError(); pend != cudaSuccess)
+    return acg::set_error(ACG_ERR_CUDA,
+                          "acg_initial_mu_noalloc: a CUDA error from before this call was pending: %s",
+                          cudaGetErrorString(pend));
   if (pattern_nodes == 0 || pattern_nodes > (uint64_t)kNaMaxCols)
     return acg::set_error(ACG_ERR_UNSUPPORTED,
                           "acg_initial_mu_noalloc: %llu pattern vertices; it supports 1..%d",
@@ -138,13 +178,16 @@ extern "C" acg_status acg_initial_mu_noalloc(const double* data_node_feats, uint
   double* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {  // once per device, with that device current
+    const unsigned long long ctx = current_context_id();
+    // once per device and context, with that device current
+    if (!g_scratch_ptr[dev] || (ctx != 0 && ctx != g_scratch_ctx[dev])) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (e != cudaSuccess)
         return acg::set_error(ACG_ERR_CUDA, "acg_initial_mu_noalloc: cudaGetSymbolAddress: %s",
                               cudaGetErrorString(e));
       g_scratch_ptr[dev] = static_cast<double*>(p);
+      g_scratch_ctx[dev] = ctx ? ctx : current_context_id();
     }
     scratch = g_scratch_ptr[dev];
   }

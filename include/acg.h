@@ -238,8 +238,11 @@ acg_status acg_batch_destroy(acg_batch* b);
  * file-scope device array of about 1.5 MB that every GPU loading the library
  * keeps until exit.  Limits: 1..128 pattern vertices, feature dimension
  * 1..32 (else ACG_ERR_UNSUPPORTED).  The first call on each device looks the
- * array's address up (make it before any stream capture).  All calls share the
- * array: calls whose work overlaps on the GPU race and must be serialised.
+ * array's address up (make it before any stream capture); so does the first
+ * call after cudaDeviceReset, which gives the device a new context.  All
+ * calls share the array: calls whose work overlaps on the GPU race and must
+ * be serialised.  A CUDA error already pending on the calling thread is
+ * returned (ACG_ERR_CUDA, named as earlier) before anything is launched.
  * Inputs and output are caller-owned device memory (FP64, row-major). */
 acg_status acg_initial_mu_noalloc(const double* data_node_feats, uint64_t num_nodes,
                                   uint64_t feat_dim, const double* pattern_node_feats,
@@ -277,6 +280,18 @@ acg_status acg_backward(acg_plan* plan, const double* grad_mu, double* grad_data
  * allocation) selects plain cudaMalloc / cudaFree instead; results are the
  * same bytes either way. */
 acg_status acg_release_cached_memory(void);
+
+/* Testing aids for out-of-memory handling (no counterpart in the reference,
+ * whose cudaMalloc calls go unchecked, main.cu:85-99).
+ * acg_inject_alloc_failure(n): the n-th device allocation the library makes
+ * from now on (counted over every thread) fails as if the device were out of
+ * memory, and the call that made it returns ACG_ERR_OUT_OF_MEMORY; n <= 0
+ * cancels a pending injection.
+ * acg_device_memory_in_use: synchronises the device, then reports the bytes
+ * in use in the library's memory pool and in the device's default pool (the
+ * scratch of the CSR build); a failed call must leave it where it was. */
+acg_status acg_inject_alloc_failure(int64_t nth);
+acg_status acg_device_memory_in_use(int64_t* bytes);
 
 /* ---------------- errors ----------------------------------------------- */
 const char* acg_status_string(acg_status s);

@@ -13,7 +13,7 @@
  *
  * Parity pin: tests/test_oracle.py checks this restatement against golden
  * outputs of the unmodified reference compiled for the CPU (oracle/_ref, built
- * by oracle/build_ref.sh with Thrust's OpenMP backend) on seeded inputs, stored
+ * by `make -C oracle ref` with Thrust's OpenMP backend) on seeded inputs, stored
  * under tests/golden/.
  *
  * Determinism: every reduction sums fixed 4096-element chunks and then the

@@ -33,10 +33,12 @@ _L = None
 
 
 def build(reference_dir: str | None = None) -> None:
-    """Build liboracle.so, and the reference CPU binary when its sources exist."""
+    """Build liboracle.so, and the reference CPU binary when a reference
+    checkout is given (``reference_dir`` or the environment variable
+    ACG_REFERENCE_DIR) and holds its sources."""
     subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
-    ref = reference_dir or os.environ.get("ACG_REFERENCE_DIR", "/root/reference")
-    if Path(ref, "src", "main.cu").exists():
+    ref = reference_dir or os.environ.get("ACG_REFERENCE_DIR")
+    if ref and Path(ref, "src", "main.cu").exists():
         subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={ref}"], check=True,
                        stderr=subprocess.DEVNULL)
 

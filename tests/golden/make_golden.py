@@ -4,10 +4,10 @@ Each case is a (data.bin, pattern.bin) pair in the reference's binary format
 plus mu.bin: the exact doubles that the UNMODIFIED reference program
 (src/main.cu of porumbes/application_classification, built for the CPU with
 Thrust's OpenMP backend by oracle/Makefile's `ref` target, output captured in
-binary by oracle/ref_shim) prints for that pair.  Needs the reference sources
-(default /root/reference, or ACG_REFERENCE_DIR) and runs only where they are.
+binary by oracle/ref_shim) prints for that pair.  Needs a checkout of the
+reference sources, named by the environment variable ACG_REFERENCE_DIR:
 
-    python tests/golden/make_golden.py
+    ACG_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -27,7 +27,10 @@ from application_classification_gb300 import build as _build  # noqa: E402
 from application_classification_gb300.graph import Graph, gen_er, gen_rmat, plant  # noqa: E402
 from oracle import oracle  # noqa: E402
 
-REF = Path(os.environ.get("ACG_REFERENCE_DIR", "/root/reference"))
+_ref = os.environ.get("ACG_REFERENCE_DIR")
+if not _ref:
+    raise SystemExit("set ACG_REFERENCE_DIR to the reference checkout")
+REF = Path(_ref)
 
 
 def georgiy():

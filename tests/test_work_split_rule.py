@@ -16,7 +16,8 @@ PROBE = r"""
 #include <cstdio>
 #include "acg_internal.h"
 int main() {
-  const double totals[] = {0, 1, 100, 15000, 77824, 1e6, 1.2e7, 1e9};
+  // up to totals past 2^32 steps (graphs of hundreds of millions of vertices)
+  const double totals[] = {0, 1, 100, 15000, 77824, 1e6, 1.2e7, 1e9, 3e9, 6e10};
   const int warps[] = {1, 1216, 4864};
   const int maxr[] = {1, 16, 32};
   for (double t : totals)

@@ -48,6 +48,40 @@ def test_noalloc_matches_regular_entry_point(cuda, name):
         assert np.abs(got - ref).max() <= FP64_REL * max(1.0, np.abs(ref).max())
 
 
+def _numpy_mu0(x, y):
+    """mu[r][p] = -d(r, p) - log sum_r' exp(-d(r', p)), d the Euclidean distance
+    (the reference's initial MU, main.cu:109-120), in FP64 numpy."""
+    d = np.sqrt(((x[:, None, :] - y[None, :, :]) ** 2).sum(-1))
+    m = (-d).max(0)
+    return -d - (m + np.log(np.exp(-d - m).sum(0)))
+
+
+def test_noalloc_limits_and_stale_partials(cuda):
+    """The largest pattern (128 vertices) and feature dimension (32): two rows
+    per block, the statistics pass over 5,000 rows strides its grid several
+    times and the output pass its 640,000 entries too.  The second call has a
+    different, smaller input (fewer blocks than the first): a read of the first
+    call's partials left in the shared array would change its result."""
+    import torch
+
+    rng = np.random.default_rng(7)
+    stream = torch.cuda.current_stream()
+    for n, p, k in ((5000, 128, 32), (300, 128, 32), (5000, 128, 32)):
+        x = rng.normal(size=(n, k))
+        y = rng.normal(size=(p, k))
+        ref = _numpy_mu0(x, y)
+        dx = matcher.DeviceGraph.from_tensors(torch.from_numpy(x).to(cuda), torch.zeros((0, 1)),
+                                              torch.zeros(0), torch.zeros(0))
+        dy = matcher.DeviceGraph.from_tensors(torch.from_numpy(y).to(cuda), torch.zeros((0, 1)),
+                                              torch.zeros(0), torch.zeros(0))
+        out = torch.full((n, p), float("nan"), dtype=torch.float64, device=cuda)
+        _noalloc(dx, dy, out, stream)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        assert np.isfinite(got).all()
+        assert np.abs(got - ref).max() <= FP64_REL * max(1.0, np.abs(ref).max())
+
+
 def test_noalloc_rejects_oversized_pattern(cuda):
     import torch
 
