@@ -240,7 +240,7 @@ __global__ void work_split_kernel(const unsigned long long* __restrict__ excl,
 // vertex; a part is a run of items of near-equal total cost.
 acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* out,
                                 std::vector<DevBuf>* owned, cudaStream_t s, int max_ranges,
-                                int chunk_div) {
+                                int chunk_div, int max_chunk) {
   const int n = c.n;
   if (nwarps < 1) return set_error(ACG_ERR_INVALID_ARGUMENT, "work split: %d warps", nwarps);
   if (n == 0) {  // no items: every part is empty
@@ -280,7 +280,7 @@ acg_status acg::build_warp_work(const Csr& c, int nwarps, int step, WarpWork* ou
   const int nparts = work_parts((double)htotal, nwarps, max_ranges);
   const double per_part = (double)htotal / nparts;
   const long long cs = std::max(4LL, (long long)(per_part / chunk_div));  // chunk, in steps
-  const int chunk = (int)std::min<long long>(1LL << 24, cs * step);
+  const int chunk = (int)std::min<long long>(std::max(1, max_chunk), cs * step);
   work_count_kernel<<<ceil_div(n, 256), 256, 0, s>>>(c.off, n, chunk, nit, npart, hub);
   if (cudaGetLastError() != cudaSuccess) return fail(set_error(ACG_ERR_CUDA, "work count launch failed"));
   // counts -> offsets (the n-th entry, zero, becomes the total)
@@ -333,10 +333,11 @@ acg_status iterate(acg_plan* P, int t, double* mu_out, cudaStream_t s) {
   if (P->kernel_timing) cudaEventRecord(P->kev[3 * (t - 1)], s);
   if constexpr (std::is_same_v<T, float>) {
     if (Pe > 0 && P->edge_tc && !P->rec) {  // costs recomputed on the tensor cores
-      EdgeTcArgs ta{D->ef32, P->pe, D->dcsr.other, D->dst_of, D->dcsr.off,
-                    (const float*)P->vr[(t - 1) & 1], (float*)P->M, P->et_H, P->et_T, P->et_cnt,
-                    P->dev_err, (long long)D->De, D->Ke, D->ke32, Pe, Pp, P->et_tpc};
-      ACG_TRY(launch_edge_tc(ta, D->num_sms, s));
+      const WarpWork& w = P->etw;
+      EdgeTcArgs ta{D->ef32, P->pe, D->dcsr.other, (const float*)P->vr[(t - 1) & 1], (float*)P->M,
+                    w.items, w.wsplit, P->et_part, w.pheavy, w.hbase, w.hcount, w.hvert, P->et_hcnt,
+                    P->dev_err, (long long)D->De, D->Ke, D->ke32, Pe, Pp};
+      ACG_TRY(launch_edge_tc(ta, w.nparts, s));
       P->launches += 1;
       goto vertex_phase;
     }
@@ -602,13 +603,14 @@ constexpr int kEdgeChunkDiv = ACG_EDGE_CHUNK_DIV;
 
 // The work split for (CSR, parts, step, chunk divisor), built once per data graph.
 static acg_status get_work(acg_data* D, int which, int nwarps, int step, WarpWork* out,
-                           cudaStream_t s, int max_ranges = 1, int chunk_div = 4) {
-  const auto key = std::make_tuple(which, nwarps, step, max_ranges, chunk_div);
+                           cudaStream_t s, int max_ranges = 1, int chunk_div = 4,
+                           int max_chunk = 1 << 24) {
+  const auto key = std::make_tuple(which, nwarps, step, max_ranges, chunk_div, max_chunk);
   auto it = D->work.find(key);
   if (it == D->work.end()) {
     WarpWork w;
     ACG_TRY(build_warp_work(which == 0 ? D->dcsr : D->scsr, nwarps, step, &w, &D->owned, s,
-                            max_ranges, chunk_div));
+                            max_ranges, chunk_div, max_chunk));
     it = D->work.emplace(key, w).first;
   }
   *out = it->second;
@@ -686,15 +688,9 @@ acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& 
     }
   }
   if (P->edge_tc) {
-    P->et_tpc = edge_tc_tiles_per_chunk(De, D->num_sms);
-    const size_t nch = (size_t)edge_tc_chunks(De, P->et_tpc);
-    alloc(sizeof(float) * nch * Pp, (void**)&P->et_H);
-    alloc(sizeof(float) * nch * Pp, (void**)&P->et_T);
-    alloc(sizeof(int) * nch, (void**)&P->et_cnt);
-    if (st == ACG_OK && !D->dst_of) {
-      st = dev_alloc(&D->owned, sizeof(int) * (size_t)De, (void**)&D->dst_of, s);
-      if (st == ACG_OK) st = launch_csr_rows(D->dcsr.off, Dn, D->dst_of, s);
-    }
+    st = get_work(D, 0, D->num_sms, 1, &P->etw, s, 1, 1, kEdgeTcChunk);
+    alloc(sizeof(float) * (size_t)std::max(1, P->etw.npartial) * Pp, (void**)&P->et_part);
+    alloc(sizeof(int) * (size_t)std::max(1, P->etw.nheavy), (void**)&P->et_hcnt);
   }
   if (o.cnull) {
     alloc(sizeof(double) * 3 * std::max(1, Pe), (void**)&P->cnull);
@@ -1018,8 +1014,9 @@ acg_status acg_plan_stats(acg_plan* P, acg_stats* out) {
   // mixed precision) read, Y and Z written, the in-degree offsets.
   const double cvb = P->prec == ACG_PREC_MIXED ? 2.0 * eb : eb;
   out->bytes_edge_phase = De * (Pe * eb + 4.0) + 2.0 * Dn * Pe * eb + (double)P->ew.nitems * 16.0;
-  if (P->edge_tc)  // costs recomputed: per in-edge its FP32 features, source and destination
-    out->bytes_edge_phase = De * (P->data->Ke * 4.0 + 8.0) + 2.0 * Dn * Pe * eb;
+  if (P->edge_tc)  // costs recomputed: per in-edge its FP32 features and source
+    out->bytes_edge_phase = De * (P->data->Ke * 4.0 + 4.0) + 2.0 * Dn * Pe * eb +
+                            (double)P->etw.nitems * 16.0;
   out->bytes_vertex_phase = Dn * (4.0 * Pe * eb + Pn * cvb + 2.0 * Pe * eb + 4.0);
   out->bytes_iters = (out->bytes_edge_phase + out->bytes_vertex_phase) * P->iters;
   out->launches = P->launches;

@@ -1,21 +1,20 @@
 // acg_cdist_tc.cu -- the edge cost matrix on the 5th-generation tensor cores
 // (tcgen05), for the mixed-precision path.
 //
-// dE[r][q] = ||x_r - y_q|| (ac.hxx:33-56) as ||x||^2 + ||y||^2 - 2 x.y: the
-// cross term is a [128 rows] x [N columns] x [K'] product per tile, in TF32
-// with a three-term split that carries FP32 accuracy:
-//     x = x0 + x1, y = y0 + y1 (x0 = tf32(x), x1 = tf32(x - x0))
-//     x.y ~ x0.y0 + x1.y0 + x0.y1   (the dropped x1.y1 is ~2^-22 relative)
-// laid out along K as A' = [x0 | x1 | x0], B' = [y0 | y0 | y1] in blocks of KM
-// (the feature dimension padded to 4), K' = 3 KM padded to a multiple of 8
-// (one tcgen05.mma.kind::tf32 per 8).  Both sides are
-// first centred on the mean pattern feature vector m (distances do not change)
-// and the norms are FP32 sums.  The norm form's error scales with
-// ||x - m||^2 + ||y - m||^2 (FP32 accumulation, the dropped x1.y1), not with
-// d^2, so a pair with kNear * d^2 < ||x - m||^2 + ||y - m||^2 is recomputed
-// exactly in the difference form from the FP32 features: near pairs (the
-// planted ones) and data whose feature spread is large against the distances
-// keep full FP32 accuracy.  For N(0,1) features almost no pair is recomputed.
+// dE[r][q] = ||x_r - y_q|| (ac.hxx:33-56) as ||x||^2 + ||y||^2 - 2 x.y, all
+// three terms accumulated by the tensor cores: a [128 rows] x [N columns] x
+// [K'] product per tile in TF32, with a three-term split that carries FP32
+// accuracy in the cross term and the FP32 norms fed in as hi/lo TF32 pairs
+// against ones (the operand layout is in acg_tc.cuh, dist_kp / dist_b_elem /
+// dist_a_norms).  Both sides are first centred on the mean pattern feature
+// vector m (distances do not change).  The norm form's error scales with
+// ||x - m||^2 + ||y - m||^2, not with d^2, so a pair with
+// 8 d^2 < ||x - m||^2 + ||y - m||^2 is recomputed exactly in the difference
+// form from the FP32 features (dist_finish): near pairs (the planted ones) and
+// data whose feature spread is large against the distances keep full FP32
+// accuracy.  For N(0,1) features almost no pair is recomputed.  The edge phase
+// that recomputes these costs in every iteration (acg_edge_tc.cu) uses the
+// same operands and rule, so both give the same bits.
 //
 // One persistent CTA (8 warps) walks tiles of 128 data rows:
 //   feature rows [128][kstride] FP32 --cp.async.bulk (TMA) + mbarrier--> smem
@@ -43,10 +42,6 @@ using namespace tc;
 
 constexpr int kTT = 256;               // threads per CTA
 constexpr int kTM = 128;               // data rows per tile (the MMA's M)
-#ifndef ACG_TC_NEAR
-#define ACG_TC_NEAR 8.0f
-#endif
-constexpr float kNear = ACG_TC_NEAR;  // see the header: the relative recompute threshold
 constexpr int kStg = 20;  // staging row stride (floats): 16 columns + 16 bytes (no bank conflicts)
 
 // Dynamic shared memory layout (byte offsets, each 128-aligned).
@@ -57,7 +52,7 @@ __host__ __device__ inline TcLayout tc_layout(int K, int kstride, int Pp, int N)
   TcLayout L;
   (void)K;
   (void)Pp;
-  const uint32_t kp = (uint32_t)(3 * kstride + 7) / 8 * 8;  // K' padded to the MMA's K step
+  const uint32_t kp = (uint32_t)dist_kp(kstride);  // K' padded to the MMA's K step
   uint32_t o = 0;
   // A' also holds the epilogue's staging rows (8 warps x 32 rows x kStg)
   const uint32_t abytes = (uint32_t)kTM * kp * 4, sbytes = (uint32_t)(kTT / 32) * 32 * kStg * 4;
@@ -85,11 +80,11 @@ struct TcArgs {
 };
 
 // KM: the feature dimension padded to 4 (the FP32 row stride).  A' holds
-// [x0 | x1 | x0] in blocks of KM columns, so each 4-wide core column comes
-// from one block and is one 16-byte store.
+// [x0 | x1 | x0 | norms] in blocks of KM columns, so each 4-wide core column
+// comes from one block and is one 16-byte store.
 template <int KM>
 __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
-  constexpr int KP = (3 * KM + 7) / 8 * 8;  // K' padded to the MMA's K step
+  constexpr int KP = dist_kp(KM);            // K' padded to the MMA's K step
   constexpr int KB = KM / 4;                // core columns per block
   extern __shared__ __align__(1024) unsigned char sm[];
   const TcLayout L = tc_layout(a.K, KM, a.Pp, a.N);
@@ -128,19 +123,8 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
     sY[i] = (q < P && k < K) ? (float)a.y[(size_t)q * K + k] : 0.f;
   }
   __syncthreads();
-  // B' = [y0 | y0 | y1] of y - m (zero rows q >= P and columns k >= 3 KM), the
-  // centred norms; A' zeroed (its padding columns stay zero)
-  for (int i = tid; i < N * KP; i += kTT) {
-    const int q = i / KP, k = i - q * KP;
-    float v = 0.f;
-    if (k < 3 * KM) {
-      const int blk = k / KM, kk = k - blk * KM;
-      const float yc = q < P ? sY[(size_t)q * KM + kk] - smean[kk] : 0.f;
-      const float y0 = tf32_round(yc);
-      v = blk == 2 ? tf32_round(yc - y0) : y0;
-    }
-    *reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(sB) + kmaj_off(q, k, N)) = v;
-  }
+  // the centred pattern norms, then B' (acg_tc.cuh); A' zeroed (its padding
+  // columns stay zero)
   for (int q = tid; q < N; q += kTT) {
     float s = 0.f;
     if (q < P)
@@ -149,6 +133,13 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
         s = fmaf(yc, yc, s);
       }
     sny[q] = s;
+  }
+  __syncthreads();
+  for (int i = tid; i < N * KP; i += kTT) {
+    const int q = i / KP, k = i - q * KP, kk = k % KM;
+    const float yk = (q < P && k < 3 * KM) ? sY[(size_t)q * KM + kk] - smean[kk] : 0.f;
+    const float v = dist_b_elem(yk, q < P ? sny[q] : 0.f, q < P, k, KM);
+    *reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(sB) + kmaj_off(q, k, N)) = v;
   }
   for (int i = tid; i < kTM * KP; i += kTT) sA[i] = 0.f;
   for (int r = tid; r < kTM; r += kTT) snx[r] = 0.f;
@@ -224,7 +215,10 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
                 make_float4(h1[0], h1[1], h1[2], h1[3]);
           }
         }
-        if (h == 0) snx[r] = s;
+        if (h == 0) {
+          snx[r] = s;
+          *reinterpret_cast<float4*>(A + (uint32_t)(3 * KB) * lboA + rb) = dist_a_norms(s);
+        }
       }
     }
     fence_proxy_async();  // the generic-proxy writes of A' before the MMA reads them
@@ -263,21 +257,9 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
 #pragma unroll
           for (int w = 0; w < 4; ++w) {
             const int j = 4 * j4 + w, q = c * 16 + j;
-            const float sn = nx + nyv[w];
-            float d2 = fmaf(-2.f, __uint_as_float(v[j]), sn);
-            if (q < P && kNear * d2 < sn) {  // cancellation: exact difference form
-              const float* yq = sY + (size_t)q * KM;
-              const float* xr = sXb + (size_t)r * KM;
-              float acc = 0.f;
-#pragma unroll
-              for (int k = 0; k < KM; ++k) {
-                const float t = xr[k] - yq[k];
-                acc = fmaf(t, t, acc);
-              }
-              d2 = acc;
-            }
-            d2 = fmaxf(d2, 0.f);
-            d[j] = (q < P && r < nr) ? (d2 > 0.f ? d2 * rsqrtf(d2) : 0.f) : 0.f;
+            d[j] = (q < P && r < nr) ? dist_finish<KM>(__uint_as_float(v[j]), nx + nyv[w], sXb + (size_t)r * KM,
+                                                       sY + (size_t)q * KM)
+                                     : 0.f;
           }
         }
 #pragma unroll

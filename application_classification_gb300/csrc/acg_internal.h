@@ -54,9 +54,10 @@ struct WarpWork {
 // run time past the first); a chunk is 1 / chunk_div of a part's cost (at least
 // 4 steps).
 constexpr int kMinRangeSteps = 16;
+// max_chunk caps the chunk length (positions) of heavy vertices.
 acg_status build_warp_work(const Csr& c, int nwarps, int step, WarpWork* out,
                            std::vector<DevBuf>* owned, cudaStream_t s, int max_ranges = 1,
-                           int chunk_div = 4);
+                           int chunk_div = 4, int max_chunk = 1 << 24);
 // Parts of a split for nwarps warps whose total cost is `total` steps.
 inline int work_parts(double total, int nwarps, int max_ranges) {
   if (max_ranges <= 1 || nwarps < 1) return std::max(1, nwarps);

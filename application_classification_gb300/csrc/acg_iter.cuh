@@ -87,34 +87,32 @@ acg_status launch_capture_s(const double* S, const int* iters_p, int t, double* 
 
 // Edge phase of FP32 plans with the costs recomputed on the tensor cores
 // (acg_edge_tc.cu): M[v][q] = max over in-edges e of z[s_e][q] - ||x_e - y_q||,
-// d formed as the tensor-core edge cost matrix forms it.
+// d formed as the tensor-core edge cost matrix forms it.  One CTA per part of
+// the item split (items of at most 128 positions; heavy vertices chunked).
 struct EdgeTcArgs {
   const float* x;      // [De][KM] FP32 edge features in dst-CSR order (zero past K)
   const double* y;     // [P][K] pattern edge features
   const int* src_of;   // [De] source vertex of each dst-CSR position
-  const int* dst_of;   // [De] destination vertex of each dst-CSR position
-  const int* off;      // [Dn + 1] dst-CSR offsets
   const float* z;      // [Dn][Pp] gathered by source
   float* M;            // [Dn][Pp] out (rows of vertices without in-edges untouched)
-  float* H;            // [nchunks][Pp] partial rows: head / through pieces of a chunk
-  float* T;            // [nchunks][Pp] partial rows: tail pieces
-  int* cnt;            // [nchunks] arrival counts, zero before and after a launch
+  const int4* items;   // {vertex, first position, end position, partial row or -1}
+  const int* wsplit;   // [parts + 1]: CTA b does items [wsplit[b], wsplit[b+1])
+  float* partial;      // [npartial][Pp] rows of heavy-vertex chunks
+  const int* pheavy;   // [npartial] heavy vertex of each partial row
+  const int* hbase;    // per heavy vertex: first partial row, chunk count, vertex
+  const int* hcount;
+  const int* hvert;
+  int* hcnt;           // [nheavy] chunks done, zero before and after a launch
   int* err;            // set to 1 when a bounded wait gave up
   long long De;
   int K, KM, P, Pp;
-  int tpc;             // tiles of 128 in-edges per chunk
   // set by launch_edge_tc
-  int N = 0, tcols = 0, ntiles = 0, nchunks = 0;
+  int N = 0, tcols = 0;
 };
 bool edge_tc_eligible(int K, int kstride, int P, int Pp);
 size_t edge_tc_smem(int kstride, int Pp);
-int edge_tc_tiles_per_chunk(long long De, int num_sms);
-inline int edge_tc_chunks(long long De, int tpc) {
-  return (int)(((De + 127) / 128 + tpc - 1) / tpc);
-}
-acg_status launch_edge_tc(const EdgeTcArgs& a, int num_sms, cudaStream_t s);
-// dst_of[i] = v for every position i in [off[v], off[v+1]).
-acg_status launch_csr_rows(const int* off, int n, int* dst_of, cudaStream_t s);
+constexpr int kEdgeTcChunk = 128;  // positions per chunk of a heavy vertex (one tile)
+acg_status launch_edge_tc(const EdgeTcArgs& a, int parts, cudaStream_t s);
 
 struct WarpShape {
   int npow;  // lanes covering one [Pp] row (power of two <= 32)

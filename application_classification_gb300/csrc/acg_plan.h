@@ -35,10 +35,9 @@ struct acg_data {
   float* nf32 = nullptr;
   float* ef32 = nullptr;
   int ke32 = 0;
-  int* dst_of = nullptr;      // [De] destination of each dst-CSR position (built on first use)
   // warp work splits, shared by every plan on this graph: key = (0 dst / 1 src
-  // CSR, warps, positions per step)
-  std::map<std::tuple<int, int, int, int, int>, acg::WarpWork> work;
+  // CSR, parts, positions per step, ranges per part, chunk divisor, chunk cap)
+  std::map<std::tuple<int, int, int, int, int, int>, acg::WarpWork> work;
   std::vector<acg::DevBuf> owned;
 };
 
@@ -120,11 +119,10 @@ struct acg_plan {
   int64_t launches = 0;
   bool ran = false;
   bool cdist_tc = false;       // edge cost matrix on the tensor cores
-  bool edge_tc = false;        // edge phase recomputes the costs on the tensor cores
-  int et_tpc = 0;              // its tiles per chunk, chunk pieces and counts
-  float* et_H = nullptr;
-  float* et_T = nullptr;
-  int* et_cnt = nullptr;
+  bool edge_tc = false;        // edge phase recomputes the costs on the tensor cores:
+  acg::WarpWork etw;           // its item split (one part per CTA),
+  float* et_part = nullptr;    // partial rows of heavy-vertex chunks [npartial][Pp]
+  int* et_hcnt = nullptr;      // and chunks done per heavy vertex
   int* heavy_ctr = nullptr;    // [nheavy] chunks of each heavy vertex done in this edge phase
   int* range_ctr = nullptr;    // [2] range claims and finished warps of the range-split
                                // kernels (one at a time on the plan's stream; each

@@ -115,5 +115,56 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t tmem, uint32_t cols) {
   asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(cols) : "memory");
 }
 
+// ---- the distance MMA shared by the edge cost matrix (acg_cdist_tc.cu) and
+// the edge phase that recomputes it (acg_edge_tc.cu).  With x, y centred on
+// the mean pattern feature vector and split into TF32 parts (x0 = tf32(x),
+// x1 = tf32(x - x0), likewise y), the operands along K are
+//     A' = [x0 | x1 | x0 | nx0 nx1 1 1],  B' = [-2y0 | -2y0 | -2y1 | 1 1 ny0 ny1]
+// in blocks of KM (the feature dimension padded to 4), nx = ||x||^2 and
+// ny = ||y||^2 in FP32 split the same way, so one accumulator holds
+//     d2 = nx + ny - 2 (x0.y0 + x1.y0 + x0.y1)       (x1.y1 ~ 2^-22 relative, dropped)
+// and K' = 3 KM + 4 padded to the MMA's K step of 8.
+__host__ __device__ constexpr int dist_kp(int KM) { return (3 * KM + 4 + 7) / 8 * 8; }
+
+// Element k of row q of B' from yk, the centred FP32 feature k % KM of pattern
+// row q (k < 3 KM), the row's norm ny, and whether the row exists (pad rows:
+// zero but for the two 1s, so their d2 is nx).
+__device__ __forceinline__ float dist_b_elem(float yk, float ny, bool real, int k, int KM) {
+  if (k < 3 * KM) {
+    if (!real) return 0.f;
+    const float y0 = tf32_round(yk);
+    return -2.f * (k >= 2 * KM ? tf32_round(yk - y0) : y0);
+  }
+  const int e = k - 3 * KM;
+  if (e == 0 || e == 1) return 1.f;
+  if (!real || e > 3) return 0.f;
+  const float n0 = tf32_round(ny);
+  return e == 2 ? n0 : tf32_round(ny - n0);
+}
+
+// The norm block of a row of A': (nx0, nx1, 1, 1).
+__device__ __forceinline__ float4 dist_a_norms(float nx) {
+  const float n0 = tf32_round(nx);
+  return make_float4(n0, tf32_round(nx - n0), 1.f, 1.f);
+}
+
+// d from the accumulator's d2 for a pair with pattern row q < P: a pair whose
+// d2 is small against its norms (8 d2 < sn = nx + ny: cancellation) is
+// recomputed exactly in the difference form from the FP32 rows xr, yr.
+template <int KM>
+__device__ __forceinline__ float dist_finish(float d2, float sn, const float* xr, const float* yr) {
+  if (8.0f * d2 < sn) {
+    float acc = 0.f;
+#pragma unroll 1
+    for (int k = 0; k < KM; ++k) {
+      const float u = xr[k] - yr[k];
+      acc = fmaf(u, u, acc);
+    }
+    d2 = acc;
+  }
+  d2 = fmaxf(d2, 0.f);
+  return d2 > 0.f ? d2 * rsqrtf(d2) : 0.f;
+}
+
 }  // namespace tc
 }  // namespace acg

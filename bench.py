@@ -78,6 +78,9 @@ def parse():
     ap.add_argument("--workload", default="rmat22",
                     help="one of %s, or rmatS_P_E (RMAT scale S, pattern P/E)" % sorted(WORKLOADS))
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--edge-kernel", default="auto", choices=["auto", "stored", "fused"],
+                    help="the mixed path's edge phase: read the stored edge cost matrix, or "
+                         "recompute the costs on the tensor cores (acg_options.edge_kernel)")
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-fp64", action="store_true")
@@ -275,7 +278,8 @@ def run_ours(args, ws, rank, local):
 
     # ---- device-resident match
     dg = matcher.DataGraph(d)
-    plan = matcher.Plan(dg, p, args.precision)
+    ek = args.edge_kernel if args.precision == "mixed" else "auto"
+    plan = matcher.Plan(dg, p, args.precision, edge_kernel=ek)
     out = torch.empty((d.num_nodes, p.num_nodes), dtype=torch.float64, device=dev)
     for _ in range(args.warmup):
         plan.run(out)
@@ -301,7 +305,7 @@ def run_ours(args, ws, rank, local):
     # per-phase durations (CUDA events around each phase of every iteration,
     # on a second plan so that the timed region above carries no extra events)
     del plan
-    tplan = matcher.Plan(dg, p, args.precision, kernel_timing=True)
+    tplan = matcher.Plan(dg, p, args.precision, kernel_timing=True, edge_kernel=ek)
     tplan.run(out)
     phase = []
     for _ in range(min(args.steps, 3)):
