@@ -94,7 +94,7 @@ def build(verbose: bool = False, force: bool = False, out_dir: Path | None = Non
     if force or todo or not lib.exists() or any(o.stat().st_mtime > lib.stat().st_mtime for o in objs):
         tmp = out / "libacg.so.tmp"
         cmd = [_nvcc(), ARCH, "-shared", "-o", str(tmp), *map(str, objs),
-               "-Xcompiler", "-fopenmp", "-lgomp", "-cudart", "static"]
+               "-Xcompiler", "-fopenmp", "-lgomp", "-ldl", "-cudart", "static"]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         r = subprocess.run(cmd, capture_output=True, text=True)
