@@ -197,12 +197,12 @@ __global__ void __launch_bounds__(kET, 1) edge_tc_kernel(const EdgeTcArgs a) {
   if (tid == 0) {
     for (int i = 0; i < 3; ++i) {
       mbar_init(bar(B_FFULL + i), 1);
-      mbar_init(bar(B_FEMPTY + i), kSplitWarps * 32);  // every split thread reads the slot
+      mbar_init(bar(B_FEMPTY + i), kSplitWarps);  // one arrival per split warp
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(bar(B_MMA + i), 1);
-      mbar_init(bar(B_NX + i), kSplitWarps * 32);
-      mbar_init(bar(B_ACCFREE + i), kEpiWarps * 32);
+      mbar_init(bar(B_NX + i), kSplitWarps);
+      mbar_init(bar(B_ACCFREE + i), kEpiWarps);  // one arrival per epilogue warp
     }
     for (int i = 0; i < kRing; ++i) mbar_init(bar(B_ZFULL + i), kGatherWarps * 32);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -319,8 +319,11 @@ __global__ void __launch_bounds__(kET, 1) edge_tc_kernel(const EdgeTcArgs a) {
       } else if (h == 0) {
         snx[(t & 1) * kTM + r] = 0.f;
       }
-      mbar_arrive(bar(B_FEMPTY + t % 3));
-      mbar_arrive(bar(B_NX + (t & 1)));
+      __syncwarp();
+      if (lane == 0) {  // the warp's reads of the feature slot and writes of the norms are done
+        mbar_arrive(bar(B_FEMPTY + t % 3));
+        mbar_arrive(bar(B_NX + (t & 1)));
+      }
       fence_proxy_async();  // the generic-proxy writes of A' before the MMA reads them
       fence_before();
       named_bar(1, kSplitWarps * 32);
@@ -437,7 +440,8 @@ __global__ void __launch_bounds__(kET, 1) edge_tc_kernel(const EdgeTcArgs a) {
         }
       }
       fence_before();
-      mbar_arrive(bar(B_ACCFREE + (t & 1)));  // the accumulator and the tile's norms are free
+      __syncwarp();
+      if (lane == 0) mbar_arrive(bar(B_ACCFREE + (t & 1)));  // the accumulator and the tile's norms are free
       named_bar(2, kEpiWarps * 32);
       if (e == 0 && lane == 0) {
         __threadfence_block();
@@ -538,7 +542,8 @@ __global__ void __launch_bounds__(kET, 1) edge_tc_kernel(const EdgeTcArgs a) {
   __syncthreads();
   if (ld_volatile(abort)) {
     // copies and MMAs issued and not waited for land before the CTA leaves
-    // (at most three feature copies and two MMA commits; bounded waits)
+    // (at most three feature copies and two MMA commits; bounded waits; the
+    // gather threads waited for their row copies themselves)
     if (tid == 0)
       for (int t = smisc[M_FWAITED]; t < smisc[M_FISSUED]; ++t)
         mbar_wait(bar(B_FFULL + t % 3), (uint32_t)((t / 3) & 1));

@@ -370,6 +370,32 @@ def run_ours(args, ws, rank, local):
         ms64 = e0.elapsed_time(e1) / args.fp64_steps
         mu64 = out64.cpu().numpy()
         s64 = pl64.stats()
+        # per-phase times of the FP64 iterations (a second plan with events
+        # around each phase) against their bytes and their FP64 operations:
+        # the edge phase does a subtraction and a maximum per (in-edge, column)
+        t64 = matcher.Plan(dg, p, "fp64", kernel_timing=True)
+        t64.run(out64)
+        st64 = t64.stats()
+        del t64
+        it64 = max(1, int(st64["num_iters"]))
+        e_ms = st64["ms_edge_phase"] / it64
+        v_ms = st64["ms_vertex_phase"] / it64
+        fp64_ops = 2.0 * d.num_edges * p.num_edges
+        fp64_nominal = 1.25e12 / 2  # FP64 instructions per second (1.25 TFLOP/s counts an FMA as 2)
+        fp64_roof = {
+            "edge_phase": {"launch_ms": round(e_ms, 3), "bytes": st64["bytes_edge_phase"],
+                           "achieved_gbs": round(st64["bytes_edge_phase"] / (e_ms * 1e-3) / 1e9, 1),
+                           "hbm_frac": round(st64["bytes_edge_phase"] / (e_ms * 1e-3) / 1e9 / peak, 4),
+                           "fp64_ops": fp64_ops,
+                           "fp64_ops_per_s": round(fp64_ops / (e_ms * 1e-3), 1),
+                           "fp64_frac_of_nominal": round(fp64_ops / (e_ms * 1e-3) / fp64_nominal, 4)},
+            "vertex_phase": {"launch_ms": round(v_ms, 3), "bytes": st64["bytes_vertex_phase"],
+                             "achieved_gbs": round(st64["bytes_vertex_phase"] / (v_ms * 1e-3) / 1e9, 1),
+                             "hbm_frac": round(st64["bytes_vertex_phase"] / (v_ms * 1e-3) / 1e9 / peak, 4)},
+            "bound": "fp64 pipe (GB300's FP64 rate: nominal 1.25 TFLOP/s, 1/64 of its FP32 rate), "
+                     "not HBM",
+            "nominal_fp64": "1.25 TFLOP/s, NVIDIA's figure (no measured FP64 peak on this pool)",
+        }
         diff = np.abs(mu_mixed - mu64)
         a64, am = mu64.argmax(1), mu_mixed.argmax(1)
         srt = np.sort(mu64, axis=1)
@@ -378,6 +404,7 @@ def run_ours(args, ws, rank, local):
         result["plain_fp64"] = {
             "ms": round(ms64, 3), "speedup_mixed_vs_fp64": round(ms64 / value, 2),
             "phases_ms": {k: round(s64[k], 3) for k in ("ms_cdist", "ms_init", "ms_iters")},
+            "roofline": fp64_roof,
             "max_abs_dmu": float(diff.max()), "max_abs_mu": float(np.abs(mu64).max()),
             "argmax_identical_except_ties": bool(((a64 == am) | tie).all()),
             "argmax_mismatch_rows": int((a64 != am).sum()),
