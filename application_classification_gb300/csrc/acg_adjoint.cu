@@ -1481,7 +1481,7 @@ struct Adj {
     const bool f32 = sizeof(T) == 4;
     const int* row = vertex ? nullptr : (f32 ? nullptr : D->dcsr.eid);
     const int* orow = vertex ? nullptr : D->dcsr.eid;
-    const int kstride = vertex ? K : (f32 ? D->ke32 : K);
+    const int kstride = f32 ? (vertex ? D->kv32 : D->ke32) : K;
     cudaError_t le = cudaSuccess;
     auto launch = [&](auto kmc) {
       constexpr int KM = decltype(kmc)::value;

@@ -32,11 +32,12 @@ using namespace acg;
 namespace {
 acg_status ensure_f32(acg_data* D, cudaStream_t s) {
   if (D->nf32) return ACG_OK;
+  D->kv32 = (D->Kv + 3) / 4 * 4;
   D->ke32 = (D->Ke + 3) / 4 * 4;
   float *nf = nullptr, *ef = nullptr;
-  ACG_TRY(dev_alloc(&D->owned, sizeof(float) * (size_t)D->Dn * std::max(1, D->Kv), (void**)&nf, s));
+  ACG_TRY(dev_alloc(&D->owned, sizeof(float) * (size_t)D->Dn * std::max(1, D->kv32), (void**)&nf, s));
   ACG_TRY(dev_alloc(&D->owned, sizeof(float) * (size_t)D->De * std::max(1, D->ke32), (void**)&ef, s));
-  ACG_TRY(launch_convert_rows(D->node_feats, nullptr, D->Dn, D->Kv, nf, D->Kv, s));
+  ACG_TRY(launch_convert_rows(D->node_feats, nullptr, D->Dn, D->Kv, nf, D->kv32, s));
   ACG_TRY(launch_convert_rows(D->edge_feats, D->dcsr.eid, D->De, D->Ke, ef, D->ke32, s));
   D->nf32 = nf;
   D->ef32 = ef;
@@ -383,6 +384,8 @@ vertex_phase:
                       mu_out, P->pat, Dn, Pn, Pe, Pp, P->Pnp, P->maxdeg, P->iters_p, t,
                       t == 1, t == P->iters};
   va.cnull = P->cnull;
+  va.vsched = P->vsched;
+  va.vterms = P->vterms;
   const bool rec = P->rec && P->rec->has(t);
   if (rec) {
     va.rec_f = (T*)P->rec->f[t];
@@ -533,10 +536,21 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s, const UnionOut
 template <typename T, typename F>
 acg_status run_cdist(acg_plan* P, acg_data* D, long long lim, const F* nf, int nfs, const F* ef,
                      int efs, bool gather, cudaStream_t s) {
-  CdistRbArgs<T, F> av{nf, nullptr, nullptr, P->pv, (T*)P->CV, P->bpart, D->Dn, D->De, lim,
-                       D->Kv, nfs, P->Pn, P->Pnp, P->Pnp};
-  ACG_TRY(launch_cdist_rb(av, kCdistVertex, P->cv_blocks, s));
-  ACG_TRY(launch_finalize(P->bpart, P->cv_blocks, StatSpec{P->Pn, 2 * P->Pn}, P->gv, s));
+  int vcols = P->cv_blocks;  // partial columns of the vertex statistics
+  bool vdone = false;
+  if constexpr (std::is_same_v<T, float> && std::is_same_v<F, float>) {
+    if (P->cdist_tc_v) {
+      ACG_TRY(launch_cdist_vertex_tc(nf, nfs, D->Kv, P->pv, P->Pn, P->Pnp, (float*)P->CV, P->bpart, D->Dn,
+                                     P->cv_blocks, &vcols, P->dev_err, D->num_sms, s));
+      vdone = true;
+    }
+  }
+  if (!vdone) {
+    CdistRbArgs<T, F> av{nf, nullptr, nullptr, P->pv, (T*)P->CV, P->bpart, D->Dn, D->De, lim,
+                         D->Kv, nfs, P->Pn, P->Pnp, P->Pnp};
+    ACG_TRY(launch_cdist_rb(av, kCdistVertex, P->cv_blocks, s));
+  }
+  ACG_TRY(launch_finalize(P->bpart, vcols, StatSpec{P->Pn, 2 * P->Pn}, P->gv, s));
   // rows in dst-CSR order; with no data edges the kernel writes empty partials
   CdistRbArgs<T, F> ae{ef, gather ? D->dcsr.eid : nullptr, D->dcsr.eid, P->pe, (T*)P->dE,
                        nullptr, D->De, D->De, lim, D->Ke, efs, P->Pe, P->Pp, P->Pp};
@@ -558,7 +572,7 @@ acg_status Cdist<double>::run(acg_plan* P, acg_data* D, long long lim, cudaStrea
 }
 
 acg_status Cdist<float>::run(acg_plan* P, acg_data* D, long long lim, cudaStream_t s) {
-  return run_cdist<float, float>(P, D, lim, D->nf32, D->Kv, D->ef32, D->ke32, false, s);
+  return run_cdist<float, float>(P, D, lim, D->nf32, D->kv32, D->ef32, D->ke32, false, s);
 }
 
 }  // namespace
@@ -697,10 +711,16 @@ acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& 
   alloc(sizeof(int), (void**)&P->dev_err);
   if (P->prec == ACG_PREC_MIXED && o.cdist_kernel != 1) {
     P->cdist_tc = cdist_tc_eligible(D->Ke, (D->Ke + 3) / 4 * 4, Pe, Pp);
-    if (!P->cdist_tc && o.cdist_kernel == 2) {
+    P->cdist_tc_v = cdist_tc_eligible(D->Kv, (D->Kv + 3) / 4 * 4, Pn, P->Pnp);
+    if (o.cdist_kernel == 2 && !P->cdist_tc) {
       dev_free_all(&P->owned);
       return set_error(ACG_ERR_UNSUPPORTED,
                        "tensor-core cdist: edge feature dim %d, %d pattern edges", D->Ke, Pe);
+    }
+    if (o.cdist_kernel == 2 && !P->cdist_tc_v) {
+      dev_free_all(&P->owned);
+      return set_error(ACG_ERR_UNSUPPORTED,
+                       "tensor-core cdist: vertex feature dim %d, %d pattern vertices", D->Kv, Pn);
     }
   }
   // the edge phase recomputing the costs (single plans with the tensor-core
@@ -772,8 +792,16 @@ acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& 
     int md = 0;
     for (int p = 0; p < Pn; ++p) md = std::max(md, io[p + 1] - io[p] + oo[p + 1] - oo[p]);
     P->maxdeg = md;
-    P->vert_blocks = eb == 8 ? vertex_update_blocks<double>(Pn, Pe, Pp, P->Pnp, md, nsm, Dn)
-                             : vertex_update_blocks<float>(Pn, Pe, Pp, P->Pnp, md, nsm, Dn);
+    std::vector<uint32_t> vs;
+    P->vterms = vertex_warp_schedule(spec.pat.data(), Pn, Pe, Pp, P->Pnp, &vs);
+    if (P->vterms > 0) {
+      st = dev_alloc(&P->owned, sizeof(uint32_t) * vs.size(), (void**)&P->vsched, s);
+      if (st != ACG_OK) return fail(st);
+      ACG_CUDA_TRY(cudaMemcpyAsync(P->vsched, vs.data(), sizeof(uint32_t) * vs.size(),
+                                   cudaMemcpyHostToDevice, s));
+    }
+    P->vert_blocks = eb == 8 ? vertex_update_blocks<double>(Pn, Pe, Pp, P->Pnp, P->vterms, nsm, Dn)
+                             : vertex_update_blocks<float>(Pn, Pe, Pp, P->Pnp, P->vterms, nsm, Dn);
     if (o.vertex_blocks_per_sm > 0)
       P->vert_blocks = std::min(P->vert_blocks, nsm * o.vertex_blocks_per_sm);
   }

@@ -40,5 +40,12 @@ acg_status launch_cdist_edges(const CdistRbArgs<T, F>& a, int blocks, cudaStream
 bool cdist_tc_eligible(int K, int kstride, int P, int Pp);
 acg_status launch_cdist_edges_tc(const float* x, int kstride, int K, const double* y, int P, int Pp,
                                  float* out, long long nrows, int* err, int num_sms, cudaStream_t s);
+// The vertex cost matrix of the mixed path on the tensor cores, with the
+// per-column statistics of kCdistVertex as block partials (StatSpec{P, 2P}),
+// one partial column per CTA: at most max_grid CTAs (0: no cap), the count
+// used returned in *grid_used (at least 1; with no rows the partials are empty).
+acg_status launch_cdist_vertex_tc(const float* x, int kstride, int K, const double* y, int P, int Pp,
+                                  float* out, double* bpart, long long nrows, int max_grid, int* grid_used,
+                                  int* err, int num_sms, cudaStream_t s);
 
 }  // namespace acg

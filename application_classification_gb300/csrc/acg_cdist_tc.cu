@@ -1,7 +1,8 @@
-// acg_cdist_tc.cu -- the edge cost matrix on the 5th-generation tensor cores
-// (tcgen05), for the mixed-precision path.
+// acg_cdist_tc.cu -- the edge and vertex cost matrices on the 5th-generation
+// tensor cores (tcgen05), for the mixed-precision path.
 //
-// dE[r][q] = ||x_r - y_q|| (ac.hxx:33-56) as ||x||^2 + ||y||^2 - 2 x.y, all
+// dE[r][q] = ||x_r - y_q|| (ac.hxx:33-56, main.cu:110), and likewise dV
+// (main.cu:109) with its per-column statistics, as ||x||^2 + ||y||^2 - 2 x.y, all
 // three terms accumulated by the tensor cores: a [128 rows] x [N columns] x
 // [K'] product per tile in TF32, with a three-term split that carries FP32
 // accuracy in the cross term and the FP32 norms fed in as hi/lo TF32 pairs
@@ -22,7 +23,10 @@
 //   threads split them into A' in the no-swizzle K-major core-matrix layout
 //   thread 0 issues K'/8 MMAs into a TMEM accumulator, tcgen05.commit -> mbarrier
 //   warps (lane quarter w % 4, column half w / 4) tcgen05.ld the accumulator,
-//     form d and store their rows' 16-column chunks as 16-byte stores.
+//     form d and store their rows' 16-column chunks as 16-byte stores; for
+//     the vertex matrix each lane also folds one column of the staged chunk
+//     (16 of the warp's rows) into max(-d), LSE(d), LSE(-d) (main.cu:112,
+//     116-117), merged per CTA in FP64 into the block partials at the end.
 // Every mbarrier wait is bounded: on expiry the CTA records an error flag,
 // waits (bounded) for its own operations in flight, frees its TMEM and exits.
 #include <cuda_runtime.h>
@@ -74,6 +78,7 @@ struct TcArgs {
   const float* x;   // [nrows][KM] FP32 features (zero past K), in output row order
   const double* y;  // [P][K]
   float* out;       // [nrows][Pp]
+  double* bpart;    // vertex matrix: block partials (StatSpec{P, 2P}), one column per CTA
   int* err;         // set to 1 when a bounded wait gave up
   long long nrows;
   int K, P, Pp, N, tcols;
@@ -81,8 +86,9 @@ struct TcArgs {
 
 // KM: the feature dimension padded to 4 (the FP32 row stride).  A' holds
 // [x0 | x1 | x0 | norms] in blocks of KM columns, so each 4-wide core column
-// comes from one block and is one 16-byte store.
-template <int KM>
+// comes from one block and is one 16-byte store.  STATS: the vertex matrix's
+// column statistics.
+template <int KM, bool STATS>
 __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
   constexpr int KP = dist_kp(KM);            // K' padded to the MMA's K step
   constexpr int KB = KM / 4;                // core columns per block
@@ -154,6 +160,17 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
   bool pend[2] = {false, false};  // a bulk load into buffer i is in flight (uniform)
   bool pend_mma = false;
   bool ok = true;
+  // column statistics of lane l: column c * 16 + (l & 15) of the warp's chunk
+  // slot j (c = warp / 4 + 2 j), over rows (l / 16) * 16 .. +15 of its 32
+  constexpr int kSlots = STATS ? 4 : 1;
+  float cmx[kSlots];
+  OnlineLse<float> cl1[kSlots], cl2[kSlots];
+#pragma unroll
+  for (int j = 0; j < kSlots; ++j) {
+    cmx[j] = -CUDART_INF_F;
+    cl1[j].init();
+    cl2[j].init();
+  }
 
   long long tile = blockIdx.x;
   if (tile < ntiles) {
@@ -248,7 +265,8 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
       const float nx = snx[r];
       float* stg = sA + warp * 32 * kStg;  // [32][kStg], 16-column rows + padding
       // one chunk: d from the accumulator column values, staged, stored
-      auto emit = [&](int c, const uint32_t (&v)[16]) {
+      auto emit = [&](int c, const uint32_t (&v)[16], float& mx, OnlineLse<float>& l1,
+                      OnlineLse<float>& l2) {
         float d[16];
 #pragma unroll
         for (int j4 = 0; j4 < 4; ++j4) {
@@ -276,13 +294,28 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
             *reinterpret_cast<float4*>(a.out + (size_t)(r0 + rw + rr) * Pp + col) =
                 *reinterpret_cast<const float4*>(stg + rr * kStg + qt * 4);
         }
+        if constexpr (STATS) {
+          const int q = c * 16 + (lane & 15), h0 = (lane >> 4) * 16;
+          if (q < P)
+#pragma unroll 4
+            for (int i = 0; i < 16; ++i) {
+              if (rw + h0 + i >= nr) break;
+              const float dv = stg[(h0 + i) * kStg + (lane & 15)];
+              mx = fmaxf(mx, -dv);
+              l1.add(dv);
+              l2.add(-dv);
+            }
+        }
         __syncwarp();
       };
-      for (int c = warp >> 2; c < N / 16; c += 2) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int c = (warp >> 2) + 2 * j;
+        if (c >= N / 16) break;
         uint32_t v[16];
         ld16(tmem + ((uint32_t)rw << 16) + (uint32_t)c * 16, v);
         wait_ld();
-        emit(c, v);
+        emit(c, v, cmx[STATS ? j : 0], cl1[STATS ? j : 0], cl2[STATS ? j : 0]);
       }
     }
     fence_before();
@@ -294,6 +327,42 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
     for (int i = 0; i < 2; ++i)
       if (pend[i]) mbar_wait(bar[i], ph[i]);
     if (pend_mma) mbar_wait(bar[2], ph[2]);
+  }
+  if constexpr (STATS) {
+    // block partials, one chunk slot at a time: column q's eight partials
+    // (row quarters w % 4 of column half (q / 16) % 2, lane halves) merged in
+    // a fixed order
+    double* red = reinterpret_cast<double*>(sm + L.a);  // idle now: 256 x 5 doubles fit
+    const int ncols = gridDim.x, col = blockIdx.x;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (32 * j >= P) break;
+      __syncthreads();
+      double* e = red + (size_t)tid * 5;
+      e[0] = (double)cmx[j];
+      e[1] = cl1[j].mval();
+      e[2] = cl1[j].sval();
+      e[3] = cl2[j].mval();
+      e[4] = cl2[j].sval();
+      __syncthreads();
+      const int q = 32 * j + tid;
+      if (tid < 32 && q < P) {
+        double m = -CUDART_INF, am = -CUDART_INF, as = 0, bm = -CUDART_INF, bs = 0;
+        const int wh = ((q >> 4) & 1) * 4;
+        for (int wq = 0; wq < 4; ++wq)
+          for (int h = 0; h < 2; ++h) {
+            const double* x = red + (size_t)((wh + wq) * 32 + (q & 15) + 16 * h) * 5;
+            m = fmax(m, x[0]);
+            lse_merge(am, as, x[1], x[2]);
+            lse_merge(bm, bs, x[3], x[4]);
+          }
+        a.bpart[(size_t)q * ncols + col] = m;
+        a.bpart[(size_t)(P + 2 * q) * ncols + col] = am;
+        a.bpart[(size_t)(P + 2 * q + 1) * ncols + col] = as;
+        a.bpart[(size_t)(P + 2 * (P + q)) * ncols + col] = bm;
+        a.bpart[(size_t)(P + 2 * (P + q) + 1) * ncols + col] = bs;
+      }
+    }
   }
   fence_before();
   __syncthreads();
@@ -310,40 +379,55 @@ bool cdist_tc_eligible(int K, int kstride, int P, int Pp) {
   return P > 0 && K >= 1 && K <= 32 && kstride == (K + 3) / 4 * 4 && N <= 128;
 }
 
-template <int KM>
-static acg_status launch_tc(const TcArgs& a, int num_sms, cudaStream_t s) {
+template <int KM, bool STATS>
+static acg_status launch_tc(const TcArgs& a, int num_sms, int max_grid, int* grid_used, cudaStream_t s) {
   const TcLayout L = tc_layout(a.K, KM, a.Pp, a.N);
-  ACG_CUDA_TRY(cudaFuncSetAttribute(cdist_tc_kernel<KM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)L.total));
-  ACG_CUDA_TRY(cudaFuncSetAttribute(cdist_tc_kernel<KM>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                    100));
+  auto* fn = cdist_tc_kernel<KM, STATS>;
+  ACG_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total));
+  ACG_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   // resident CTAs per SM from shared memory, registers and TMEM (512 columns)
   int dev = 0, smem_sm = 0, resv = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
   cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev);
   cudaFuncAttributes fa{};
-  ACG_CUDA_TRY(cudaFuncGetAttributes(&fa, cdist_tc_kernel<KM>));
+  ACG_CUDA_TRY(cudaFuncGetAttributes(&fa, fn));
   const int regs = (fa.numRegs + 7) / 8 * 8;
   int nb = smem_sm / (int)(L.total + resv);
   nb = std::min(nb, 65536 / std::max(1, regs * kTT));
   nb = std::max(1, std::min(nb, 512 / a.tcols));
   const long long ntiles = (a.nrows + kTM - 1) / kTM;
-  const int grid = (int)std::min<long long>(ntiles, (long long)num_sms * nb);
-  cdist_tc_kernel<KM><<<grid, kTT, L.total, s>>>(a);
+  long long grid = std::min<long long>(ntiles, (long long)num_sms * nb);
+  if (max_grid > 0) grid = std::min<long long>(grid, max_grid);
+  grid = std::max<long long>(grid, 1);  // a CTA with no tile still writes empty partials
+  fn<<<(int)grid, kTT, L.total, s>>>(a);
   ACG_LAUNCH_CHECK();
+  if (grid_used) *grid_used = (int)grid;
   return ACG_OK;
 }
 
-acg_status launch_cdist_edges_tc(const float* x, int kstride, int K, const double* y, int P, int Pp,
-                                 float* out, long long nrows, int* err, int num_sms, cudaStream_t s) {
-  if (P == 0 || nrows == 0) return ACG_OK;
-  if (!cdist_tc_eligible(K, kstride, P, Pp))
-    return set_error(ACG_ERR_UNSUPPORTED, "tensor-core cdist: K=%d, %d columns", K, P);
+template <bool STATS>
+static acg_status launch_km(const TcArgs& a, int kstride, int num_sms, int max_grid, int* grid_used,
+                            cudaStream_t s) {
+  switch (kstride) {
+    case 4: return launch_tc<4, STATS>(a, num_sms, max_grid, grid_used, s);
+    case 8: return launch_tc<8, STATS>(a, num_sms, max_grid, grid_used, s);
+    case 12: return launch_tc<12, STATS>(a, num_sms, max_grid, grid_used, s);
+    case 16: return launch_tc<16, STATS>(a, num_sms, max_grid, grid_used, s);
+    case 20: return launch_tc<20, STATS>(a, num_sms, max_grid, grid_used, s);
+    case 24: return launch_tc<24, STATS>(a, num_sms, max_grid, grid_used, s);
+    case 28: return launch_tc<28, STATS>(a, num_sms, max_grid, grid_used, s);
+    default: return launch_tc<32, STATS>(a, num_sms, max_grid, grid_used, s);
+  }
+}
+
+static TcArgs tc_args(const float* x, int K, const double* y, int P, int Pp, float* out, double* bpart,
+                      long long nrows, int* err) {
   TcArgs a;
   a.x = x;
   a.y = y;
   a.out = out;
+  a.bpart = bpart;
   a.err = err;
   a.nrows = nrows;
   a.K = K;
@@ -351,16 +435,24 @@ acg_status launch_cdist_edges_tc(const float* x, int kstride, int K, const doubl
   a.Pp = Pp;
   a.N = (Pp + 15) / 16 * 16;
   a.tcols = a.N <= 32 ? 32 : (a.N <= 64 ? 64 : 128);
-  switch (kstride) {
-    case 4: return launch_tc<4>(a, num_sms, s);
-    case 8: return launch_tc<8>(a, num_sms, s);
-    case 12: return launch_tc<12>(a, num_sms, s);
-    case 16: return launch_tc<16>(a, num_sms, s);
-    case 20: return launch_tc<20>(a, num_sms, s);
-    case 24: return launch_tc<24>(a, num_sms, s);
-    case 28: return launch_tc<28>(a, num_sms, s);
-    default: return launch_tc<32>(a, num_sms, s);
-  }
+  return a;
+}
+
+acg_status launch_cdist_edges_tc(const float* x, int kstride, int K, const double* y, int P, int Pp,
+                                 float* out, long long nrows, int* err, int num_sms, cudaStream_t s) {
+  if (P == 0 || nrows == 0) return ACG_OK;
+  if (!cdist_tc_eligible(K, kstride, P, Pp))
+    return set_error(ACG_ERR_UNSUPPORTED, "tensor-core cdist: K=%d, %d columns", K, P);
+  return launch_km<false>(tc_args(x, K, y, P, Pp, out, nullptr, nrows, err), kstride, num_sms, 0, nullptr, s);
+}
+
+acg_status launch_cdist_vertex_tc(const float* x, int kstride, int K, const double* y, int P, int Pp,
+                                  float* out, double* bpart, long long nrows, int max_grid, int* grid_used,
+                                  int* err, int num_sms, cudaStream_t s) {
+  if (!cdist_tc_eligible(K, kstride, P, Pp))
+    return set_error(ACG_ERR_UNSUPPORTED, "tensor-core vertex cdist: K=%d, %d columns", K, P);
+  return launch_km<true>(tc_args(x, K, y, P, Pp, out, bpart, nrows, err), kstride, num_sms, max_grid,
+                         grid_used, s);
 }
 
 }  // namespace acg

@@ -137,6 +137,32 @@ struct OnlineLse<float> {
     kahan(__expf(x - mn));
     m = mn;
   }
+  // Four values at once (-inf entries add nothing): one rescale of the running
+  // sum for the block's maximum, the four terms summed in FP32 first.
+  __device__ __forceinline__ void add4_fast(float x0, float x1, float x2, float x3) {
+    const float m4 = fmaxf(fmaxf(x0, x1), fmaxf(x2, x3));
+    if (!(m4 > -CUDART_INF_F)) return;
+    const float mn = fmaxf(m, m4);
+    const float sc = __expf(m - mn);  // m = -inf -> 0
+    s *= sc;
+    c *= sc;
+    kahan((__expf(x0 - mn) + __expf(x1 - mn)) + (__expf(x2 - mn) + __expf(x3 - mn)));
+    m = mn;
+  }
+  // add2_fast of four compensated values hi + lo (hi = -inf: nothing)
+  __device__ __forceinline__ void add2x4_fast(const float (&hi)[4], const float (&lo)[4]) {
+    const float m4 = fmaxf(fmaxf(hi[0], hi[1]), fmaxf(hi[2], hi[3]));
+    if (!(m4 > -CUDART_INF_F)) return;
+    const float mn = fmaxf(m, m4);
+    const float sc = __expf(m - mn);
+    s *= sc;
+    c *= sc;
+    float e[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) e[i] = __expf(hi[i] - mn) * (1.f + lo[i]);
+    kahan((e[0] + e[1]) + (e[2] + e[3]));
+    m = mn;
+  }
   __device__ __forceinline__ double mval() const { return (double)m; }
   __device__ __forceinline__ double sval() const { return (double)s - (double)c; }
 };

@@ -32,6 +32,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <limits>
+#include <vector>
 
 #include "acg_device.cuh"
 #include "acg_iter.cuh"
@@ -706,39 +707,59 @@ vertex_update_kernel(const VertexUpdArgs<T> a) {
 // per-q constants and statistics of its columns live in registers.  Each warp
 // walks a contiguous range of vertices; their rows are staged into a per-warp
 // double-buffered ring (kVps vertices per stage) with cp.async, so a warp never
-// waits on another.  Per vertex: F, R from the staged M, Y; the compensated
-// MU_raw[p] from a per-warp shared copy of F|R through precomputed incidence
-// indices (in-edges of p ascending, then out-edges ascending -- the order of
-// the tile form); the new Y, Z from MU_raw[dst_q], MU_raw[src_q].  Vertices
-// without in-edges have M rows of -inf (set once, never written by phase A).
+// waits on another.  Per stage:
+//   1. F, R of each staged vertex from its M, Y rows, written over them in the
+//      stage (the CV rows are negated in place);
+//   2. the compensated sums MU_raw[v][p] = -CV[v][p] + sum F + sum R of all
+//      staged vertices through a per-lane schedule built on the host
+//      (vertex_warp_schedule): each (vertex, p) sum is one job whose terms are
+//      -CV, then F[q] of the in-edges q of p ascending, then R[q] of its
+//      out-edges ascending -- the order of the tile form -- and the jobs are
+//      spread over the lanes longest first, so a lane runs ~1/32 of the
+//      stage's terms instead of the largest pattern degree for every vertex;
+//   3. per staged vertex: the MU_raw statistics and outputs of the lane's p,
+//      and the new Y, Z of its columns from MU_raw[dst_q], MU_raw[src_q].
+// Every sum keeps its terms and their order, so the results do not depend on
+// how the jobs are spread.  Vertices without in-edges have M rows of -inf (set
+// once, never written by phase A).
 #ifndef ACG_VTX_VPS
 #define ACG_VTX_VPS 4
 #endif
 constexpr int kVps = ACG_VTX_VPS;  // vertices per stage
 constexpr int kVw = kBT / 32;
+// schedule word: element offset of the term in the stage (bits 0-11), first
+// term of its job (bit 12), last term (bit 13), the job's slot jv * (32 PPL + 1)
+// + p in the per-warp MU_raw rows (bits 16-24); stored [t / 4][lane][t % 4]
+constexpr uint32_t kSchedStart = 1u << 12, kSchedEnd = 1u << 13;
+
+// Element offsets of one stage: M, Y, dEmin, B rows [kVps][Pp], then the CV
+// rows [kVps][Pnp] and (FP32) their low parts.
+struct VwStage {
+  int oM, oY, oE, oB, oC, oCl, n;
+  __host__ __device__ VwStage(int Pp, int Pnp, bool lo) {
+    oM = 0;
+    oY = kVps * Pp;
+    oE = 2 * kVps * Pp;
+    oB = 3 * kVps * Pp;
+    oC = 4 * kVps * Pp;
+    oCl = oC + kVps * Pnp;
+    n = oCl + (lo ? kVps * Pnp : 0);
+  }
+};
 
 template <typename T, int QPL, int PPL>
 struct VwSmem {
-  size_t pat, inc, ring, fr, mu, total, stage, warp_ring, oM, oY, oE, oB, oC, oCl, fr_n, mu_n;
-  __host__ __device__ VwSmem(int Pn, int Pe, int Pp, int Pnp, int maxdeg) {
+  size_t pat, sched, ring, mu, total, stage, warp_ring, mu_n;
+  __host__ __device__ VwSmem(int Pn, int Pe, int Pp, int Pnp, int nterms) {
     const size_t sz = sizeof(T);
     size_t o = 0;
     pat = o; o += a16(sizeof(int) * (size_t)(4 * Pe + 2 * (Pn + 1)));
-    inc = o; o += a16(sizeof(int) * (size_t)PPL * maxdeg * 32);
-    size_t so = 0;  // one stage; row sizes are 16-byte multiples
-    oM = so; so += (size_t)kVps * Pp * sz;
-    oY = so; so += (size_t)kVps * Pp * sz;
-    oE = so; so += (size_t)kVps * Pp * sz;
-    oB = so; so += (size_t)kVps * Pp * sz;
-    oC = so; so += (size_t)kVps * Pnp * sz;
-    oCl = so; so += sz == 4 ? (size_t)kVps * Pnp * sz : 0;
-    stage = so;
-    warp_ring = 2 * so;
+    sched = o; o += a16(sizeof(uint32_t) * (size_t)nterms * 32);
+    stage = (size_t)VwStage(Pp, Pnp, sz == 4).n * sz;  // row sizes are 16-byte multiples
+    warp_ring = 2 * stage;
     const size_t red = sizeof(double) * (size_t)kVw * (6 * Pe + 2 * Pn);  // aliases the rings
     ring = o; o += a16(red > kVw * warp_ring ? red : kVw * warp_ring);
-    fr_n = 2 * 32 * QPL + 4;  // F | R | zeros
-    fr = o; o += a16((size_t)kVw * fr_n * sz);
-    mu_n = 2 * 32 * PPL;      // MU_raw hi | lo
+    mu_n = 2 * kVps * (32 * PPL + 1);  // MU_raw hi | lo rows of the staged vertices
     mu = o; o += a16((size_t)kVw * mu_n * sz);
     total = o;
   }
@@ -771,8 +792,7 @@ __device__ __forceinline__ void st_n(T* p, const T (&x)[N]) {
   }
 }
 
-// Two blocks per SM bounds the registers at 128 (RMAT-22 vertex phase 1.76 ms;
-// no bound: 1.90 ms; one block: 2.65 ms)
+// Two blocks per SM bounds the registers at 128
 #ifndef ACG_VTX_MINB
 #define ACG_VTX_MINB 2
 #endif
@@ -780,37 +800,17 @@ template <typename T, int QPL, int PPL>
 __global__ void __launch_bounds__(kBT, ACG_VTX_MINB)
 vertex_warp_kernel(const VertexUpdArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int Pe = a.Pe, Pn = a.Pn, Pp = a.Pp, Pnp = a.Pnp, Dn = a.Dn, maxdeg = a.maxdeg;
-  const VwSmem<T, QPL, PPL> L(Pn, Pe, Pp, Pnp, maxdeg);
+  const int Pe = a.Pe, Pn = a.Pn, Pp = a.Pp, Pnp = a.Pnp, Dn = a.Dn, nterms = a.vterms;
+  const VwSmem<T, QPL, PPL> L(Pn, Pe, Pp, Pnp, nterms);
+  const VwStage G(Pp, Pnp, sizeof(T) == 4);
   const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
   int* s_pat = reinterpret_cast<int*>(smem + L.pat);
-  int* s_inc = reinterpret_cast<int*>(smem + L.inc);
+  uint32_t* s_sched = reinterpret_cast<uint32_t*>(smem + L.sched);
   for (int t = tid; t < 4 * Pe + 2 * (Pn + 1); t += kBT) s_pat[t] = a.pat[t];
+  for (int t = tid; t < nterms * 32; t += kBT) s_sched[t] = a.vsched[t];
   __syncthreads();
   const int* s_psrc = s_pat;
   const int* s_pdst = s_pat + Pe;
-  const int* s_inoff = s_pat + 2 * Pe;
-  const int* s_inq = s_inoff + Pn + 1;
-  const int* s_outoff = s_inq + Pe;
-  const int* s_outq = s_outoff + Pn + 1;
-  constexpr int kZero = 2 * 32 * QPL;
-  // incidence index of lane l, pattern vertex p = l + 32 j, round t, at
-  // s_inc[(j * maxdeg + t) * 32 + l]: F[q] (dst_q = p), then R[q] (src_q = p),
-  // then a zero
-  for (int i = tid; i < PPL * maxdeg * 32; i += kBT) {
-    const int l = i & 31, t = (i >> 5) % maxdeg, j = (i >> 5) / maxdeg;
-    const int p = l + 32 * j;
-    int code = kZero;
-    if (p < Pn) {
-      const int nin = s_inoff[p + 1] - s_inoff[p];
-      const int nout = s_outoff[p + 1] - s_outoff[p];
-      if (t < nin)
-        code = s_inq[s_inoff[p] + t];
-      else if (t < nin + nout)
-        code = 32 * QPL + s_outq[s_outoff[p] + t - nin];
-    }
-    s_inc[i] = code;
-  }
 
   // per-q constants of the lane's columns (see the tile form for the algebra)
   const double* g = a.glob_in;
@@ -874,33 +874,16 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
     const int p = lane + 32 * j;
     plast[j] = p < Pn && __ldg(a.iters_p + p) == a.t;
   }
-  __syncthreads();  // s_inc complete
-  // With maxdeg <= kPackDeg the lane's incidence codes (< 256) live in
-  // registers, four to a word; the padding codes index a zero.
-  constexpr int kPackDeg = 16;
-  const bool packed = maxdeg <= kPackDeg;
-  uint32_t pk[PPL][kPackDeg / 4];
-#pragma unroll
-  for (int j = 0; j < PPL; ++j)
-#pragma unroll
-    for (int w = 0; w < kPackDeg / 4; ++w) {
-      uint32_t x = 0;
-#pragma unroll
-      for (int b = 0; b < 4; ++b) {
-        const int t = 4 * w + b;
-        const uint32_t c = packed && t < maxdeg ? (uint32_t)s_inc[(j * maxdeg + t) * 32 + lane] : (uint32_t)kZero;
-        x |= c << (8 * b);
-      }
-      pk[j][w] = x;
-    }
 
   const long long nw = (long long)gridDim.x * kVw;
   const long long gw = (long long)blockIdx.x * kVw + wib;
   const int vb = (int)(gw * Dn / nw), ve = (int)((gw + 1) * Dn / nw);
   unsigned char* ring = smem + L.ring + (size_t)wib * L.warp_ring;
-  T* sfr = reinterpret_cast<T*>(smem + L.fr) + (size_t)wib * L.fr_n;
   T* smu = reinterpret_cast<T*>(smem + L.mu) + (size_t)wib * L.mu_n;
-  if (lane < 4) sfr[kZero + lane] = T(0);
+  // MU_raw rows of the staged vertices, one word apart in bank order so that
+  // the lanes ending jobs of one p for different vertices do not collide
+  constexpr int kMuRow = 32 * PPL + 1;
+  constexpr int kMuLo = kVps * kMuRow;  // the low parts after the high parts
   const size_t rowb = (size_t)Pp * sizeof(T), crow = (size_t)Pnp * sizeof(T);
   auto issue = [&](int v0, int buf) {
     const int nv = min(kVps, ve - v0);
@@ -909,17 +892,17 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
     const int n16 = (int)((size_t)nv * rowb / 16);
     const size_t go = (size_t)v0 * rowb;
     for (int c = lane; c < n16; c += 32) {
-      cp16(st + L.oM + c * 16, reinterpret_cast<const unsigned char*>(a.M) + go + c * 16);
-      cp16(st + L.oY + c * 16, reinterpret_cast<const unsigned char*>(a.vf) + go + c * 16);
-      cp16(st + L.oE + c * 16, reinterpret_cast<const unsigned char*>(a.dEmin) + go + c * 16);
-      cp16(st + L.oB + c * 16, reinterpret_cast<const unsigned char*>(a.B) + go + c * 16);
+      cp16(st + G.oM * sizeof(T) + c * 16, reinterpret_cast<const unsigned char*>(a.M) + go + c * 16);
+      cp16(st + G.oY * sizeof(T) + c * 16, reinterpret_cast<const unsigned char*>(a.vf) + go + c * 16);
+      cp16(st + G.oE * sizeof(T) + c * 16, reinterpret_cast<const unsigned char*>(a.dEmin) + go + c * 16);
+      cp16(st + G.oB * sizeof(T) + c * 16, reinterpret_cast<const unsigned char*>(a.B) + go + c * 16);
     }
     const int c16 = (int)((size_t)nv * crow / 16);
     const size_t co = (size_t)v0 * crow;
     for (int c = lane; c < c16; c += 32) {
-      cp16(st + L.oC + c * 16, reinterpret_cast<const unsigned char*>(a.CV) + co + c * 16);
+      cp16(st + G.oC * sizeof(T) + c * 16, reinterpret_cast<const unsigned char*>(a.CV) + co + c * 16);
       if constexpr (sizeof(T) == 4)
-        cp16(st + L.oCl + c * 16, reinterpret_cast<const unsigned char*>(a.CVlo) + co + c * 16);
+        cp16(st + G.oCl * sizeof(T) + c * 16, reinterpret_cast<const unsigned char*>(a.CVlo) + co + c * 16);
     }
   };
   issue(vb, 0);
@@ -930,82 +913,143 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
     cp_commit();
     cp_wait1();
     __syncwarp();
-    const unsigned char* st = ring + (size_t)buf * L.stage;
+    T* st = reinterpret_cast<T*>(ring + (size_t)buf * L.stage);
     const int nv = min(kVps, ve - v0);
-    for (int jv = 0; jv < nv; ++jv) {
-      const int v = v0 + jv;
-      T F[QPL], R[QPL], em[QPL], b[QPL];
+    // ---- 1. F over M, R over Y; -CV (and its low part) in place
+#pragma unroll
+    for (int jv = 0; jv < kVps; ++jv) {
+      if (jv >= nv) break;
       if (qon) {
-        T m[QPL], y[QPL];
-        lds_n<T, QPL>(reinterpret_cast<const T*>(st + L.oM) + jv * Pp + qo, m);
-        lds_n<T, QPL>(reinterpret_cast<const T*>(st + L.oY) + jv * Pp + qo, y);
-        lds_n<T, QPL>(reinterpret_cast<const T*>(st + L.oE) + jv * Pp + qo, em);
-        lds_n<T, QPL>(reinterpret_cast<const T*>(st + L.oB) + jv * Pp + qo, b);
+        T m[QPL], y[QPL], F[QPL], R[QPL];
+        T* sm_ = st + G.oM + jv * Pp + qo;
+        T* sy_ = st + G.oY + jv * Pp + qo;
+        lds_n<T, QPL>(sm_, m);
+        lds_n<T, QPL>(sy_, y);
 #pragma unroll
         for (int k = 0; k < QPL; ++k) {
           // no in-edges: M = -inf; no out-edges: Y = -inf; the fill wins
           F[k] = fmax(fF[k], (m[k] - dFh[k]) - dFl[k]);
           R[k] = fmax(fR[k], (y[k] - dRh[k]) - dRl[k]);
         }
-        st_n<T, QPL>(sfr + qo, F);
-        st_n<T, QPL>(sfr + 32 * QPL + qo, R);
+        st_n<T, QPL>(sm_, F);
+        st_n<T, QPL>(sy_, R);
       }
-      __syncwarp();
-      // MU_raw = -CV + sum F + sum R, compensated (CV carries a low part)
-      const T* sC = reinterpret_cast<const T*>(st + L.oC) + jv * Pnp;
 #pragma unroll
       for (int j = 0; j < PPL; ++j) {
         const int p = lane + 32 * j;
-        CSum<T> mu;
-        mu.init(p < Pn ? -sC[p] : T(0));
-        if constexpr (sizeof(T) == 4)
-          mu.lo = p < Pn ? -(reinterpret_cast<const T*>(st + L.oCl) + jv * Pnp)[p] : T(0);
-        if (packed) {
-#pragma unroll
-          for (int w = 0; w < kPackDeg / 4; ++w) {
-            if (4 * w < maxdeg) {  // uniform over the warp
-              const uint32_t x = pk[j][w];
-              mu.add(sfr[x & 0xffu]);
-              mu.add(sfr[(x >> 8) & 0xffu]);
-              mu.add(sfr[(x >> 16) & 0xffu]);
-              mu.add(sfr[x >> 24]);
-            }
-          }
-        } else {
-          const int* inc = s_inc + j * maxdeg * 32 + lane;
-          for (int t = 0; t < maxdeg; ++t) mu.add(sfr[inc[t * 32]]);
-        }
-        smu[p] = mu.hi;
-        if constexpr (sizeof(T) == 4) smu[32 * PPL + p] = mu.lo;
         if (p < Pn) {
-          lmu[j].add2_fast(mu.hi, mu.lo);
-          if (plast[j]) a.mu_raw[(size_t)v * Pn + p] = mu.dvalue();
-          if (a.rec_mh) {
-            a.rec_mh[(size_t)v * Pn + p] = mu.hi;
-            a.rec_ml[(size_t)v * Pn + p] = mu.lo;
+          T* c = st + G.oC + jv * Pnp + p;
+          *c = -*c;
+          if constexpr (sizeof(T) == 4) c[G.oCl - G.oC] = -c[G.oCl - G.oC];
+        }
+      }
+    }
+    __syncwarp();
+    // ---- 2. the compensated sums of the stage's (vertex, p) jobs, four terms
+    // per step: their schedule words in one 16-byte load, their values loaded
+    // before the dependent additions
+    {
+      T hi = T(0), lo = T(0);
+      const uint4* sch = reinterpret_cast<const uint4*>(s_sched) + lane;
+      for (int t4 = 0; t4 < nterms / 4; ++t4) {
+        const uint4 w4 = sch[t4 * 32];
+        const uint32_t w[4] = {w4.x, w4.y, w4.z, w4.w};
+        T x[4], xl[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const T* xp = st + (w[u] & 0xfffu);
+          x[u] = *xp;
+          if constexpr (sizeof(T) == 4) xl[u] = (w[u] & kSchedStart) ? xp[G.oCl - G.oC] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const bool first = (w[u] & kSchedStart) != 0;
+          const T h0 = first ? T(0) : hi;
+          if constexpr (sizeof(T) == 4) {
+            // a job starts from (0, -CV_lo) and adds -CV_hi: exactly (-CV_hi, -CV_lo)
+            const T l0 = first ? xl[u] : lo;
+            const T sm = h0 + x[u];
+            const T bp = sm - h0;
+            lo = l0 + ((h0 - (sm - bp)) + (x[u] - bp));
+            hi = sm;
+          } else {
+            hi = h0 + x[u];
+          }
+          if (w[u] & kSchedEnd) {
+            const int slot = (int)((w[u] >> 16) & 0x1ffu);
+            smu[slot] = hi;
+            if constexpr (sizeof(T) == 4) smu[kMuLo + slot] = lo;
           }
         }
       }
-      __syncwarp();
+    }
+    __syncwarp();
+    // ---- 3. per staged vertex: MU_raw outputs, new Y and Z; the FP32 column
+    // log-sum-exps take the stage's values four at a time
+    constexpr bool kBatch = sizeof(T) == 4 && kVps == 4;
+    T lrv[QPL][kVps], lfv[QPL][kVps], muh[PPL][kVps], mul[PPL][kVps];
+#pragma unroll
+    for (int jv = 0; jv < kVps; ++jv) {
+#pragma unroll
+      for (int k = 0; k < QPL; ++k) lrv[k][jv] = lfv[k][jv] = neg_inf<T>();
+#pragma unroll
+      for (int j = 0; j < PPL; ++j) {
+        muh[j][jv] = neg_inf<T>();
+        mul[j][jv] = T(0);
+      }
+    }
+#pragma unroll
+    for (int jv = 0; jv < kVps; ++jv) {
+      if (jv >= nv) break;
+      const int v = v0 + jv;
+      const T* mu_hi = smu + jv * kMuRow;
+#pragma unroll
+      for (int j = 0; j < PPL; ++j) {
+        const int p = lane + 32 * j;
+        if (p < Pn) {
+          const T h = mu_hi[p];
+          const T l = sizeof(T) == 4 ? mu_hi[kMuLo + p] : T(0);
+          if constexpr (kBatch) {
+            muh[j][jv] = h;
+            mul[j][jv] = l;
+          } else {
+            lmu[j].add2_fast(h, l);
+          }
+          if (plast[j]) a.mu_raw[(size_t)v * Pn + p] = (double)h + (double)l;
+          if (a.rec_mh) {
+            a.rec_mh[(size_t)v * Pn + p] = h;
+            a.rec_ml[(size_t)v * Pn + p] = l;
+          }
+        }
+      }
       if (!a.last && qon) {
-        T yo[QPL], zo[QPL], fo[QPL];
+        T F[QPL], R[QPL], em[QPL], b[QPL], yo[QPL], zo[QPL], fo[QPL];
+        lds_n<T, QPL>(st + G.oM + jv * Pp + qo, F);
+        lds_n<T, QPL>(st + G.oY + jv * Pp + qo, R);
+        lds_n<T, QPL>(st + G.oE + jv * Pp + qo, em);
+        lds_n<T, QPL>(st + G.oB + jv * Pp + qo, b);
 #pragma unroll
         for (int k = 0; k < QPL; ++k) {
           // f = VF' - cR, r = VR' - cF: the shift comes off the compensated
           // MU_raw first, the small message after
           T f, r;
           if constexpr (sizeof(T) == 4) {
-            f = ((smu[qd[k]] - cRh[k]) - F[k]) + (smu[32 * PPL + qd[k]] - cRl[k]);
-            r = ((smu[qs[k]] - cFh[k]) - R[k]) + (smu[32 * PPL + qs[k]] - cFl[k]);
+            f = ((mu_hi[qd[k]] - cRh[k]) - F[k]) + (mu_hi[kMuLo + qd[k]] - cRl[k]);
+            r = ((mu_hi[qs[k]] - cFh[k]) - R[k]) + (mu_hi[kMuLo + qs[k]] - cFl[k]);
           } else {
-            f = (smu[qd[k]] - cRh[k]) - F[k];
-            r = (smu[qs[k]] - cFh[k]) - R[k];
+            f = (mu_hi[qd[k]] - cRh[k]) - F[k];
+            r = (mu_hi[qs[k]] - cFh[k]) - R[k];
           }
           if (qo + k < Pe) {
             mxF[k] = fmax(mxF[k], f);
             mxR[k] = fmax(mxR[k], r);
-            lr[k].add_fast(f + b[k]);
-            lf[k].add_fast(r + b[k]);
+            if constexpr (kBatch) {
+              lrv[k][jv] = f + b[k];
+              lfv[k][jv] = r + b[k];
+            } else {
+              lr[k].add_fast(f + b[k]);
+              lf[k].add_fast(r + b[k]);
+            }
             yo[k] = f - em[k];  // no out-edges: dEmin = +inf, Y = -inf
             zo[k] = r;
             fo[k] = f;
@@ -1020,6 +1064,15 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
           st_n<T, QPL>(a.rec_r + (size_t)v * Pp + qo, zo);
         }
       }
+    }
+    if constexpr (kBatch) {
+#pragma unroll
+      for (int k = 0; k < QPL; ++k) {
+        lr[k].add4_fast(lrv[k][0], lrv[k][1], lrv[k][2], lrv[k][3]);
+        lf[k].add4_fast(lfv[k][0], lfv[k][1], lfv[k][2], lfv[k][3]);
+      }
+#pragma unroll
+      for (int j = 0; j < PPL; ++j) lmu[j].add2x4_fast(muh[j], mul[j]);
     }
     __syncwarp();  // this stage's buffer is free for the stage after next
   }
@@ -1149,8 +1202,8 @@ size_t vertex_update_smem(int pn, int pe, int pp) {
 }
 
 template <typename T, int QPL, int PPL>
-size_t vertex_warp_setup(int pn, int pe, int pp, int pnp, int maxdeg) {
-  const size_t sm = VwSmem<T, QPL, PPL>(pn, pe, pp, pnp, maxdeg).total;
+size_t vertex_warp_setup(int pn, int pe, int pp, int pnp, int nterms) {
+  const size_t sm = VwSmem<T, QPL, PPL>(pn, pe, pp, pnp, nterms).total;
   if (sm > 48 * 1024)
     cudaFuncSetAttribute(vertex_warp_kernel<T, QPL, PPL>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -1172,8 +1225,10 @@ bool warp_form(int pn, int pp, F&& f) {
 template <typename T>
 acg_status launch_vertex_update(const VertexUpdArgs<T>& a, int blocks, cudaStream_t s) {
   cudaError_t le = cudaSuccess;
+  if (a.vsched == nullptr && a.Pn > 0 && a.Pn <= 64 && a.Pp <= 64)
+    return set_error(ACG_ERR_INVALID_ARGUMENT, "vertex phase: no schedule for the warp form");
   const bool warp = warp_form(a.Pn, a.Pp, [&]<int QPL, int PPL>() {
-    const size_t sm = vertex_warp_setup<T, QPL, PPL>(a.Pn, a.Pe, a.Pp, a.Pnp, a.maxdeg);
+    const size_t sm = vertex_warp_setup<T, QPL, PPL>(a.Pn, a.Pe, a.Pp, a.Pnp, a.vterms);
     vertex_warp_kernel<T, QPL, PPL><<<blocks, kBT, sm, s>>>(a);
     le = cudaGetLastError();
   });
@@ -1192,10 +1247,10 @@ acg_status launch_vertex_update(const VertexUpdArgs<T>& a, int blocks, cudaStrea
 }
 
 template <typename T>
-int vertex_update_blocks(int pn, int pe, int pp, int pnp, int maxdeg, int num_sms, int dn) {
+int vertex_update_blocks(int pn, int pe, int pp, int pnp, int nterms, int num_sms, int dn) {
   int nb = 0;
   const bool warp = warp_form(pn, pp, [&]<int QPL, int PPL>() {
-    const size_t sm = vertex_warp_setup<T, QPL, PPL>(pn, pe, pp, pnp, maxdeg);
+    const size_t sm = vertex_warp_setup<T, QPL, PPL>(pn, pe, pp, pnp, nterms);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, vertex_warp_kernel<T, QPL, PPL>, kBT,
                                                       sm) != cudaSuccess)
       nb = 1;
@@ -1205,6 +1260,53 @@ int vertex_update_blocks(int pn, int pe, int pp, int pnp, int maxdeg, int num_sm
   const long long tiles = (dn + V - 1) / V;
   const long long b = (long long)num_sms * vertex_update_blocks_per_sm<T>(pn, pe, pp);
   return (int)(tiles < 1 ? 1 : (tiles < b ? tiles : b));
+}
+
+int vertex_warp_schedule(const int* pat, int pn, int pe, int pp, int pnp, std::vector<uint32_t>* out) {
+  out->clear();
+  if (pn <= 0 || pn > 64 || pp > 64) return 0;
+  const int ppl = pn <= 32 ? 1 : 2;
+  const VwStage G(pp, pnp, false);  // element offsets of M, Y, CV (the same for FP32 and FP64)
+  const int* inoff = pat + 2 * pe;
+  const int* inq = inoff + pn + 1;
+  const int* outoff = inq + pe;
+  const int* outq = outoff + pn + 1;
+  // jobs (jv, p), longest first (ties: jv, then p), each to the least loaded
+  // lane (ties: the lowest)
+  struct Job {
+    int jv, p, len;
+  };
+  std::vector<Job> jobs;
+  for (int jv = 0; jv < kVps; ++jv)
+    for (int p = 0; p < pn; ++p)
+      jobs.push_back({jv, p, 1 + inoff[p + 1] - inoff[p] + outoff[p + 1] - outoff[p]});
+  std::stable_sort(jobs.begin(), jobs.end(), [](const Job& x, const Job& y) { return x.len > y.len; });
+  std::vector<std::vector<uint32_t>> lanes(32);
+  for (const Job& j : jobs) {
+    int best = 0;
+    for (int l = 1; l < 32; ++l)
+      if (lanes[l].size() < lanes[best].size()) best = l;
+    std::vector<uint32_t>& L = lanes[best];
+    const uint32_t slot = (uint32_t)(j.jv * (32 * ppl + 1) + j.p) << 16;
+    std::vector<uint32_t> terms;
+    terms.push_back((uint32_t)(G.oC + j.jv * pnp + j.p));  // -CV
+    for (int i = inoff[j.p]; i < inoff[j.p + 1]; ++i)        // F[q], dst_q = p
+      terms.push_back((uint32_t)(G.oM + j.jv * pp + inq[i]));
+    for (int i = outoff[j.p]; i < outoff[j.p + 1]; ++i)      // R[q], src_q = p
+      terms.push_back((uint32_t)(G.oY + j.jv * pp + outq[i]));
+    terms.front() |= kSchedStart;
+    terms.back() |= kSchedEnd;
+    for (uint32_t& w : terms) L.push_back(w | slot);
+  }
+  size_t nt = 0;
+  for (const auto& L : lanes) nt = std::max(nt, L.size());
+  nt = (nt + 3) / 4 * 4;
+  // [t / 4][lane][t % 4]: a lane's four next words are one 16-byte load.
+  // Padding terms come after a lane's last job and change nothing it stores.
+  out->assign(nt * 32, 0u);
+  for (int l = 0; l < 32; ++l)
+    for (size_t t = 0; t < lanes[l].size(); ++t) (*out)[(t / 4) * 128 + l * 4 + t % 4] = lanes[l][t];
+  return (int)nt;
 }
 
 acg_status launch_capture_s(const double* S, const int* iters_p, int t, double* S_final, int Pn,

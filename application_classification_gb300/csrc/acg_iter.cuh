@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "acg_internal.h"
 
 namespace acg {
@@ -79,7 +81,16 @@ struct VertexUpdArgs {
   T* rec_ml = nullptr;
   // C-null term ([Pe], subtracted from both fills of each column; null: none)
   const double* cnull = nullptr;
+  // warp form (Pn <= 64, Pp <= 64): the per-lane schedule of the compensated
+  // MU_raw sums of one stage, [vterms][32] (vertex_warp_schedule)
+  const uint32_t* vsched = nullptr;
+  int vterms = 0;
 };
+// The warp form's schedule for a pattern (pat: the incidence arrays of
+// build_incidence): per lane, the terms of its (staged vertex, pattern vertex)
+// sums in order.  Returns the terms per lane, 0 when the pattern takes the
+// tile form.
+int vertex_warp_schedule(const int* pat, int pn, int pe, int pp, int pnp, std::vector<uint32_t>* out);
 // S_final[p] = S[p] of this iteration where it is p's last (S = the column
 // log-sum-exp of MU_raw in the statistics just finalised).
 acg_status launch_capture_s(const double* S, const int* iters_p, int t, double* S_final, int Pn,
@@ -139,7 +150,7 @@ int vertex_update_blocks_per_sm(int pn, int pe, int pp);
 // Grid of the vertex phase: the warp form (Pp <= 64, Pn <= 64) runs one wave
 // of resident blocks; the tile form one block per tile up to resident blocks.
 template <typename T>
-int vertex_update_blocks(int pn, int pe, int pp, int pnp, int maxdeg, int num_sms, int dn);
+int vertex_update_blocks(int pn, int pe, int pp, int pnp, int nterms, int num_sms, int dn);
 // Set every element of p[0, n) to v.
 template <typename T>
 acg_status launch_fill(T* p, size_t n, T v, cudaStream_t s);

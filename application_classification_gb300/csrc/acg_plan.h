@@ -31,10 +31,11 @@ struct acg_data {
   int* pos_in_dst = nullptr;  // [De] dst-CSR row of each src-CSR position
   int num_sms = acg::kNumSMs;
   // FP32 copies of the features for the mixed path, built on first use:
-  // nodes [Dn][Kv], edges [De][ke32] in dst-CSR order.
+  // nodes [Dn][kv32], edges [De][ke32] in dst-CSR order (rows zero-padded
+  // to a multiple of 4 features: 16-byte rows).
   float* nf32 = nullptr;
   float* ef32 = nullptr;
-  int ke32 = 0;
+  int kv32 = 0, ke32 = 0;
   // warp work splits, shared by every plan on this graph: key = (0 dst / 1 src
   // CSR, parts, positions per step, ranges per part, chunk divisor, chunk cap)
   std::map<std::tuple<int, int, int, int, int, int>, acg::WarpWork> work;
@@ -92,6 +93,8 @@ struct acg_plan {
   acg::WarpWork ew, sw;
   int edge_blocks = 1, src_blocks = 1, vert_blocks = 1;
   int maxdeg = 0;              // max over pattern vertices of in- plus out-degree
+  uint32_t* vsched = nullptr;  // vertex phase, warp form: per-lane schedule [vterms][32]
+  int vterms = 0;
   // work buffers (element type per precision)
   void* dE = nullptr;
   void* vf = nullptr;
@@ -119,6 +122,7 @@ struct acg_plan {
   int64_t launches = 0;
   bool ran = false;
   bool cdist_tc = false;       // edge cost matrix on the tensor cores
+  bool cdist_tc_v = false;     // vertex cost matrix on the tensor cores
   bool edge_tc = false;        // edge phase recomputes the costs on the tensor cores:
   acg::WarpWork etw;           // its item split (one part per CTA),
   float* et_part = nullptr;    // partial rows of heavy-vertex chunks [npartial][Pp]

@@ -23,7 +23,7 @@ from . import _lib
 from .graph import Graph
 
 PRECISIONS = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
-# acg_options.cdist_kernel: the mixed path's edge cost matrix
+# acg_options.cdist_kernel: the mixed path's edge and vertex cost matrices
 CDIST_KERNELS = {"auto": 0, "simt": 1, "tensor": 2}
 # acg_options.edge_kernel: the mixed path's edge phase (costs recomputed on the
 # tensor cores, or read from the stored edge cost matrix)

@@ -81,6 +81,10 @@ def parse():
     ap.add_argument("--edge-kernel", default="auto", choices=["auto", "stored", "fused"],
                     help="the mixed path's edge phase: read the stored edge cost matrix, or "
                          "recompute the costs on the tensor cores (acg_options.edge_kernel)")
+    ap.add_argument("--cdist-kernel", default="auto", choices=["auto", "simt", "tensor"],
+                    help="mixed path: cost matrices on the tensor cores where the shape allows "
+                         "(auto), always on the CUDA cores (simt), or tensor cores only "
+                         "(acg_options.cdist_kernel)")
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-fp64", action="store_true")
@@ -279,7 +283,8 @@ def run_ours(args, ws, rank, local):
     # ---- device-resident match
     dg = matcher.DataGraph(d)
     ek = args.edge_kernel if args.precision == "mixed" else "auto"
-    plan = matcher.Plan(dg, p, args.precision, edge_kernel=ek)
+    ck = args.cdist_kernel if args.precision == "mixed" else "auto"
+    plan = matcher.Plan(dg, p, args.precision, edge_kernel=ek, cdist_kernel=ck)
     out = torch.empty((d.num_nodes, p.num_nodes), dtype=torch.float64, device=dev)
     for _ in range(args.warmup):
         plan.run(out)
@@ -305,7 +310,7 @@ def run_ours(args, ws, rank, local):
     # per-phase durations (CUDA events around each phase of every iteration,
     # on a second plan so that the timed region above carries no extra events)
     del plan
-    tplan = matcher.Plan(dg, p, args.precision, kernel_timing=True, edge_kernel=ek)
+    tplan = matcher.Plan(dg, p, args.precision, kernel_timing=True, edge_kernel=ek, cdist_kernel=ck)
     tplan.run(out)
     phase = []
     for _ in range(min(args.steps, 3)):

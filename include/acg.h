@@ -83,13 +83,15 @@ typedef struct acg_options {
                          max-message fills of column q in every iteration.
                          0 (default): the reference's behaviour.  Single plans
                          only (acg_batch_create and the adjoint reject it). */
-  int32_t cdist_kernel; /* the edge cost matrix of the mixed-precision path:
-                           0 (default) tensor cores (tcgen05, TF32 split, see
-                           acg_cdist_tc.cu) when the shape allows it (edge
-                           feature dim <= 32, <= 128 padded pattern edges),
-                           else CUDA cores; 1 always CUDA cores; 2 tensor
-                           cores or ACG_ERR_UNSUPPORTED.  FP64 plans always
-                           use CUDA cores. */
+  int32_t cdist_kernel; /* the edge and vertex cost matrices of the
+                           mixed-precision path: 0 (default) each on the
+                           tensor cores (tcgen05, TF32 split, see
+                           acg_cdist_tc.cu) when its shape allows it
+                           (feature dim <= 32, <= 128 padded pattern edges /
+                           vertices), else on the CUDA cores; 1 always CUDA
+                           cores; 2 both on the tensor cores or
+                           ACG_ERR_UNSUPPORTED.  FP64 plans always use CUDA
+                           cores. */
   int32_t autotune;   /* acg_batch_create only: 1 = measure before grouping
                          (see acg_batch_create); 0 (default) = greedy packing
                          with the default launch shapes */

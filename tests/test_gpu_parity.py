@@ -294,18 +294,20 @@ def test_cnull_rejected_by_batch_and_adjoint(cuda):
     data.close()
 
 
-# (data vertices, data edges, edge feature dim, pattern vertices, pattern edges)
-TC_SHAPES = [(300, 3000, 17, 6, 10), (1000, 127, 17, 4, 5), (2000, 20000, 1, 5, 8),
-             (2000, 20001, 3, 8, 16), (5000, 60000, 32, 10, 33), (3000, 40000, 17, 16, 64),
-             (3000, 40000, 20, 30, 100)]
+# (data vertices, data edges, edge feature dim, pattern vertices, pattern edges,
+#  vertex feature dim)
+TC_SHAPES = [(300, 3000, 17, 6, 10, 13), (1000, 127, 17, 4, 5, 1), (2000, 20000, 1, 5, 8, 3),
+             (2000, 20001, 3, 8, 16, 32), (5000, 60000, 32, 10, 33, 20), (3000, 40000, 17, 16, 64, 8),
+             (3000, 40000, 20, 30, 100, 13), (129, 2000, 4, 33, 40, 4)]
 
 
-@pytest.mark.parametrize("dn,de,ke,pn,pe", TC_SHAPES)
-def test_cdist_tensor_cores_vs_cuda_cores(cuda, dn, de, ke, pn, pe):
-    """The mixed path's edge cost matrix on the tensor cores (TF32 split,
-    tcgen05) against the CUDA-core kernel and the oracle: ragged last tiles,
-    1..32 feature dims, 1..7 MMA column blocks."""
-    d = graph.gen_er(dn, de - pe, kv=13, ke=ke, seed=dn + de)
+@pytest.mark.parametrize("dn,de,ke,pn,pe,kv", TC_SHAPES)
+def test_cdist_tensor_cores_vs_cuda_cores(cuda, dn, de, ke, pn, pe, kv):
+    """The mixed path's edge and vertex cost matrices on the tensor cores (TF32
+    split, tcgen05; the vertex matrix with its column statistics) against the
+    CUDA-core kernels and the oracle: ragged last tiles, 1..32 feature dims,
+    1..8 MMA column blocks."""
+    d = graph.gen_er(dn, de - pe, kv=kv, ke=ke, seed=dn + de)
     d, p, _, _ = graph.plant(d, pn, pe, 0.05, seed=ke)
     ref = oracle.match(d, p)
     data = matcher.DataGraph(d)
@@ -322,8 +324,37 @@ def test_cdist_tensor_cores_vs_cuda_cores(cuda, dn, de, ke, pn, pe):
     assert _argmax_same(out["tensor"], ref, tol=1e-5)
 
 
-def test_cdist_tensor_cores_unsupported_shape(cuda):
-    d = graph.gen_er(200, 1000, kv=13, ke=40, seed=1)
+# wide patterns (up to the 128-column limit of both cost matrices): with no BP
+# iteration mu is the normalised vertex cost matrix, so its values and column
+# statistics are compared without the amplification of 32 mixed-precision
+# iterations (which wide patterns like these push past 1e-4 on the CUDA cores
+# too)
+WIDE_SHAPES = [(4000, 50000, 5, 100, 120, 17), (3000, 30000, 17, 128, 127, 13), (500, 3000, 8, 97, 100, 1)]
+
+
+@pytest.mark.parametrize("dn,de,ke,pn,pe,kv", WIDE_SHAPES)
+def test_vertex_cost_matrix_tensor_cores_wide(cuda, dn, de, ke, pn, pe, kv):
+    d = graph.gen_er(dn, de - pe, kv=kv, ke=ke, seed=dn + pn)
+    d, p, _, _ = graph.plant(d, pn, pe, 0.05, seed=kv)
+    ref = oracle.match(d, p, num_iters=0)
+    data = matcher.DataGraph(d)
+    out = {}
+    for kern in ("tensor", "simt"):
+        plan = matcher.Plan(data, p, "mixed", cdist_kernel=kern, num_iters=0)
+        out[kern] = plan.run().cpu().numpy()
+        plan.stats()
+        plan.close()
+    data.close()
+    assert np.abs(out["simt"] - ref).max() <= 2e-5
+    assert np.abs(out["tensor"] - ref).max() <= 2e-5
+    assert _argmax_same(out["tensor"], ref, tol=1e-5)
+
+
+@pytest.mark.parametrize("kv,ke", [(13, 40), (40, 13)])
+def test_cdist_tensor_cores_unsupported_shape(cuda, kv, ke):
+    """A feature dim above 32 on either side: "tensor" is refused, "auto" runs
+    that matrix on the CUDA cores (and the other one on the tensor cores)."""
+    d = graph.gen_er(200, 1000, kv=kv, ke=ke, seed=1)
     d, p, _, _ = graph.plant(d, 4, 6, 0.05, seed=1)
     data = matcher.DataGraph(d)
     with pytest.raises(AcgError) as e:
