@@ -555,6 +555,11 @@ acg_status run_cdist(acg_plan* P, acg_data* D, long long lim, const F* nf, int n
   CdistRbArgs<T, F> ae{ef, gather ? D->dcsr.eid : nullptr, D->dcsr.eid, P->pe, (T*)P->dE,
                        nullptr, D->De, D->De, lim, D->Ke, efs, P->Pe, P->Pp, P->Pp};
   if constexpr (std::is_same_v<T, float> && std::is_same_v<F, float>) {
+    if (P->cdist_tc && P->edge_costs_ready) {  // written while the features were uploaded
+      P->edge_costs_ready = false;
+      P->launches += 2;
+      return ACG_OK;
+    }
     if (P->cdist_tc) {
       ACG_TRY(launch_cdist_edges_tc(ef, efs, D->Ke, P->pe, P->Pe, P->Pp, (float*)P->dE, D->De,
                                     P->dev_err, D->num_sms, s));
@@ -1140,8 +1145,9 @@ acg_status acg_match_graphs_host(const acg_graph* data, const acg_graph* pattern
   if (!mu_out_host && data->num_nodes * pattern->num_nodes > 0)
     return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_match_graphs_host: mu_out_host is null");
   cudaStream_t s = (cudaStream_t)stream;
-  cudaStream_t s2 = nullptr;
-  cudaEvent_t ev = nullptr;
+  cudaStream_t s2 = nullptr, s3 = nullptr;
+  constexpr int kChunks = 16;  // edge-feature upload pieces (mixed precision)
+  cudaEvent_t ev = nullptr, ev_nodes = nullptr, ev_csr = nullptr, ev_plan = nullptr, ev_chunk[kChunks] = {};
   std::vector<DevBuf> tmp;
   acg_data* D = nullptr;
   acg_plan* P = nullptr;
@@ -1152,54 +1158,107 @@ acg_status acg_match_graphs_host(const acg_graph* data, const acg_graph* pattern
     return st == ACG_OK;
   };
   cuda_ok(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking), "stream");
-  cuda_ok(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
-  // device copies of the four arrays of each graph: allocate, then copy the
-  // endpoints (the CSRs need them) on `stream` and the features on the second
-  // stream, which run while the CSRs are built
+  cuda_ok(cudaStreamCreateWithFlags(&s3, cudaStreamNonBlocking), "stream");
+  for (cudaEvent_t* e : {&ev, &ev_nodes, &ev_csr, &ev_plan}) cuda_ok(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event");
+  for (auto& e : ev_chunk) cuda_ok(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+  // Device copies of the four arrays of each graph: the endpoints (the CSRs
+  // need them) and the pattern on `stream`, the data features on the second
+  // stream while the CSRs are built.  The host link (~210 GB/s, the same for
+  // copy engines and for kernels reading pinned memory) is the critical path,
+  // so with mixed precision the edge features go up in pieces and a third
+  // stream turns each piece, as it lands, into its FP32 rows (destination-CSR
+  // order, through the inverse of the CSR's edge order) and, once the plan
+  // exists, into its rows of the edge cost matrix: the match then starts with
+  // dE written.  FP64 plans read the caller's FP64 features and wait for them.
   acg_graph dg = *data, pg = *pattern;
   const size_t m = data->num_edges, n = data->num_nodes;
+  const bool mixed = opt && opt->precision == ACG_PREC_MIXED;
+  const bool chunked = mixed && m > 0 && data->edge_feat_dim > 0 && n > 0 && data->node_feat_dim > 0;
   struct Up {
     const void* h;
     size_t bytes;
-    bool second;
+    int lane;  // 0: stream, 1: second stream, 2: second stream in pieces
     const void** out;
   };
   const Up ups[] = {
-      {data->srcs, 8 * m, false, (const void**)&dg.srcs},
-      {data->dsts, 8 * m, false, (const void**)&dg.dsts},
-      {pattern->srcs, 8 * pattern->num_edges, false, (const void**)&pg.srcs},
-      {pattern->dsts, 8 * pattern->num_edges, false, (const void**)&pg.dsts},
-      {pattern->node_feats, 8 * pattern->num_nodes * pattern->node_feat_dim, false, (const void**)&pg.node_feats},
-      {pattern->edge_feats, 8 * pattern->num_edges * pattern->edge_feat_dim, false, (const void**)&pg.edge_feats},
-      {data->node_feats, 8 * n * data->node_feat_dim, true, (const void**)&dg.node_feats},
-      {data->edge_feats, 8 * m * data->edge_feat_dim, true, (const void**)&dg.edge_feats}};
+      {data->srcs, 8 * m, 0, (const void**)&dg.srcs},
+      {data->dsts, 8 * m, 0, (const void**)&dg.dsts},
+      {pattern->srcs, 8 * pattern->num_edges, 0, (const void**)&pg.srcs},
+      {pattern->dsts, 8 * pattern->num_edges, 0, (const void**)&pg.dsts},
+      {pattern->node_feats, 8 * pattern->num_nodes * pattern->node_feat_dim, 0, (const void**)&pg.node_feats},
+      {pattern->edge_feats, 8 * pattern->num_edges * pattern->edge_feat_dim, 0, (const void**)&pg.edge_feats},
+      {data->node_feats, 8 * n * data->node_feat_dim, 1, (const void**)&dg.node_feats},
+      {data->edge_feats, 8 * m * data->edge_feat_dim, chunked ? 2 : 1, (const void**)&dg.edge_feats}};
   void* dptr[8] = {};
   for (int i = 0; i < 8 && st == ACG_OK; ++i)
     if (ups[i].h && ups[i].bytes) st = dev_alloc(&tmp, ups[i].bytes, &dptr[i], s);
-  cuda_ok(cudaStreamSynchronize(s), "alloc");  // the allocations exist for both streams
-  for (int i = 0; i < 8 && st == ACG_OK; ++i)
-    if (dptr[i] && cuda_ok(cudaMemcpyAsync(dptr[i], ups[i].h, ups[i].bytes, cudaMemcpyHostToDevice,
-                                           ups[i].second ? s2 : s), "copy"))
-      *ups[i].out = dptr[i];
+  cuda_ok(cudaStreamSynchronize(s), "alloc");  // the allocations exist for every stream
+  const size_t ke = data->edge_feat_dim;
+  auto piece = [&](int c) { return std::make_pair(m * c / kChunks, m * (c + 1) / kChunks); };
+  for (int i = 0; i < 8 && st == ACG_OK; ++i) {
+    if (!dptr[i]) continue;
+    if (ups[i].lane == 2) {
+      for (int c = 0; c < kChunks && st == ACG_OK; ++c) {
+        const auto [e0, e1] = piece(c);
+        if (e1 > e0)
+          cuda_ok(cudaMemcpyAsync((double*)dptr[i] + e0 * ke, (const double*)ups[i].h + e0 * ke,
+                                  (e1 - e0) * ke * 8, cudaMemcpyHostToDevice, s2), "copy");
+        cuda_ok(cudaEventRecord(ev_chunk[c], s2), "event record");
+      }
+    } else {
+      cuda_ok(cudaMemcpyAsync(dptr[i], ups[i].h, ups[i].bytes, cudaMemcpyHostToDevice, ups[i].lane ? s2 : s),
+              "copy");
+    }
+    if (st == ACG_OK) *ups[i].out = dptr[i];
+    if (i == 6) cuda_ok(cudaEventRecord(ev_nodes, s2), "event record");
+  }
   cuda_ok(cudaEventRecord(ev, s2), "event record");
   double* mu = nullptr;
   if (st == ACG_OK) st = dev_alloc(&tmp, sizeof(double) * n * pattern->num_nodes, (void**)&mu, s);
   if (st == ACG_OK) st = acg_data_create(&dg, s, &D);  // reads the endpoints only
-  // Mixed precision reads the data features only through their FP32 copies:
-  // those are made on the second stream once the features and the CSRs are
-  // there, while the plan is built on `stream` (the host link, ~210 GB/s, is
-  // the critical path).  FP64 plans wait for the features first.
-  const bool mixed = opt && opt->precision == ACG_PREC_MIXED;
-  if (st == ACG_OK && mixed) {
-    cudaEvent_t csr = nullptr;
-    if (cuda_ok(cudaEventCreateWithFlags(&csr, cudaEventDisableTiming), "event") &&
-        cuda_ok(cudaEventRecord(csr, s), "event record") && cuda_ok(cudaStreamWaitEvent(s2, csr, 0), "wait"))
+  int* pos = nullptr;
+  float* x32 = nullptr;
+  if (st == ACG_OK && chunked) {
+    // the FP32 copies ensure_f32 would make, made here piece by piece
+    D->kv32 = (D->Kv + 3) / 4 * 4;
+    D->ke32 = (D->Ke + 3) / 4 * 4;
+    float *nf = nullptr, *ef = nullptr;
+    st = dev_alloc(&D->owned, sizeof(float) * (size_t)D->Dn * D->kv32, (void**)&nf, s);
+    if (st == ACG_OK) st = dev_alloc(&D->owned, sizeof(float) * (size_t)D->De * D->ke32, (void**)&ef, s);
+    if (st == ACG_OK) st = dev_alloc(&tmp, sizeof(int) * (size_t)D->De, (void**)&pos, s);
+    if (st == ACG_OK) st = dev_alloc(&tmp, sizeof(float) * (size_t)D->De * D->ke32, (void**)&x32, s);
+    if (st == ACG_OK && cuda_ok(cudaEventRecord(ev_csr, s), "event record") &&
+        cuda_ok(cudaStreamWaitEvent(s3, ev_csr, 0), "wait")) {
+      st = launch_inverse_perm(D->dcsr.eid, D->De, pos, s3);
+      if (st == ACG_OK && cuda_ok(cudaStreamWaitEvent(s3, ev_nodes, 0), "wait"))
+        st = launch_convert_rows(D->node_feats, nullptr, D->Dn, D->Kv, nf, D->kv32, s3);
+      D->nf32 = nf;  // the plan finds the copies made (on s3, which `stream` waits for below)
+      D->ef32 = ef;
+    }
+  } else if (st == ACG_OK && mixed) {
+    if (cuda_ok(cudaEventRecord(ev_csr, s), "event record") && cuda_ok(cudaStreamWaitEvent(s2, ev_csr, 0), "wait"))
       st = ensure_f32(D, s2);
-    if (csr) cudaEventDestroy(csr);
     cuda_ok(cudaEventRecord(ev, s2), "event record");
   }
   if (st == ACG_OK && !mixed) cuda_ok(cudaStreamWaitEvent(s, ev, 0), "wait");
   if (st == ACG_OK) st = acg_plan_create(D, &pg, opt, s, &P);
+  if (st == ACG_OK && chunked) {
+    // each piece as it lands: FP32 rows, then (tensor-core plans) its rows of dE
+    const bool costs = P->cdist_tc && P->Pe > 0;
+    if (costs && cuda_ok(cudaEventRecord(ev_plan, s), "event record"))
+      cuda_ok(cudaStreamWaitEvent(s3, ev_plan, 0), "wait");
+    for (int c = 0; c < kChunks && st == ACG_OK; ++c) {
+      const auto [e0, e1] = piece(c);
+      if (e1 <= e0 || !cuda_ok(cudaStreamWaitEvent(s3, ev_chunk[c], 0), "wait")) continue;
+      st = launch_convert_scatter(D->edge_feats, (long long)e0, (long long)e1, D->Ke, pos, x32, D->ef32,
+                                  D->ke32, s3);
+      if (st == ACG_OK && costs)
+        st = launch_cdist_edges_tc(x32 + e0 * D->ke32, D->ke32, D->Ke, P->pe, P->Pe, P->Pp, (float*)P->dE,
+                                   (long long)(e1 - e0), P->dev_err, D->num_sms, s3, pos + e0);
+    }
+    if (st == ACG_OK) P->edge_costs_ready = costs;
+    cuda_ok(cudaEventRecord(ev, s3), "event record");
+  }
   if (st == ACG_OK && mixed) cuda_ok(cudaStreamWaitEvent(s, ev, 0), "wait");
   if (st == ACG_OK) st = acg_match(P, mu, s);
   if (st == ACG_OK && n * pattern->num_nodes > 0)
@@ -1207,11 +1266,16 @@ acg_status acg_match_graphs_host(const acg_graph* data, const acg_graph* pattern
                             cudaMemcpyDeviceToHost, s), "copy back");
   if (st == ACG_OK) cuda_ok(cudaStreamSynchronize(s), "synchronise");
   if (s2) cudaStreamSynchronize(s2);
+  if (s3) cudaStreamSynchronize(s3);
   acg_plan_destroy(P);
   acg_data_destroy(D);
   dev_free_all(&tmp);
-  if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t e : {ev, ev_nodes, ev_csr, ev_plan})
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : ev_chunk)
+    if (e) cudaEventDestroy(e);
   if (s2) cudaStreamDestroy(s2);
+  if (s3) cudaStreamDestroy(s3);
   return st;
 }
 

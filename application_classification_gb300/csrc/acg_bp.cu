@@ -196,6 +196,26 @@ __global__ void convert_rows_kernel(const double* __restrict__ src, const int* _
   dst[t] = x;
 }
 
+// Rows [e0, e1) of src (original edge order) as FP32, zero padded to kstride:
+// into x32 in the same order and into dst at row pos[e].
+__global__ void convert_scatter_kernel(const double* __restrict__ src, long long e0, long long e1, int K,
+                                       const int* __restrict__ pos, float* __restrict__ x32,
+                                       float* __restrict__ dst, int kstride) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (e1 - e0) * kstride) return;
+  const long long e = e0 + t / kstride;
+  const int k = (int)(t % kstride);
+  const float x = k < K ? __double2float_rn(src[(size_t)e * K + k]) : 0.f;
+  x32[(size_t)e * kstride + k] = x;
+  dst[(size_t)__ldg(pos + e) * kstride + k] = x;
+}
+
+// pos[perm[r]] = r
+__global__ void inverse_perm_kernel(const int* __restrict__ perm, long long n, int* __restrict__ pos) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) pos[perm[r]] = (int)r;
+}
+
 // ------------------------------------------------------ init vertex pass
 // CV = dV - LSE_v(dV), MU0 = -dV - LSE_v(-dV) (main.cu:112,116-117);
 // RMax0/FMax0 from the quirk buffer maxima (main.cu:113-114,119-120,135-146);
@@ -390,6 +410,22 @@ acg_status launch_convert_rows(const double* src, const int* row, long long n, i
   const long long tot = n * kstride;
   if (tot == 0) return ACG_OK;
   convert_rows_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(src, row, n, K, dst, kstride);
+  ACG_LAUNCH_CHECK();
+  return ACG_OK;
+}
+
+acg_status launch_convert_scatter(const double* src, long long e0, long long e1, int K, const int* pos,
+                                  float* x32, float* dst, int kstride, cudaStream_t s) {
+  const long long tot = (e1 - e0) * kstride;
+  if (tot <= 0) return ACG_OK;
+  convert_scatter_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(src, e0, e1, K, pos, x32, dst, kstride);
+  ACG_LAUNCH_CHECK();
+  return ACG_OK;
+}
+
+acg_status launch_inverse_perm(const int* perm, long long n, int* pos, cudaStream_t s) {
+  if (n == 0) return ACG_OK;
+  inverse_perm_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(perm, n, pos);
   ACG_LAUNCH_CHECK();
   return ACG_OK;
 }

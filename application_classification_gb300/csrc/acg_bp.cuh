@@ -39,6 +39,12 @@ acg_status launch_finalize(const double* bpart, int nblocks, StatSpec spec, doub
 // dst[i][k] = (float)src[row ? row[i] : i][k] for k < K, zero up to kstride.
 acg_status launch_convert_rows(const double* src, const int* row, long long n, int K, float* dst,
                                int kstride, cudaStream_t s);
+// Rows [e0, e1) of src (original edge order) to FP32 (zero padded to kstride):
+// into x32 in the same order and into dst at row pos[e].
+acg_status launch_convert_scatter(const double* src, long long e0, long long e1, int K, const int* pos,
+                                  float* x32, float* dst, int kstride, cudaStream_t s);
+// pos[perm[r]] = r for r < n
+acg_status launch_inverse_perm(const int* perm, long long n, int* pos, cudaStream_t s);
 
 template <typename T>
 struct InitArgs {

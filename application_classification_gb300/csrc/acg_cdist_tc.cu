@@ -79,6 +79,7 @@ struct TcArgs {
   const double* y;  // [P][K]
   float* out;       // [nrows][Pp]
   double* bpart;    // vertex matrix: block partials (StatSpec{P, 2P}), one column per CTA
+  const int* rowmap;  // optional output row of each input row (null: the same row)
   int* err;         // set to 1 when a bounded wait gave up
   long long nrows;
   int K, P, Pp, N, tcols;
@@ -290,9 +291,11 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int rr = i * 8 + (lane >> 2);
-          if (rw + rr < nr && col < Pp)
-            *reinterpret_cast<float4*>(a.out + (size_t)(r0 + rw + rr) * Pp + col) =
+          if (rw + rr < nr && col < Pp) {
+            const long long orow = a.rowmap ? (long long)__ldg(a.rowmap + r0 + rw + rr) : r0 + rw + rr;
+            *reinterpret_cast<float4*>(a.out + (size_t)orow * Pp + col) =
                 *reinterpret_cast<const float4*>(stg + rr * kStg + qt * 4);
+          }
         }
         if constexpr (STATS) {
           const int q = c * 16 + (lane & 15), h0 = (lane >> 4) * 16;
@@ -422,8 +425,9 @@ static acg_status launch_km(const TcArgs& a, int kstride, int num_sms, int max_g
 }
 
 static TcArgs tc_args(const float* x, int K, const double* y, int P, int Pp, float* out, double* bpart,
-                      long long nrows, int* err) {
+                      long long nrows, int* err, const int* rowmap = nullptr) {
   TcArgs a;
+  a.rowmap = rowmap;
   a.x = x;
   a.y = y;
   a.out = out;
@@ -439,11 +443,13 @@ static TcArgs tc_args(const float* x, int K, const double* y, int P, int Pp, flo
 }
 
 acg_status launch_cdist_edges_tc(const float* x, int kstride, int K, const double* y, int P, int Pp,
-                                 float* out, long long nrows, int* err, int num_sms, cudaStream_t s) {
+                                 float* out, long long nrows, int* err, int num_sms, cudaStream_t s,
+                                 const int* rowmap) {
   if (P == 0 || nrows == 0) return ACG_OK;
   if (!cdist_tc_eligible(K, kstride, P, Pp))
     return set_error(ACG_ERR_UNSUPPORTED, "tensor-core cdist: K=%d, %d columns", K, P);
-  return launch_km<false>(tc_args(x, K, y, P, Pp, out, nullptr, nrows, err), kstride, num_sms, 0, nullptr, s);
+  return launch_km<false>(tc_args(x, K, y, P, Pp, out, nullptr, nrows, err, rowmap), kstride, num_sms, 0,
+                          nullptr, s);
 }
 
 acg_status launch_cdist_vertex_tc(const float* x, int kstride, int K, const double* y, int P, int Pp,

@@ -159,11 +159,13 @@ void dev_free_on(std::vector<DevBuf>* owned, cudaStream_t s) {
 // ---------------------------------------------------------------- scan
 namespace {
 
-// Short-lived scratch of the CSR build: the device's default stream-ordered
-// pool, or plain cudaMalloc when ACG_MEMPOOL=0.
+// Short-lived scratch of the CSR build and the work splits: the library's
+// pool (which keeps its memory, so a repeated build maps nothing new), or
+// plain cudaMalloc when ACG_MEMPOOL=0.
 cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
   if (injected_failure()) return cudaErrorMemoryAllocation;
-  return pool_enabled() ? cudaMallocAsync(p, bytes, s) : cudaMalloc(p, bytes);
+  cudaMemPool_t pool = device_pool();
+  return pool ? cudaMallocFromPoolAsync(p, bytes, pool, s) : cudaMalloc(p, bytes);
 }
 
 void scratch_free(void* p, cudaStream_t s) {

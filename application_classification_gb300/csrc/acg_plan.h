@@ -122,6 +122,7 @@ struct acg_plan {
   int64_t launches = 0;
   bool ran = false;
   bool cdist_tc = false;       // edge cost matrix on the tensor cores
+  bool edge_costs_ready = false;  // the next match finds dE already written (one-shot host call)
   bool cdist_tc_v = false;     // vertex cost matrix on the tensor cores
   bool edge_tc = false;        // edge phase recomputes the costs on the tensor cores:
   acg::WarpWork etw;           // its item split (one part per CTA),

@@ -87,6 +87,7 @@ def parse():
                          "(acg_options.cdist_kernel)")
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-warmup", type=int, default=2)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -442,13 +443,17 @@ def run_ours(args, ws, rank, local):
                                                         C.c_void_p(mu_host.data_ptr()),
                                                         C.c_void_p(stream.cuda_stream)), "e2e")
 
-        e2e_step()
+        for _ in range(args.e2e_warmup):  # the library's memory pool grows to its working size
+            e2e_step()
         torch.cuda.synchronize()
         barrier(ws)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
+        step_ms = []
         for _ in range(args.e2e_steps):
-            e2e_step()
+            t_0 = time.perf_counter()
+            e2e_step()  # returns once mu is in host memory
+            step_ms.append(round((time.perf_counter() - t_0) * 1e3, 1))
         e1.record(stream)
         torch.cuda.synchronize()
         barrier(ws)
@@ -457,8 +462,11 @@ def run_ours(args, ws, rank, local):
                          "h2d_bytes_per_step": int(sum(h.numel() * h.element_size() for h in hs)),
                          "d2h_bytes_per_step": int(mu_host.numel() * 8),
                          "steps": args.e2e_steps,
-                         "includes": "acg_match_graphs_host: H2D of both graphs (features overlapped "
-                                     "with the CSR build), CSR build, allocation, match, D2H of mu"}
+                         "includes": "acg_match_graphs_host: H2D of both graphs (mixed: the edge "
+                                     "features in 16 pieces, each turned into FP32 rows and edge-cost "
+                                     "rows as it lands, under the CSR build and the plan), CSR build, "
+                                     "allocation, match, D2H of mu",
+                         "warmup": args.e2e_warmup, "step_ms_host": step_ms}
         del hs
 
     # ---- CPU baseline (rank 0, N=1 only)

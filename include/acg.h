@@ -183,7 +183,11 @@ acg_status acg_match_graphs(const acg_graph* data, const acg_graph* pattern,
  * num_nodes] in host memory.  The edge endpoints are copied first and the data
  * graph's CSR orderings are built while the features are still being copied
  * (on a second stream); pinned host buffers let the copies run asynchronously.
- * Device memory comes from the library's pool.  Synchronises `stream`. */
+ * With ACG_PREC_MIXED the edge features go up in pieces, and each piece is
+ * turned into its FP32 rows and (tensor-core plans) its rows of the edge cost
+ * matrix as it lands (a third stream), so the match starts with the costs
+ * written; mu is bit-identical to acg_match's.  Device memory comes from the
+ * library's pool.  Synchronises `stream`. */
 acg_status acg_match_graphs_host(const acg_graph* data, const acg_graph* pattern,
                                  const acg_options* opt, double* mu_out_host, void* stream);
 
