@@ -820,6 +820,9 @@ acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& 
     }
   }
   P->cv_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), 64), nsm * 2));
+  // the tensor-core vertex matrix: up to four CTAs per SM (its per-tile chain
+  // is latency-bound; the launch takes what fits, at most this many)
+  if (P->cdist_tc_v) P->cv_blocks = std::max(1, std::min(ceil_div(std::max(1, Dn), 128), nsm * 4));
   P->ce_blocks = std::max(1, std::min(ceil_div(std::max(1, De), 256), nsm * 8));
 
   const size_t vrow = (size_t)Dn * Pp * eb;
