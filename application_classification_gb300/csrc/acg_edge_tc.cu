@@ -72,7 +72,6 @@ constexpr int kWarps = kConsWarp0 + kConsWarps;  // 27
 constexpr int kET = kWarps * 32;                 // 864 threads
 constexpr int kRing = 4;                         // gathered-row ring slots
 constexpr int kMaxCols = 64;
-constexpr long long kSpinCount = 1LL << 22;
 
 inline __host__ __device__ int zstride_of(int Pp) { return Pp % 8 == 0 ? Pp + 4 : Pp; }
 
@@ -109,23 +108,6 @@ enum { B_FFULL = 0, B_FEMPTY = 3, B_MMA = 6, B_NX = 8, B_ACCFREE = 10, B_ZFULL =
 enum { M_ABORT = 0, M_VREADY = 1, M_CLAIM = 2, M_FWAITED = 3, M_FISSUED = 4, M_MISSUED = 5,
        M_NYMAX = 6 /* float */, M_CONSUMED = 8 /* .. +kRing */ };
 
-__device__ __forceinline__ void named_bar(int id, int n) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
-}
-// Named barrier over n threads that also ANDs a predicate across them.
-__device__ __forceinline__ bool named_bar_and(int id, int n, bool pred) {
-  uint32_t r;
-  asm volatile(
-      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n barrier.red.and.pred p, %2, %3, q;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(r)
-      : "r"((uint32_t)pred), "r"(id), "r"(n)
-      : "memory");
-  return r != 0;
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
 __device__ __forceinline__ void cp16(uint32_t sdst, const void* gsrc) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sdst), "l"(gsrc) : "memory");
 }
@@ -134,36 +116,6 @@ __device__ __forceinline__ void cp_arrive(uint32_t bar) {
   asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
 }
 __device__ __forceinline__ void cp_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-__device__ __forceinline__ int ld_volatile(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
-
-// Bounded wait on an mbarrier phase that also gives up when another role has
-// recorded an abort.
-__device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, const int* abort) {
-  for (long long i = 0; i < kSpinCount; ++i) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if ((i & 63) == 63 && ld_volatile(abort)) return false;
-  }
-  return false;
-}
-// Bounded wait until *p >= target (a monotonic count in shared memory).
-__device__ __forceinline__ bool wait_count(const int* p, int target, const int* abort) {
-  for (long long i = 0; i < kSpinCount; ++i) {
-    if (ld_volatile(p) >= target) {
-      __threadfence_block();
-      return true;
-    }
-    if (ld_volatile(abort)) return false;
-    __nanosleep(32);
-  }
-  return false;
-}
 
 template <int KM>
 __global__ void __launch_bounds__(kET, 1) edge_tc_kernel(const EdgeTcArgs a) {

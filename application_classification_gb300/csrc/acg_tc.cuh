@@ -61,6 +61,57 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
   }
   return false;
 }
+// Role synchronisation of the warp-specialised kernels: named barriers over a
+// role's threads, arrivals, and waits that also give up once another role has
+// recorded an abort in shared memory.
+__device__ __forceinline__ void named_bar(int id, int n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+// Named barrier over n threads that also ANDs a predicate across them.
+__device__ __forceinline__ bool named_bar_and(int id, int n, bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n barrier.red.and.pred p, %2, %3, q;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)pred), "r"(id), "r"(n)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ int ld_volatile(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+
+// Bounded wait on an mbarrier phase that also gives up when another role has
+// recorded an abort.
+__device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, const int* abort) {
+  for (long long i = 0; i < kSpin; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((i & 63) == 63 && ld_volatile(abort)) return false;
+  }
+  return false;
+}
+// Bounded wait until *p >= target (a monotonic count in shared memory).
+__device__ __forceinline__ bool wait_count(const int* p, int target, const int* abort) {
+  for (long long i = 0; i < kSpin; ++i) {
+    if (ld_volatile(p) >= target) {
+      __threadfence_block();
+      return true;
+    }
+    if (ld_volatile(abort)) return false;
+    __nanosleep(32);
+  }
+  return false;
+}
+
 // Bulk copy global -> shared completing on `bar` (which expects `bytes`).
 // dst, src 16-byte aligned, bytes a multiple of 16.
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
