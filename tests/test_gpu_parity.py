@@ -298,15 +298,18 @@ def test_cnull_rejected_by_batch_and_adjoint(cuda):
 #  vertex feature dim)
 TC_SHAPES = [(300, 3000, 17, 6, 10, 13), (1000, 127, 17, 4, 5, 1), (2000, 20000, 1, 5, 8, 3),
              (2000, 20001, 3, 8, 16, 32), (5000, 60000, 32, 10, 33, 20), (3000, 40000, 17, 16, 64, 8),
-             (3000, 40000, 20, 30, 100, 13), (129, 2000, 4, 33, 40, 4)]
+             (3000, 40000, 20, 30, 100, 13), (129, 2000, 4, 33, 40, 4),
+             # 32 features x 112 columns: past the pipeline's shared memory, the chained kernel
+             (3000, 40000, 32, 30, 100, 13)]
 
 
 @pytest.mark.parametrize("dn,de,ke,pn,pe,kv", TC_SHAPES)
 def test_cdist_tensor_cores_vs_cuda_cores(cuda, dn, de, ke, pn, pe, kv):
     """The mixed path's edge and vertex cost matrices on the tensor cores (TF32
-    split, tcgen05; the vertex matrix with its column statistics) against the
-    CUDA-core kernels and the oracle: ragged last tiles, 1..32 feature dims,
-    1..8 MMA column blocks."""
+    split, tcgen05: the warp-specialised pipeline, or the chained kernel where
+    the pipeline's shared memory does not fit; the vertex matrix with its
+    column statistics) against the CUDA-core kernels and the oracle: ragged
+    last tiles, 1..32 feature dims, 1..8 MMA column blocks."""
     d = graph.gen_er(dn, de - pe, kv=kv, ke=ke, seed=dn + de)
     d, p, _, _ = graph.plant(d, pn, pe, 0.05, seed=ke)
     ref = oracle.match(d, p)
