@@ -83,6 +83,10 @@ def test_match_graphs_host_pieces(cuda, dn, de, ke, pn, pe):
     a = matcher.match_host(d, p, "mixed")
     b = matcher.match(d, p, "mixed")
     assert np.array_equal(a, b)
+    # the C-null term (it reads the edge cost matrix the pieces wrote)
+    a = matcher.match_host(d, p, "mixed", cnull=True)
+    b = matcher.match(d, p, "mixed", cnull=True)
+    assert np.array_equal(a, b)
 
 
 def test_release_cached_memory(cuda):
