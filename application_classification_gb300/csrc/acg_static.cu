@@ -78,6 +78,34 @@ __device__ __forceinline__ void kahan_add(T& s, T& c, T x) {
 template <typename T>
 __device__ __forceinline__ T exp_ref_limit() { return sizeof(T) == 4 ? T(60) : T(600); }
 
+// The FP32 one-vector-per-lane shapes stage the gathered dE rows through a
+// per-warp ring in shared memory with cp.async: a stage is one step's positions
+// (S * kSU rows, 2 KB), issued kSrcAhead stages ahead of the step that reads
+// it, so the rows in flight no longer cost registers.
+constexpr int kSrcAhead = 3;
+constexpr int kSrcSlots = kSrcAhead + 2;  // a step spans at most two stages
+constexpr int kSrcStageBytes = 32 * kSU * 16;
+template <typename T, int NQV>
+__host__ __device__ constexpr bool src_staged() { return sizeof(T) == 4 && NQV == 1; }
+template <typename T, int NQV>
+__host__ __device__ constexpr size_t src_stage_smem() {
+  return src_staged<T, NQV>() ? (size_t)(kST / 32) * kSrcSlots * kSrcStageBytes : 0;
+}
+__device__ __forceinline__ void src_cp16(void* sdst, const void* gsrc) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void src_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+// wait until at most n of this thread's copy groups are pending (n <= kSrcAhead)
+__device__ __forceinline__ void src_wait(int n) {
+  switch (n) {
+    case 0: asm volatile("cp.async.wait_group 0;\n" ::: "memory"); break;
+    case 1: asm volatile("cp.async.wait_group 1;\n" ::: "memory"); break;
+    case 2: asm volatile("cp.async.wait_group 2;\n" ::: "memory"); break;
+    default: asm volatile("cp.async.wait_group 3;\n" ::: "memory"); break;
+  }
+}
+
 #if ACG_SRC_MINB > 0
 #define ACG_SRC_BOUNDS __launch_bounds__(kST, ACG_SRC_MINB)
 #else
@@ -103,8 +131,46 @@ __device__ __forceinline__ void src_stats_range(const SrcStatsArgs<T>& a, int it
   for (int u = 0; u < kSU; ++u) {
     const int e = base + slot + S * u;
     const bool ok = e < item.z;
-    ridx[u] = ok ? __ldg(a.row_of + e) : 0;
+    ridx[u] = ok && !src_staged<T, NQV>() ? __ldg(a.row_of + e) : 0;
     eidx[u] = ok ? __ldg(a.eid + e) : 0;
+  }
+  // staged: the warp's positions [P0, P1) in stages of STEP rows, stage j in
+  // ring slot j % kSrcSlots
+  const int lane = threadIdx.x & 31;
+  const int P0 = item.y;
+  const int P1 = src_staged<T, NQV>() ? __ldg(a.items + it_end - 1).z : 0;
+  const int nst = (P1 - P0 + STEP - 1) / STEP;
+  VT* ring = nullptr;
+  int issued = 0;
+  // dE rows of the next stage to issue, loaded one stage ahead of their copies
+  int nrow[kSU];
+  auto load_rows = [&](int j) {
+#pragma unroll
+    for (int i = 0; i < kSU; ++i) {
+      const int e = P0 + j * STEP + (lane + 32 * i) / NPOW;
+      nrow[i] = j < nst && e < P1 ? __ldg(a.row_of + e) : 0;
+    }
+  };
+  auto issue_stage = [&]() {  // stage `issued`: STEP rows x NPOW chunks, kSU 16-byte chunks a lane
+    if (issued < nst) {
+      VT* dst = ring + (size_t)(issued % kSrcSlots) * (kSrcStageBytes / 16);
+#pragma unroll
+      for (int i = 0; i < kSU; ++i) {
+        const int c = lane + 32 * i, row = c / NPOW, qv = c % NPOW;
+        const int e = P0 + issued * STEP + row;
+        if (e < P1 && qv * W < Pp)
+          src_cp16(dst + c, reinterpret_cast<const VT*>(a.dE + (size_t)nrow[i] * Pp) + qv);
+      }
+    }
+    src_commit();  // one group per stage (empty past the range)
+    ++issued;
+    load_rows(issued);
+  };
+  if constexpr (src_staged<T, NQV>()) {
+    extern __shared__ __align__(16) unsigned char src_ring[];
+    ring = reinterpret_cast<VT*>(src_ring) + (size_t)(threadIdx.x >> 5) * kSrcSlots * (kSrcStageBytes / 16);
+    load_rows(0);
+    for (int j = 0; j < kSrcAhead; ++j) issue_stage();
   }
   // Per column: the minimum mn of dE and sum_i exp(-dE_i) (with a compensation
   // term; -dE <= 0, so the sum cannot overflow): one exponential and no branch
@@ -128,17 +194,38 @@ __device__ __forceinline__ void src_stats_range(const SrcStatsArgs<T>& a, int it
     VT x[kSU][NQV];
     bool okv[kSU];
     int ecur[kSU];
+    if constexpr (src_staged<T, NQV>()) {
+      // the stages this step reads (its first and last position's) in place,
+      // kSrcAhead more in flight
+      const int jlo = (base - P0) / STEP, jhi = min(nst - 1, (base + STEP - 1 - P0) / STEP);
+      __syncwarp();  // every lane is done with the slot the next issue rewrites
+      while (issued < jhi + 1 + kSrcAhead) issue_stage();
+      src_wait(issued - 1 - jhi);
+      __syncwarp();  // the other lanes' copies are visible
 #pragma unroll
-    for (int u = 0; u < kSU; ++u) {
-      const int e = base + slot + S * u;
-      okv[u] = e < item.z;
-      ecur[u] = eidx[u];
-#pragma unroll
-      for (int k = 0; k < NQV; ++k) {
-        const int qv = qc + NPOW * k;
-        x[u][k] = (okv[u] && qv * W < Pp)
-                      ? __ldg(reinterpret_cast<const VT*>(a.dE + (size_t)ridx[u] * Pp) + qv)
+      for (int u = 0; u < kSU; ++u) {
+        const int e = base + slot + S * u;
+        okv[u] = e < item.z;
+        ecur[u] = eidx[u];
+        const int rel = e - P0, j = rel / STEP;
+        (void)jlo;
+        x[u][0] = (okv[u] && qc * W < Pp)
+                      ? ring[(size_t)(j % kSrcSlots) * (kSrcStageBytes / 16) + (rel - j * STEP) * NPOW + qc]
                       : sfill<T>(pos_inf<T>());
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < kSU; ++u) {
+        const int e = base + slot + S * u;
+        okv[u] = e < item.z;
+        ecur[u] = eidx[u];
+#pragma unroll
+        for (int k = 0; k < NQV; ++k) {
+          const int qv = qc + NPOW * k;
+          x[u][k] = (okv[u] && qv * W < Pp)
+                        ? __ldg(reinterpret_cast<const VT*>(a.dE + (size_t)ridx[u] * Pp) + qv)
+                        : sfill<T>(pos_inf<T>());
+        }
       }
     }
     const bool item_done = base + STEP >= item.z;
@@ -153,7 +240,7 @@ __device__ __forceinline__ void src_stats_range(const SrcStatsArgs<T>& a, int it
     for (int u = 0; u < kSU; ++u) {
       const int e = nbase + slot + S * u;
       const bool ok = more && e < nend;
-      ridx[u] = ok ? __ldg(a.row_of + e) : 0;
+      ridx[u] = ok && !src_staged<T, NQV>() ? __ldg(a.row_of + e) : 0;
       eidx[u] = ok ? __ldg(a.eid + e) : 0;
     }
     // branch-free: a missing edge reads +inf, which changes no minimum, adds
@@ -254,11 +341,17 @@ __device__ __forceinline__ void src_stats_range(const SrcStatsArgs<T>& a, int it
     }
     base = nbase;
   }
+  if constexpr (src_staged<T, NQV>()) {
+    src_wait(0);  // nothing of this range in flight when the ring is reused
+    __syncwarp();
+  }
 }
 
 // The warp's own range first, then claimed ones (as edge_max_kernel).
+// The staged shapes keep two blocks (16 warps) per SM: their rows in flight sit
+// in shared memory, not in registers.
 template <typename T, int NPOW, int NQV>
-__global__ void ACG_SRC_BOUNDS
+__global__ void __launch_bounds__(kST, src_staged<T, NQV>() ? 2 : (ACG_SRC_MINB > 0 ? ACG_SRC_MINB : 1))
 src_stats_kernel(const SrcStatsArgs<T> a) {
   const int lane = threadIdx.x & 31;
   const int slot = lane / NPOW, qc = lane % NPOW;
@@ -648,11 +741,15 @@ bool init_warp_shape(int pn, int pp, F&& f) {
 
 }  // namespace
 
-#define ACG_SRC_LAUNCH(NP_, NQ_)                                           \
-  if (ws.npow == NP_ && ws.nqv == NQ_) {                                   \
-    src_stats_kernel<T, NP_, NQ_><<<blocks, kST, 0, s>>>(a);               \
-    ACG_LAUNCH_CHECK();                                                    \
-    return ACG_OK;                                                         \
+#define ACG_SRC_LAUNCH(NP_, NQ_)                                                            \
+  if (ws.npow == NP_ && ws.nqv == NQ_) {                                                    \
+    constexpr size_t sm = src_stage_smem<T, NQ_>();                                         \
+    if (sm > 48 * 1024)                                                                     \
+      ACG_CUDA_TRY(cudaFuncSetAttribute(src_stats_kernel<T, NP_, NQ_>,                      \
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)); \
+    src_stats_kernel<T, NP_, NQ_><<<blocks, kST, sm, s>>>(a);                               \
+    ACG_LAUNCH_CHECK();                                                                     \
+    return ACG_OK;                                                                          \
   }
 
 template <typename T>
@@ -691,8 +788,12 @@ acg_status launch_dst_quirk(const DstQuirkArgs<T>& a, WarpShape ws, int blocks, 
 
 #define ACG_SRC_OCC(NP_, NQ_)                                                           \
   if (ws.npow == NP_ && ws.nqv == NQ_) {                                                \
+    constexpr size_t sm = src_stage_smem<T, NQ_>();                                     \
+    if (sm > 48 * 1024)                                                                 \
+      cudaFuncSetAttribute(src_stats_kernel<T, NP_, NQ_>,                               \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);       \
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, src_stats_kernel<T, NP_, NQ_>, \
-                                                      kST, 0) != cudaSuccess)           \
+                                                      kST, sm) != cudaSuccess)          \
       nb = 1;                                                                           \
   }
 
