@@ -74,11 +74,23 @@ struct AdjWork {
   int* colsi = nullptr;                            // [2 Pe + Pn]
   double* ypart = nullptr;                         // pattern-gradient partials
   std::vector<DevBuf> owned;
+  // the backward as one CUDA graph (its launches are the same on every call
+  // with the same gradient pointers), captured on a stream of its own
+  cudaGraphExec_t gexec = nullptr;
+  cudaStream_t gstream = nullptr;
+  const void* gkey[5] = {};
+  bool gfailed = false;  // capture refused once: launch directly from then on
+  void drop_graph() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    gexec = nullptr;
+  }
 };
 
 void adj_free(acg_plan* P) {
   if (!P || !P->adj) return;
   dev_free_all(&P->adj->owned);
+  P->adj->drop_graph();
+  if (P->adj->gstream) cudaStreamDestroy(P->adj->gstream);
   delete P->adj;
   P->adj = nullptr;
 }
@@ -1657,6 +1669,7 @@ acg_status acg_match_record(acg_plan* P, double* mu_out, int32_t checkpoint_ever
   const int every = checkpoint_every > 0 ? checkpoint_every : 4;
   ACG_TRY(adj_alloc(P, every, s));
   P->adj->recorded = false;
+  P->adj->drop_graph();  // recorded afresh: the next backward is captured again
   P->last_stream = s;
   P->rec = &P->adj->ck;
   const acg_status st = run_match_any(P, mu_out, s, nullptr);
@@ -1678,9 +1691,45 @@ acg_status acg_backward(acg_plan* P, const double* grad_mu, double* g_data_node,
       (!g_pat_node && (long long)P->Pn * D->Kv > 0) || (!g_pat_edge && (long long)P->Pe * D->Ke > 0))
     return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_backward: a gradient output is null");
   cudaStream_t s = (cudaStream_t)stream;
-  return P->prec == ACG_PREC_FP64
-             ? run_backward<double>(P, grad_mu, g_data_node, g_data_edge, g_pat_node, g_pat_edge, s)
-             : run_backward<float>(P, grad_mu, g_data_node, g_data_edge, g_pat_node, g_pat_edge, s);
+  auto run = [&](cudaStream_t rs) {
+    return P->prec == ACG_PREC_FP64
+               ? run_backward<double>(P, grad_mu, g_data_node, g_data_edge, g_pat_node, g_pat_edge, rs)
+               : run_backward<float>(P, grad_mu, g_data_node, g_data_edge, g_pat_node, g_pat_edge, rs);
+  };
+  // About 150 launches, each short at small sizes: replayed as one graph.  A
+  // caller's stream that is itself being captured, and plans that time their
+  // phases with events, get the launches directly.
+  AdjWork* W = P->adj;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (W->gfailed || P->kernel_timing || cudaStreamIsCapturing(s, &cap) != cudaSuccess ||
+      cap != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return run(s);
+  }
+  const void* key[5] = {grad_mu, g_data_node, g_data_edge, g_pat_node, g_pat_edge};
+  if (W->gexec && !std::equal(key, key + 5, W->gkey)) W->drop_graph();
+  if (!W->gexec) {
+    if (!W->gstream) ACG_CUDA_TRY(cudaStreamCreateWithFlags(&W->gstream, cudaStreamNonBlocking));
+    ACG_CUDA_TRY(cudaStreamBeginCapture(W->gstream, cudaStreamCaptureModeThreadLocal));
+    const acg_status st = run(W->gstream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(W->gstream, &g);
+    if (st != ACG_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (ce != cudaSuccess || !g || cudaGraphInstantiate(&W->gexec, g, 0) != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      W->gexec = nullptr;
+      W->gfailed = true;
+      return run(s);
+    }
+    cudaGraphDestroy(g);
+    std::copy(key, key + 5, W->gkey);
+  }
+  ACG_CUDA_TRY(cudaGraphLaunch(W->gexec, s));
+  return ACG_OK;
 }
 
 }  // extern "C"
