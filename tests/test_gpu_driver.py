@@ -69,13 +69,15 @@ def test_match_graphs_host_equals_device_path(cuda):
 
 
 @pytest.mark.parametrize("dn,de,ke,pn,pe", [(50, 9, 17, 3, 2), (300, 3001, 17, 6, 10), (2000, 20003, 3, 8, 16),
-                                            (1000, 9000, 40, 5, 8), (500, 4000, 13, 20, 70)])
+                                            (1000, 9000, 40, 5, 8), (500, 4000, 13, 20, 70),
+                                            (500, 4000, 32, 30, 100)])
 def test_match_graphs_host_pieces(cuda, dn, de, ke, pn, pe):
     """Mixed precision: the one-shot call uploads the edge features in 16
     pieces and builds each piece's FP32 rows and edge-cost rows as it lands
     (rows scattered into destination-CSR order).  Same bits as the device path
     for piece sizes of 0 rows and ragged ones, a feature dim past the
-    tensor-core limit (FP32 rows only) and a pattern past 64 columns."""
+    tensor-core limit (FP32 rows only), a pattern past 64 columns, and one whose
+    cost matrix takes the chained tensor-core kernel (rows through its row map)."""
     from application_classification_gb300 import graph, matcher
 
     d = graph.gen_er(dn, de - pe, kv=13, ke=ke, seed=dn + de)
