@@ -462,9 +462,11 @@ acg_status run_match(acg_plan* P, double* mu_out, cudaStream_t s, const UnionOut
     sa.ctr = P->range_ctr;
     ACG_TRY(launch_src_stats<T>(sa, P->ws, P->src_blocks, s));
     ACG_TRY(launch_src_stats_combine<T>(sa, P->sw, s));
-    DstQuirkArgs<T> qa{P->ew.items, P->ew.nitems, P->ew.wsplit, D->dcsr.eid, (const T*)P->dE,
+    DstQuirkArgs<T> qa{P->ew.items, P->ew.nitems, P->ew.wsplit, D->dcsr.eid,
+                       (const T*)(P->dEq_cols ? P->dEq : P->dE),
                        (T*)P->Fq, (T*)P->part_iter, P->bpart, P->qlim_col, De, lim, Pp,
                        P->Pqc, P->qcov, P->ew.nparts};
+    qa.dstride = P->dEq_cols;
     ACG_TRY(launch_dst_quirk<T>(qa, P->qws, P->edge_blocks, s));
     if (P->qcov > 0 && P->ew.nitems > 0) {  // ge[q < Pqc]; the later columns stay -inf
       ACG_TRY(launch_finalize(P->bpart, P->edge_blocks, StatSpec{0, P->Pqc}, P->ge, s));
@@ -562,7 +564,8 @@ acg_status run_cdist(acg_plan* P, acg_data* D, long long lim, const F* nf, int n
     }
     if (P->cdist_tc) {
       ACG_TRY(launch_cdist_edges_tc(ef, efs, D->Ke, P->pe, P->Pe, P->Pp, (float*)P->dE, D->De,
-                                    P->dev_err, D->num_sms, s));
+                                    P->dev_err, D->num_sms, s, nullptr,
+                                    P->dEq_cols ? (float*)P->dEq : nullptr, P->dEq_cols));
       P->launches += 3;
       return ACG_OK;
     }
@@ -827,6 +830,11 @@ acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& 
 
   const size_t vrow = (size_t)Dn * Pp * eb;
   big((size_t)De * Pp * eb, &P->dE);
+  // the covered columns (q < qcov, at most 16) also as compact rows, which the
+  // quirk pass reads instead of whole cost rows; every plan has the slot (a
+  // batch shares its plans' workspaces slot by slot)
+  P->dEq_cols = (P->prec == ACG_PREC_MIXED && P->cdist_tc && P->qcov > 0 && P->Pqc <= 16) ? P->Pqc : 0;
+  big(P->dEq_cols ? (size_t)De * P->dEq_cols * sizeof(float) : 1, &P->dEq);
   big(vrow, &P->vf);
   big(vrow, &P->vr[0]);
   big(vrow, &P->vr[1]);
@@ -1257,7 +1265,8 @@ acg_status acg_match_graphs_host(const acg_graph* data, const acg_graph* pattern
                                   D->ke32, s3);
       if (st == ACG_OK && costs)
         st = launch_cdist_edges_tc(x32 + e0 * D->ke32, D->ke32, D->Ke, P->pe, P->Pe, P->Pp, (float*)P->dE,
-                                   (long long)(e1 - e0), P->dev_err, D->num_sms, s3, pos + e0);
+                                   (long long)(e1 - e0), P->dev_err, D->num_sms, s3, pos + e0,
+                                   P->dEq_cols ? (float*)P->dEq : nullptr, P->dEq_cols);
     }
     if (st == ACG_OK) P->edge_costs_ready = costs;
     cuda_ok(cudaEventRecord(ev, s3), "event record");

@@ -36,11 +36,13 @@ acg_status launch_cdist_edges(const CdistRbArgs<T, F>& a, int blocks, cudaStream
 
 // The edge cost matrix of the mixed path on the tensor cores (acg_cdist_tc.cu):
 // out[rowmap ? rowmap[r] : r][q] = ||x[r] - y[q]|| for q < P, 0 for P <= q < Pp;
-// x FP32 rows of stride kstride.  *err is set to 1 if a bounded wait gave up.
+// x FP32 rows of stride kstride.  With outq, the same rows' columns q < qcols
+// (a multiple of 4, at most 16) also go to outq[row][qcols].  *err is set to 1
+// if a bounded wait gave up.
 bool cdist_tc_eligible(int K, int kstride, int P, int Pp);
 acg_status launch_cdist_edges_tc(const float* x, int kstride, int K, const double* y, int P, int Pp,
                                  float* out, long long nrows, int* err, int num_sms, cudaStream_t s,
-                                 const int* rowmap = nullptr);
+                                 const int* rowmap = nullptr, float* outq = nullptr, int qcols = 0);
 // The vertex cost matrix of the mixed path on the tensor cores, with the
 // per-column statistics of kCdistVertex as block partials (StatSpec{P, 2P}),
 // one partial column per CTA: at most max_grid CTAs (0: no cap), the count

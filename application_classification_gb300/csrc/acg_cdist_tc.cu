@@ -80,6 +80,8 @@ struct TcArgs {
   float* out;       // [nrows][Pp]
   double* bpart;    // vertex matrix: block partials (StatSpec{P, 2P}), one column per CTA
   const int* rowmap;  // optional output row of each input row (null: the same row)
+  float* outq;        // optional compact copy of columns [0, qcols) ([nrows][qcols]; qcols <= 16)
+  int qcols;
   int* err;         // set to 1 when a bounded wait gave up
   long long nrows;
   int K, P, Pp, N, tcols;
@@ -293,8 +295,9 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
           const int rr = i * 8 + (lane >> 2);
           if (rw + rr < nr && col < Pp) {
             const long long orow = a.rowmap ? (long long)__ldg(a.rowmap + r0 + rw + rr) : r0 + rw + rr;
-            *reinterpret_cast<float4*>(a.out + (size_t)orow * Pp + col) =
-                *reinterpret_cast<const float4*>(stg + rr * kStg + qt * 4);
+            const float4 v4 = *reinterpret_cast<const float4*>(stg + rr * kStg + qt * 4);
+            *reinterpret_cast<float4*>(a.out + (size_t)orow * Pp + col) = v4;
+            if (col < a.qcols) *reinterpret_cast<float4*>(a.outq + (size_t)orow * a.qcols + col) = v4;
           }
         }
         if constexpr (STATS) {
@@ -612,7 +615,6 @@ __global__ void __launch_bounds__(kWsT, 1) cdist_ws_kernel(const TcArgs a) {
       const long long r0 = tile_of(it) * kTM;
       const float nx = snx[(it & 3) * kTM + r];
       const float thr = 0.125f * (nx + nymax);
-      const float* xr = a.x + (size_t)(r0 + (r < nr ? r : 0)) * KM;
       // output rows of the four rows this lane stores, i * 8 + lane / 4
       int orow[4];  // row indices fit 31 bits (the CSR positions are int)
 #pragma unroll
@@ -638,6 +640,7 @@ __global__ void __launch_bounds__(kWsT, 1) cdist_ws_kernel(const TcArgs a) {
             d[j] = d2 * rsqrtf(d2);
           }
         } else {
+          const float* xr = a.x + (size_t)(r0 + (r < nr ? r : 0)) * KM;  // rare: near pairs
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int q = c * 16 + j;
@@ -664,6 +667,18 @@ __global__ void __launch_bounds__(kWsT, 1) cdist_ws_kernel(const TcArgs a) {
             if (orow[i] >= 0)
               *reinterpret_cast<float4*>(a.out + (size_t)orow[i] * Pp + col) =
                   *reinterpret_cast<const float4*>(stg + (i * 8 + (lane >> 2)) * kStg + qt * 4);
+        }
+        if (c == 0 && col < a.qcols) {  // the covered columns' compact copy (qcols <= 16: chunk 0)
+#pragma unroll 1
+          for (int i = 0; i < 4; ++i) {
+            const int rr = q4 * 32 + i * 8 + (lane >> 2);
+            if (rr < nr) {  // the output row again (no register kept live for it)
+              const long long row = r0 + rr;
+              const long long o = a.rowmap ? (long long)__ldg(a.rowmap + row) : row;
+              *reinterpret_cast<float4*>(a.outq + (size_t)o * a.qcols + col) =
+                  *reinterpret_cast<const float4*>(stg + (i * 8 + (lane >> 2)) * kStg + qt * 4);
+            }
+          }
         }
         __syncwarp();
       }
@@ -742,9 +757,12 @@ static acg_status launch_km(const TcArgs& a, int kstride, int num_sms, int max_g
 }
 
 static TcArgs tc_args(const float* x, int K, const double* y, int P, int Pp, float* out, double* bpart,
-                      long long nrows, int* err, const int* rowmap = nullptr) {
+                      long long nrows, int* err, const int* rowmap = nullptr, float* outq = nullptr,
+                      int qcols = 0) {
   TcArgs a;
   a.rowmap = rowmap;
+  a.outq = outq;
+  a.qcols = outq ? qcols : 0;
   a.x = x;
   a.y = y;
   a.out = out;
@@ -787,11 +805,13 @@ static bool ws_fits(int kstride, int N) {
 
 acg_status launch_cdist_edges_tc(const float* x, int kstride, int K, const double* y, int P, int Pp,
                                  float* out, long long nrows, int* err, int num_sms, cudaStream_t s,
-                                 const int* rowmap) {
+                                 const int* rowmap, float* outq, int qcols) {
   if (P == 0 || nrows == 0) return ACG_OK;
   if (!cdist_tc_eligible(K, kstride, P, Pp))
     return set_error(ACG_ERR_UNSUPPORTED, "tensor-core cdist: K=%d, %d columns", K, P);
-  const TcArgs a = tc_args(x, K, y, P, Pp, out, nullptr, nrows, err, rowmap);
+  if (outq && (qcols % 4 || qcols > 16 || qcols > Pp))
+    return set_error(ACG_ERR_INVALID_ARGUMENT, "tensor-core cdist: compact copy of %d columns", qcols);
+  const TcArgs a = tc_args(x, K, y, P, Pp, out, nullptr, nrows, err, rowmap, outq, qcols);
   if (ws_fits(kstride, a.N)) {
     switch (kstride) {
       case 4: return launch_ws<4>(a, num_sms, s);

@@ -123,6 +123,8 @@ struct acg_plan {
   bool ran = false;
   bool cdist_tc = false;       // edge cost matrix on the tensor cores
   bool edge_costs_ready = false;  // the next match finds dE already written (one-shot host call)
+  void* dEq = nullptr;         // [De][dEq_cols]: the covered columns of dE, written with it
+  int dEq_cols = 0;            // (0: none; the quirk pass then reads dE)
   bool cdist_tc_v = false;     // vertex cost matrix on the tensor cores
   bool edge_tc = false;        // edge phase recomputes the costs on the tensor cores:
   acg::WarpWork etw;           // its item split (one part per CTA),

@@ -445,7 +445,7 @@ dst_quirk_kernel(const DstQuirkArgs<T> a) {
         for (int k = 0; k < NQV; ++k) {
           const int qv = qc + NPOW * k;
           x[u][k] = (ok && qv * W < Pqc)
-                        ? __ldcs(reinterpret_cast<const VT*>(a.dE + (size_t)e * Pp) + qv)
+                        ? __ldcs(reinterpret_cast<const VT*>(a.dE + (size_t)e * (a.dstride ? a.dstride : Pp)) + qv)
                         : sfill<T>(pos_inf<T>());
         }
       }

@@ -63,7 +63,7 @@ struct DstQuirkArgs {
   int nitems;
   const int* wsplit;
   const int* eid;      // [De] original edge id of each destination-order position
-  const T* dE;         // [De][Pp]
+  const T* dE;         // [De][dstride]: the cost rows, or their covered columns
   T* Fq;               // [Dn][Pqc]
   T* partial;          // [npartial][Pqc]
   double* bpart;       // [2 Pqc][blocks]
@@ -72,6 +72,8 @@ struct DstQuirkArgs {
   int Pp, Pqc, qcov;
   int nranges = 0;     // item ranges (wsplit has nranges + 1 entries); warp w
                        // does ranges w, w + warps, ...
+  int dstride = 0;     // row stride of dE as given: Pp, or Pqc for the compact
+                       // copy of the covered columns (0: Pp)
 };
 template <typename T>
 acg_status launch_dst_quirk(const DstQuirkArgs<T>& a, WarpShape ws, int blocks, cudaStream_t s);
