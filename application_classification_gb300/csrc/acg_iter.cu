@@ -36,6 +36,7 @@
 
 #include "acg_device.cuh"
 #include "acg_iter.cuh"
+#include "acg_vschedule.h"
 
 namespace acg {
 
@@ -727,26 +728,6 @@ vertex_update_kernel(const VertexUpdArgs<T> a) {
 #endif
 constexpr int kVps = ACG_VTX_VPS;  // vertices per stage
 constexpr int kVw = kBT / 32;
-// schedule word: element offset of the term in the stage (bits 0-11), first
-// term of its job (bit 12), last term (bit 13), the job's slot jv * (32 PPL + 1)
-// + p in the per-warp MU_raw rows (bits 16-24); stored [t / 4][lane][t % 4]
-constexpr uint32_t kSchedStart = 1u << 12, kSchedEnd = 1u << 13;
-
-// Element offsets of one stage: M, Y, dEmin, B rows [kVps][Pp], then the CV
-// rows [kVps][Pnp] and (FP32) their low parts.
-struct VwStage {
-  int oM, oY, oE, oB, oC, oCl, n;
-  __host__ __device__ VwStage(int Pp, int Pnp, bool lo) {
-    oM = 0;
-    oY = kVps * Pp;
-    oE = 2 * kVps * Pp;
-    oB = 3 * kVps * Pp;
-    oC = 4 * kVps * Pp;
-    oCl = oC + kVps * Pnp;
-    n = oCl + (lo ? kVps * Pnp : 0);
-  }
-};
-
 template <typename T, int QPL, int PPL>
 struct VwSmem {
   size_t pat, sched, ring, mu, total, stage, warp_ring, mu_n;
@@ -755,7 +736,7 @@ struct VwSmem {
     size_t o = 0;
     pat = o; o += a16(sizeof(int) * (size_t)(4 * Pe + 2 * (Pn + 1)));
     sched = o; o += a16(sizeof(uint32_t) * (size_t)nterms * 32);
-    stage = (size_t)VwStage(Pp, Pnp, sz == 4).n * sz;  // row sizes are 16-byte multiples
+    stage = (size_t)VwStage(Pp, Pnp, sz == 4, kVps).n * sz;  // row sizes are 16-byte multiples
     warp_ring = 2 * stage;
     const size_t red = sizeof(double) * (size_t)kVw * (6 * Pe + 2 * Pn);  // aliases the rings
     ring = o; o += a16(red > kVw * warp_ring ? red : kVw * warp_ring);
@@ -802,7 +783,7 @@ vertex_warp_kernel(const VertexUpdArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int Pe = a.Pe, Pn = a.Pn, Pp = a.Pp, Pnp = a.Pnp, Dn = a.Dn, nterms = a.vterms;
   const VwSmem<T, QPL, PPL> L(Pn, Pe, Pp, Pnp, nterms);
-  const VwStage G(Pp, Pnp, sizeof(T) == 4);
+  const VwStage G(Pp, Pnp, sizeof(T) == 4, kVps);
   const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
   int* s_pat = reinterpret_cast<int*>(smem + L.pat);
   uint32_t* s_sched = reinterpret_cast<uint32_t*>(smem + L.sched);
@@ -1263,50 +1244,7 @@ int vertex_update_blocks(int pn, int pe, int pp, int pnp, int nterms, int num_sm
 }
 
 int vertex_warp_schedule(const int* pat, int pn, int pe, int pp, int pnp, std::vector<uint32_t>* out) {
-  out->clear();
-  if (pn <= 0 || pn > 64 || pp > 64) return 0;
-  const int ppl = pn <= 32 ? 1 : 2;
-  const VwStage G(pp, pnp, false);  // element offsets of M, Y, CV (the same for FP32 and FP64)
-  const int* inoff = pat + 2 * pe;
-  const int* inq = inoff + pn + 1;
-  const int* outoff = inq + pe;
-  const int* outq = outoff + pn + 1;
-  // jobs (jv, p), longest first (ties: jv, then p), each to the least loaded
-  // lane (ties: the lowest)
-  struct Job {
-    int jv, p, len;
-  };
-  std::vector<Job> jobs;
-  for (int jv = 0; jv < kVps; ++jv)
-    for (int p = 0; p < pn; ++p)
-      jobs.push_back({jv, p, 1 + inoff[p + 1] - inoff[p] + outoff[p + 1] - outoff[p]});
-  std::stable_sort(jobs.begin(), jobs.end(), [](const Job& x, const Job& y) { return x.len > y.len; });
-  std::vector<std::vector<uint32_t>> lanes(32);
-  for (const Job& j : jobs) {
-    int best = 0;
-    for (int l = 1; l < 32; ++l)
-      if (lanes[l].size() < lanes[best].size()) best = l;
-    std::vector<uint32_t>& L = lanes[best];
-    const uint32_t slot = (uint32_t)(j.jv * (32 * ppl + 1) + j.p) << 16;
-    std::vector<uint32_t> terms;
-    terms.push_back((uint32_t)(G.oC + j.jv * pnp + j.p));  // -CV
-    for (int i = inoff[j.p]; i < inoff[j.p + 1]; ++i)        // F[q], dst_q = p
-      terms.push_back((uint32_t)(G.oM + j.jv * pp + inq[i]));
-    for (int i = outoff[j.p]; i < outoff[j.p + 1]; ++i)      // R[q], src_q = p
-      terms.push_back((uint32_t)(G.oY + j.jv * pp + outq[i]));
-    terms.front() |= kSchedStart;
-    terms.back() |= kSchedEnd;
-    for (uint32_t& w : terms) L.push_back(w | slot);
-  }
-  size_t nt = 0;
-  for (const auto& L : lanes) nt = std::max(nt, L.size());
-  nt = (nt + 3) / 4 * 4;
-  // [t / 4][lane][t % 4]: a lane's four next words are one 16-byte load.
-  // Padding terms come after a lane's last job and change nothing it stores.
-  out->assign(nt * 32, 0u);
-  for (int l = 0; l < 32; ++l)
-    for (size_t t = 0; t < lanes[l].size(); ++t) (*out)[(t / 4) * 128 + l * 4 + t % 4] = lanes[l][t];
-  return (int)nt;
+  return vertex_warp_schedule(pat, pn, pe, pp, pnp, kVps, out);
 }
 
 acg_status launch_capture_s(const double* S, const int* iters_p, int t, double* S_final, int Pn,
