@@ -235,6 +235,48 @@ def test_quirk_full_coverage(cuda):
     assert np.abs(matcher.match(d, p) - ref).max() <= 1e-10 * max(1, np.abs(ref).max())
 
 
+def _degenerate_graphs():
+    """Small graphs at the edges of the input space, each valid for the
+    reference's Graph layout (any endpoint below the vertex count)."""
+    rng = np.random.default_rng(11)
+
+    def g(n, edges):
+        e = np.array(edges, np.uint64).reshape(-1, 2)
+        return graph.Graph(rng.normal(size=(n, 13)), rng.normal(size=(len(e), 17)),
+                           e[:, 0].copy(), e[:, 1].copy())
+
+    er = [(int(a), int(b)) for a, b in rng.integers(0, 60, (300, 2))]
+    loops = er[:200] + [(i, i) for i in range(0, 60, 3)] + er[:40]
+    return {
+        "pattern_one_vertex": (g(60, er), g(1, [])),
+        "pattern_one_vertex_loop": (g(60, er), g(1, [(0, 0)])),
+        "pattern_loops_and_parallel_edges": (g(60, er), g(5, [(0, 1), (0, 1), (2, 2), (3, 4), (4, 3), (1, 0)])),
+        "data_loops_and_duplicates": (g(60, loops), g(4, [(0, 1), (1, 2), (2, 3)])),
+        "pattern_larger_than_data": (g(5, [(0, 1), (1, 2), (2, 3), (3, 4), (4, 0), (1, 3), (2, 2), (0, 4)]),
+                                     g(9, [(i, (i + 1) % 9) for i in range(9)] + [(0, 5), (2, 7), (8, 8)])),
+        "one_data_vertex": (g(1, [(0, 0), (0, 0)]), g(3, [(0, 1), (1, 2)])),
+        "isolated_data_vertices": (g(80, [(a % 20, b % 20) for a, b in er[:150]]),
+                                   g(4, [(0, 1), (1, 2), (2, 0), (2, 3)])),
+    }
+
+
+@pytest.mark.parametrize("case", list(_degenerate_graphs()))
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_degenerate_graphs_vs_oracle(cuda, prec, case):
+    """One-vertex patterns and data graphs, self-loops and parallel edges on
+    either side, a pattern larger than the data graph, isolated data vertices:
+    against the oracle, and the one-shot host call against the device path bit
+    for bit."""
+    d, p = _degenerate_graphs()[case]
+    ref = oracle.match(d, p)
+    mu = matcher.match(d, p, prec)
+    tol = FP64_REL * max(1.0, np.abs(ref).max()) if prec == "fp64" else MIXED_ABS
+    assert mu.shape == ref.shape and np.isfinite(mu).all()
+    assert np.abs(mu - ref).max() <= tol
+    assert _argmax_same(mu, ref, tol=1e-9 if prec == "fp64" else 1e-5)
+    assert np.array_equal(matcher.match_host(d, p, prec), mu)
+
+
 # Pattern sizes that select each form of the vertex phase: the warp form with
 # one or two edge columns and one or two pattern vertices per lane, and the
 # tile form (more than 64 padded edge columns, or more than 64 pattern vertices).
