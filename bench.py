@@ -476,6 +476,12 @@ def run_ours(args, ws, rank, local):
                                   "kind": "port", "sample": info["sample"],
                                   "validation": cpu_validation(info["sample_ms_per_unit"],
                                                                info["cores"])}
+        if info["cores"] > 1:  # the same sample on one thread
+            ms1, info1 = cpu_sample(args.workload, threads=1)
+            result["cpu_baseline"]["single_thread"] = {
+                "value": round(ms1, 1), "unit": "ms", "cores": 1,
+                "sample_s": round(info1["sample_s"], 2),
+                "thread_scaling": round(ms1 / ms, 2)}
     if rank == 0:
         print(json.dumps(result), flush=True)
 
