@@ -248,6 +248,18 @@ def cpu_validation(ms_per_unit: float, threads: int, name: str = "rmat18"):
             "model_error": round(pred / meas - 1.0, 3)}
 
 
+def cpu_model() -> str:
+    """The host CPU's model name as lscpu reports it (best effort)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+    except (OSError, subprocess.SubprocessError):
+        return "unknown"
+    for line in out.splitlines():
+        if line.lower().startswith("model name:"):
+            return line.split(":", 1)[1].strip()
+    return "unknown"
+
+
 def _units(dn, de, pn, pe):
     return (de + dn) * max(pe, 1) * (pn + 1)
 
@@ -473,7 +485,7 @@ def run_ours(args, ws, rank, local):
     if rank == 0 and ws == 1 and not args.no_cpu:
         ms, info = cpu_sample(args.workload)
         result["cpu_baseline"] = {"value": round(ms, 1), "unit": "ms", "cores": info["cores"],
-                                  "kind": "port", "sample": info["sample"],
+                                  "kind": "port", "sample": info["sample"], "cpu": cpu_model(),
                                   "validation": cpu_validation(info["sample_ms_per_unit"],
                                                                info["cores"])}
         if info["cores"] > 1:  # the same sample on one thread
@@ -519,6 +531,7 @@ def run_reference(args, ws, rank):
         "config": {"workload": f"{args.workload}: {workload_info(args.workload)[0]}",
                    "precision": "fp64 (the reference computes in FP64)"},
         "cpu_baseline": {"value": round(value, 1), "unit": "ms", "cores": nt, "kind": "port",
+                         "cpu": cpu_model(),
                          "sample": f"{sample}: {d.num_nodes} vertices / {d.num_edges} edges, "
                                    f"pattern {p.num_nodes}/{p.num_edges}, {ms_sample/1e3:.2f} s per "
                                    f"sample match, scaled by (De+Dn)*Pe*(Pn+1) x{full/units:.1f}",
