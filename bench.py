@@ -17,7 +17,8 @@ every pattern).  Prints one JSON line:
   plain_fp64  the same match computed entirely in FP64, with the error of
               the mixed result against it
   cpu_baseline  the CPU oracle (a pass-by-pass restatement of the reference)
-              on a bounded sample of the workload, scaled to a whole match
+              on a bounded sample of the workload, scaled to a whole match,
+              on all host threads and on one
 
 ``--impl reference`` times the CPU oracle instead (the reference program's
 own CPU build needs its sources, which only the development machine has).
