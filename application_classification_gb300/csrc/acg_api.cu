@@ -751,12 +751,19 @@ acg_status plan_create_impl(acg_data* D, PatternSpec&& spec, const acg_options& 
   if (o.cnull) {
     alloc(sizeof(double) * 3 * std::max(1, Pe), (void**)&P->cnull);
     alloc(sizeof(double) * 3 * std::max(1, Pe) * cnull_blocks(D->num_sms), (void**)&P->cnull_part);
+    if (!spec.qmember.empty()) {  // a union: the normaliser runs per member
+      alloc(sizeof(int) * spec.qmember.size(), (void**)&P->qmember);
+      P->nmembers = 1 + *std::max_element(spec.qmember.begin(), spec.qmember.end());
+    }
   }
   if (st != ACG_OK) return fail(st);
   std::vector<long long> qlim(Pp, 0);
   std::copy(spec.qlim.begin(), spec.qlim.end(), qlim.begin());
   ACG_CUDA_TRY(cudaMemcpyAsync(P->pat, spec.pat.data(), sizeof(int) * spec.pat.size(),
                                cudaMemcpyHostToDevice, s));
+  if (P->qmember)
+    ACG_CUDA_TRY(cudaMemcpyAsync(P->qmember, spec.qmember.data(), sizeof(int) * spec.qmember.size(),
+                                 cudaMemcpyHostToDevice, s));
   if (Pn > 0)
     ACG_CUDA_TRY(cudaMemcpyAsync(P->iters_p, spec.iters_p.data(), sizeof(int) * Pn,
                                  cudaMemcpyHostToDevice, s));

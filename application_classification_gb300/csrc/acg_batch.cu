@@ -94,12 +94,14 @@ acg_status union_spec(acg_data* D, const std::vector<HostPattern>& hp, const std
   sp.Pe = (int)cov.size();
   std::vector<uint64_t> ps(sp.Pe), pd(sp.Pe);
   sp.qlim.resize(sp.Pe);
+  sp.qmember.resize(sp.Pe);
   for (int u = 0; u < sp.Pe; ++u) {
     const Col& c = cov[u];
     const HostPattern& h = hp[mem[c.m]];
     ps[u] = (uint64_t)p0[c.m] + h.ps[c.q];
     pd[u] = (uint64_t)p0[c.m] + h.pd[c.q];
     sp.qlim[u] = c.qlim;
+    sp.qmember[u] = c.m;  // a member's columns keep their order (covered ones are its first)
   }
   ACG_TRY(build_incidence(sp.Pn, sp.Pe, ps.data(), pd.data(), &sp.pat));
   sp.iters_p.resize(sp.Pn);
@@ -320,8 +322,6 @@ acg_status acg_batch_create(acg_data* D, const acg_graph* patterns, int32_t npat
     return set_error(ACG_ERR_INVALID_ARGUMENT, "acg_batch_create: no patterns");
   acg_options o;
   ACG_TRY(resolve_options(opt, &o));
-  if (o.cnull)
-    return set_error(ACG_ERR_UNSUPPORTED, "acg_batch_create: the cnull option is for single plans");
   o.kernel_timing = 0;
   cudaStream_t s = (cudaStream_t)stream;
   std::unique_ptr<acg_batch, void (*)(acg_batch*)> B(new acg_batch(), destroy);

@@ -3,7 +3,8 @@
 // The reference leaves it out (main.cu:83 "Ignoring for now"; test.py:93-97
 // has it commented out and uses zeros).  When acg_options.cnull is set:
 //   cn[q]    = max(||pe_q||_2, max_e L(dE)[q][e]),  L(dE)[q][e] = dE[q][e] - LSE_e dE[q][e]
-//   cnull[q] = cn[q] - LSE_q cn[q]                   (normprob over the pattern edges)
+//   cnull[q] = cn[q] - LSE_q cn[q]                   (normprob over the pattern edges;
+//                                                     in a union, over each member's)
 // and every BP iteration subtracts cnull[q] from both fills of column q
 // (test.py:139-140: fwd_max = max(fwd_max, v_bak_max - cnull), likewise bak_max).
 // The column statistics of dE are one pass over the [De][Pp] matrix: per
@@ -57,29 +58,30 @@ cnull_stats_kernel(const T* __restrict__ dE, long long De, int Pe, int Pp, int c
 }
 
 // One block: cnull from the column statistics and the pattern edge features.
+// The normaliser runs over each member's columns (a union of patterns: its
+// columns' member ids in qmember; a single pattern: qmember null), one thread
+// per member merging its columns in column order.
 __global__ void __launch_bounds__(kNT)
 cnull_final_kernel(const double* __restrict__ st, const double* __restrict__ pe, int Pe, int Ke,
-                   long long De, double* __restrict__ cnull) {
-  __shared__ double s_m[kNT], s_s[kNT];
-  double lm = -CUDART_INF, ls = 0.0;
+                   long long De, const int* __restrict__ qmember, int nmembers,
+                   double* __restrict__ cnull) {
+  __shared__ double s_L[kNT];
   for (int q = threadIdx.x; q < Pe; q += kNT) {
     double nn = 0.0;
     for (int k = 0; k < Ke; ++k) nn += pe[(size_t)q * Ke + k] * pe[(size_t)q * Ke + k];
     double cn = sqrt(nn);
     if (De > 0) cn = fmax(cn, st[q] - st[Pe + q]);  // max_e L(dE)[q][e]
     cnull[q] = cn;
-    lse_merge(lm, ls, cn, 1.0);
-  }
-  s_m[threadIdx.x] = lm;
-  s_s[threadIdx.x] = ls;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int i = 1; i < kNT; ++i) lse_merge(lm, ls, s_m[i], s_s[i]);
-    s_m[0] = lm + log(ls);
   }
   __syncthreads();
-  const double L = s_m[0];
-  for (int q = threadIdx.x; q < Pe; q += kNT) cnull[q] -= L;
+  for (int m = threadIdx.x; m < nmembers; m += kNT) {
+    double lm = -CUDART_INF, ls = 0.0;
+    for (int q = 0; q < Pe; ++q)
+      if (!qmember || qmember[q] == m) lse_merge(lm, ls, cnull[q], 1.0);
+    s_L[m] = lm + log(ls);
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < Pe; q += kNT) cnull[q] -= s_L[qmember ? qmember[q] : 0];
 }
 
 }  // namespace
@@ -102,7 +104,10 @@ acg_status run_cnull(acg_plan* P, cudaStream_t s) {
     ACG_TRY(launch_finalize(P->cnull_part, (int)grid.x, StatSpec{Pe, Pe}, st, s));
     P->launches += 2;
   }
-  cnull_final_kernel<<<1, kNT, 0, s>>>(st, P->pe, Pe, P->data->Ke, De, P->cnull);
+  if (P->nmembers < 1 || P->nmembers > kNT)
+    return set_error(ACG_ERR_UNSUPPORTED, "run_cnull: %d patterns in one group", P->nmembers);
+  cnull_final_kernel<<<1, kNT, 0, s>>>(st, P->pe, Pe, P->data->Ke, De, P->qmember, P->nmembers,
+                                       P->cnull);
   ACG_LAUNCH_CHECK();
   P->launches += 1;
   return ACG_OK;

@@ -137,6 +137,8 @@ struct acg_plan {
   int* dev_err = nullptr;      // set by a device-side bounded wait that gave up
   double* cnull = nullptr;     // [Pe] C-null term, then [2 Pe] dE column stats (option cnull)
   double* cnull_part = nullptr;  // [3 Pe][cnull_blocks] block partials
+  int* qmember = nullptr;        // [Pe] member of each union column (option cnull), else null
+  int nmembers = 1;
   const acg::StateRec* rec = nullptr;  // states to record during a match (adjoint)
   acg::AdjWork* adj = nullptr;         // owned; freed by acg_plan_destroy
   std::vector<acg::DevBuf> owned;
@@ -153,6 +155,7 @@ struct PatternSpec {
   const double* pv = nullptr;       // device [Pn][Kv]
   const double* pe = nullptr;       // device [Pe][Ke]
   bool is_union = false;
+  std::vector<int> qmember;         // [Pe] member of each column (unions; empty: one member)
 };
 
 // Incidence arrays of a pattern from its endpoints (pattern_ints layout).

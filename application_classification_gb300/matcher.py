@@ -240,7 +240,8 @@ class Batch:
     batch runs as one CUDA graph launch per :meth:`run`."""
 
     def __init__(self, data: DataGraph, patterns, precision: str = "fp64", num_iters: int = -1,
-                 stream=None, autotune: bool = False, edge_blocks_per_sm: int = 0):
+                 stream=None, autotune: bool = False, edge_blocks_per_sm: int = 0,
+                 cnull: bool = False):
         self.data = data
         self.pats = [p if isinstance(p, DeviceGraph) else DeviceGraph(p) for p in patterns]
         arr = (_lib.Graph * len(self.pats))(*[p.c_graph() for p in self.pats])
@@ -253,6 +254,7 @@ class Batch:
         opt.num_iters = num_iters
         opt.autotune = 1 if autotune else 0
         opt.edge_blocks_per_sm = int(edge_blocks_per_sm)  # the autotuner picks its own
+        opt.cnull = 1 if cnull else 0
         self.precision = precision
         self.handle = C.c_void_p()
         _lib.check(_lib.lib().acg_batch_create(data.handle, C.cast(arr, C.c_void_p), len(self.pats),

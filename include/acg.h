@@ -81,8 +81,9 @@ typedef struct acg_options {
                          cnull = log-softmax over pattern edges q of
                          max(||pe_q||, max_e L(dE)[q][e]), subtracted from both
                          max-message fills of column q in every iteration.
-                         0 (default): the reference's behaviour.  Single plans
-                         only (acg_batch_create and the adjoint reject it). */
+                         0 (default): the reference's behaviour.  In a batch
+                         the normaliser runs over each pattern's own edges;
+                         the adjoint rejects it. */
   int32_t cdist_kernel; /* the edge and vertex cost matrices of the
                            mixed-precision path: 0 (default) each on the
                            tensor cores (tcgen05, TF32 split, see

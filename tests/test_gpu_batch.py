@@ -1,8 +1,8 @@
 """Many patterns against one data graph (acg_batch): every member's mu equals
 its own single-pattern match (the groups are disjoint unions), for patterns
-packed together, patterns too wide to share a group, and a data graph whose
-quirk coverage spans many columns; the captured CUDA graph relaunches to the
-same result."""
+packed together, patterns too wide to share a group, a data graph whose quirk
+coverage spans many columns, and the C-null option; the captured CUDA graph
+relaunches to the same result."""
 import numpy as np
 import pytest
 
@@ -15,14 +15,14 @@ pytestmark = pytest.mark.gpu
 FP64_REL = 1e-10
 
 
-def _batch_vs_single(d, pats, prec, tol_abs=None, autotune=False):
+def _batch_vs_single(d, pats, prec, tol_abs=None, autotune=False, cnull=False):
     dg = matcher.DataGraph(d)
-    b = matcher.Batch(dg, pats, prec, autotune=autotune)
+    b = matcher.Batch(dg, pats, prec, autotune=autotune, cnull=cnull)
     outs = [o.cpu().numpy() for o in b.run()]
     info = b.info()
     assert info["patterns"] == len(pats) and info["groups"] < len(pats)
     for p, mu in zip(pats, outs):
-        one = matcher.Plan(dg, p, prec).run().cpu().numpy()
+        one = matcher.Plan(dg, p, prec, cnull=cnull).run().cpu().numpy()
         tol = FP64_REL * max(1.0, np.abs(one).max()) if tol_abs is None else tol_abs
         assert np.abs(mu - one).max() <= tol
     return dg, b, outs
@@ -32,6 +32,23 @@ def _batch_vs_single(d, pats, prec, tol_abs=None, autotune=False):
 def test_batch_members_equal_single_matches(cuda, prec):
     d, pats, _ = graph.batch_workload(11, 10, seed=5)
     _batch_vs_single(d, pats, prec, None if prec == "fp64" else 2e-5)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_batch_cnull_members_equal_single_matches(cuda, prec):
+    """The C-null term in a batch: each member's normaliser runs over its own
+    pattern edges, so it equals the member's single match with the option."""
+    d, pats, _ = graph.batch_workload(11, 10, seed=5)
+    _batch_vs_single(d, pats, prec, None if prec == "fp64" else 2e-5, cnull=True)
+
+
+def test_batch_cnull_fp64_vs_oracle(cuda):
+    d, pats, _ = graph.batch_workload(10, 6, seed=7)
+    dg = matcher.DataGraph(d)
+    outs = [o.cpu().numpy() for o in matcher.Batch(dg, pats, "fp64", cnull=True).run()]
+    for p, mu in zip(pats, outs):
+        ref = oracle.match(d, p, cnull=True)
+        assert np.abs(mu - ref).max() <= FP64_REL * max(1.0, np.abs(ref).max())
 
 
 def test_batch_fp64_vs_oracle(cuda):

@@ -313,21 +313,9 @@ def test_cnull_vs_oracle(cuda, prec, case):
         assert _argmax_same(mu, ref, tol=1e-5)
 
 
-def test_cnull_rejected_by_batch_and_adjoint(cuda):
+def test_cnull_rejected_by_adjoint(cuda):
     d, p, _ = load_golden("er300")
     data = matcher.DataGraph(d)
-    import ctypes as C
-    from application_classification_gb300 import _lib
-
-    pg = matcher.DeviceGraph(p)
-    arr = (_lib.Graph * 1)(pg.c_graph())
-    opt = _lib.Options()
-    _lib.lib().acg_options_default(C.byref(opt))
-    opt.cnull = 1
-    h = C.c_void_p()
-    st = _lib.lib().acg_batch_create(data.handle, C.cast(arr, C.c_void_p), 1, C.byref(opt),
-                                     matcher._stream_ptr(None), C.byref(h))
-    assert st == 5
     plan = matcher.Plan(data, p, "fp64", cnull=True)
     with pytest.raises(AcgError) as e:
         plan.record()
