@@ -383,6 +383,29 @@ def test_vertex_cost_matrix_tensor_cores_wide(cuda, dn, de, ke, pn, pe, kv):
     assert _argmax_same(out["tensor"], ref, tol=1e-5)
 
 
+@pytest.mark.parametrize("dn,de,ke,pn,pe,kv", WIDE_SHAPES)
+def test_edge_cost_matrix_tensor_cores_wide(cuda, dn, de, ke, pn, pe, kv):
+    """The same wide shapes after one BP iteration, whose edge maxima read the
+    edge cost matrix (up to 128 columns, the tensor-core limit): against the
+    oracle and the CUDA-core kernels, before many iterations amplify the
+    FP32 rounding."""
+    d = graph.gen_er(dn, de - pe, kv=kv, ke=ke, seed=dn + pn)
+    d, p, _, _ = graph.plant(d, pn, pe, 0.05, seed=kv)
+    ref = oracle.match(d, p, num_iters=1)
+    data = matcher.DataGraph(d)
+    out = {}
+    for kern in ("tensor", "simt"):
+        plan = matcher.Plan(data, p, "mixed", cdist_kernel=kern, num_iters=1)
+        out[kern] = plan.run().cpu().numpy()
+        plan.stats()
+        plan.close()
+    data.close()
+    scale = max(1.0, np.abs(ref).max() / 100.0)
+    assert np.abs(out["simt"] - ref).max() <= MIXED_ABS * scale
+    assert np.abs(out["tensor"] - ref).max() <= MIXED_ABS * scale
+    assert _argmax_same(out["tensor"], ref, tol=1e-5)
+
+
 @pytest.mark.parametrize("kv,ke", [(13, 40), (40, 13)])
 def test_cdist_tensor_cores_unsupported_shape(cuda, kv, ke):
     """A feature dim above 32 on either side: "tensor" is refused, "auto" runs
