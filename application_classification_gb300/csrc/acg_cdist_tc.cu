@@ -395,7 +395,8 @@ __global__ void __launch_bounds__(kTT, 3) cdist_tc_kernel(const TcArgs a) {
 //                         d as cdist_tc_kernel forms it (near pairs recomputed
 //                         from the features in global memory), each chunk staged
 //                         and stored as 8 rows x 64 bytes (rows through the
-//                         optional row map), then ACCFREE
+//                         optional row map; the first qcols columns also as
+//                         compact rows of the outq copy), then ACCFREE
 // so the split and MMAs run up to three tiles ahead of the epilogues, and each
 // epilogue group has two tiles' time for one.  Same
 // values as cdist_tc_kernel.  Bounded waits as there; a role whose wait gives
