@@ -26,7 +26,9 @@
 // integer OR (the per-edge column masks of the maxima), the same in any order.
 //
 // Limits: single-pattern plans of at most 64 padded edge columns and 64
-// pattern vertices (the warp forms), feature dimensions up to 32.
+// pattern vertices (the warp forms), feature dimensions up to 32.  With the
+// C-null option, the term's gradient goes to the pattern edge features
+// (adj_cnull_*).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -73,6 +75,7 @@ struct AdjWork {
   double* cols = nullptr;                          // [8 Pe + 2 Pn + 8]
   int* colsi = nullptr;                            // [2 Pe + Pn]
   double* ypart = nullptr;                         // pattern-gradient partials
+  double* gcn = nullptr;                           // [Pe] gradient into the C-null term (option cnull)
   std::vector<DevBuf> owned;
   // the backward as one CUDA graph (its launches are the same on every call
   // with the same gradient pointers), captured on a stream of its own
@@ -376,6 +379,7 @@ struct StepAArgs {
   double* pv;         // [2 Pe][blocks] argmax values
   int* pi;
   int Dn, Pn, Pe, Pp;
+  const double* cnull;  // [Pe] the C-null term subtracted from both fills (option cnull), or null
 };
 
 template <typename T, int QPL, int PPL>
@@ -406,8 +410,14 @@ __global__ void __launch_bounds__(kT) adj_stepA_kernel(const StepAArgs<T> a) {
       qd[k] = pdst[q];
       qs[k] = psrc[q];
       // the fills and constants exactly as the forward's vertex phase forms them
-      fR[k] = (T)(g[q] + g[x0 + q] - g[4 * Pe + qd[k]]);
-      fF[k] = (T)(g[Pe + q] + g[x0 + Pe + q] - g[4 * Pe + qs[k]]);
+      double fr = g[q] + g[x0 + q] - g[4 * Pe + qd[k]];
+      double ff = g[Pe + q] + g[x0 + Pe + q] - g[4 * Pe + qs[k]];
+      if (a.cnull) {
+        fr -= a.cnull[q];
+        ff -= a.cnull[q];
+      }
+      fR[k] = (T)fr;
+      fF[k] = (T)ff;
       const double dR = g[2 * Pe + q], dF = g[3 * Pe + q];
       dRh[k] = (T)dR;
       dRl[k] = (T)(dR - (double)dRh[k]);
@@ -1185,6 +1195,43 @@ bool adj_warp_form(int pn, int pp, F&& f) {
   return true;
 }
 
+// ------------------------------------------------------------- C-null term
+// (option cnull) Every iteration subtracts cnull[q] from both fills of column
+// q, so the term's gradient is minus the gradients into the two fills, summed
+// over the iterations (W->cols after each step A: into fR at [0, Pe), into fF
+// at [Pe, 2 Pe)).
+__global__ void adj_cnull_acc_kernel(const double* __restrict__ cols, int Pe, double* __restrict__ gcn) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < Pe) gcn[q] -= cols[q] + cols[Pe + q];
+}
+
+// cnull[q] = cn[q] - LSE_q cn[q] with cn[q] = max(||pe_q||, max_e L(dE)[q][e]).
+// The second term is a log-softmax, never above 0 <= ||pe_q||, so cn[q] is the
+// norm (a tie at 0 sends the gradient to the norm too): the gradient reaches
+// the pattern edge features only,
+//   gpe[q] += (gcn[q] - w_q sum_q' gcn[q']) pe_q / ||pe_q||,  w_q = exp(cnull[q]),
+// added to what the cost matrix's adjoint wrote (none at ||pe_q|| = 0).  One
+// block; the sum in column order.
+__global__ void adj_cnull_pe_kernel(const double* __restrict__ gcn, const double* __restrict__ cnull,
+                                    const double* __restrict__ pe, int Pe, int Ke,
+                                    double* __restrict__ gpe) {
+  __shared__ double s_tot;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < Pe; ++q) t += gcn[q];
+    s_tot = t;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < Pe; q += blockDim.x) {
+    double nn = 0.0;
+    for (int k = 0; k < Ke; ++k) nn += pe[(size_t)q * Ke + k] * pe[(size_t)q * Ke + k];
+    const double norm = sqrt(nn);
+    if (!(norm > 0.0)) continue;
+    const double c = (gcn[q] - exp(cnull[q]) * s_tot) / norm;
+    for (int k = 0; k < Ke; ++k) gpe[(size_t)q * Ke + k] += c * pe[(size_t)q * Ke + k];
+  }
+}
+
 // ------------------------------------------------------------- host side
 template <typename T>
 struct Adj {
@@ -1287,7 +1334,7 @@ struct Adj {
     StepAArgs<T> sa{(const T*)W->gMU, first ? nullptr : (const T*)W->gFd,
                     first ? nullptr : (const T*)W->gRd, f, r, M, A, (T*)W->gdE, W->emask, (const T*)P->dEmin, g,
                     P->pat, (T*)W->gbR, (T*)W->gM, (T*)W->gdEmin, (T*)W->gCV, W->part,
-                    W->part + (size_t)4 * Pe * vblocks, W->parti, Dn, Pn, Pe, Pp};
+                    W->part + (size_t)4 * Pe * vblocks, W->parti, Dn, Pn, Pe, Pp, P->cnull};
     const size_t smA = sizeof(T) * kW * 64 * 2 + sizeof(double) * kW * 6 * std::max(1, Pe) +
                        sizeof(int) * kW * 2 * std::max(1, Pe) + 64;
     cudaError_t le = cudaSuccess;
@@ -1299,6 +1346,10 @@ struct Adj {
     });
     if (le != cudaSuccess) return set_error(ACG_ERR_CUDA, "adj_stepA: %s", cudaGetErrorString(le));
     ACG_TRY(col_final(4 * Pe, 2 * Pe, vblocks));
+    if (W->gcn && Pe > 0) {  // minus the gradients into both fills
+      adj_cnull_acc_kernel<<<ceil_div(Pe, 128), 128, 0, s>>>(W->cols, Pe, W->gcn);
+      ACG_LAUNCH_CHECK();
+    }
     if (Pe > 0) ACG_TRY(scatter());
     else ACG_TRY(fill(W->gVRe, vrow(), T(0)));
     // state t - 1 = 0 has no S term (MU0 is normalised: S(0) is identically 0)
@@ -1335,6 +1386,7 @@ struct Adj {
     ACG_TRY(fill(W->gB, vrow(), T(0)));
     ACG_TRY(fill(W->gCV, prow(), T(0)));
     ACG_TRY(fill(W->gdE, (size_t)De * Pp, T(0)));
+    if (W->gcn) ACG_CUDA_TRY(cudaMemsetAsync(W->gcn, 0, sizeof(double) * std::max(1, Pe), s));
     // the gradient into MU(T): mu = MU(T) - S(T)
     ACG_TRY(col_sums(gmu, Pn, Pn, Dn, 0));
     {
@@ -1466,6 +1518,10 @@ struct Adj {
     if (De > 0 && Pe > 0) ACG_TRY(cdist_back(false, gdef, gpef));
     else if (Pe > 0)
       ACG_CUDA_TRY(cudaMemsetAsync(gpef, 0, sizeof(double) * Pe * D->Ke, s));
+    if (W->gcn && Pe > 0) {  // the C-null term, a function of the pattern edge features
+      adj_cnull_pe_kernel<<<1, 256, 0, s>>>(W->gcn, P->cnull, P->pe, Pe, D->Ke, gpef);
+      ACG_LAUNCH_CHECK();
+    }
     return ACG_OK;
   }
 
@@ -1547,7 +1603,6 @@ acg_status adj_buf(AdjWork* W, size_t bytes, void** out, cudaStream_t s) {
 acg_status adj_check(acg_plan* P, const char* who) {
   if (!P) return set_error(ACG_ERR_INVALID_ARGUMENT, "%s: plan is null", who);
   if (P->is_union) return set_error(ACG_ERR_UNSUPPORTED, "%s: a batch group has no adjoint", who);
-  if (P->cnull) return set_error(ACG_ERR_UNSUPPORTED, "%s: no adjoint of the cnull option", who);
   if (P->Pp > 64 || P->Pn > 64 || !P->init_warp)
     return set_error(ACG_ERR_UNSUPPORTED,
                      "%s: the adjoint is built for patterns of at most 64 vertices and 64 padded edge columns",
@@ -1634,6 +1689,7 @@ acg_status adj_alloc(acg_plan* P, int every, cudaStream_t s) {
   ACG_TRY(adj_buf(W, sizeof(int) * (2 * Pe + Pn + 1), (void**)&W->colsi, s));
   const size_t ny = 4 * (size_t)nsm * std::max(Pn * (D->Kv + 1), Pe * (D->Ke + 1));
   ACG_TRY(adj_buf(W, sizeof(double) * ny, (void**)&W->ypart, s));
+  if (P->cnull) ACG_TRY(adj_buf(W, sizeof(double) * std::max<size_t>(1, Pe), (void**)&W->gcn, s));
   return ACG_OK;
 }
 

@@ -83,7 +83,8 @@ typedef struct acg_options {
                          max-message fills of column q in every iteration.
                          0 (default): the reference's behaviour.  In a batch
                          the normaliser runs over each pattern's own edges;
-                         the adjoint rejects it. */
+                         acg_backward carries the term's gradient to the
+                         pattern edge features. */
   int32_t cdist_kernel; /* the edge and vertex cost matrices of the
                            mixed-precision path: 0 (default) each on the
                            tensor cores (tcgen05, TF32 split, see

@@ -29,9 +29,12 @@ def _edge_max(base, vals, nodes, n):
     return out.scatter_reduce(1, idx, vals, reduce="amax", include_self=True)
 
 
-def match(dnf, def_, pnf, pef, srcs, dsts, psrc, pdst, iters=None):
+def match(dnf, def_, pnf, pef, srcs, dsts, psrc, pdst, iters=None, cnull=False):
     """mu [Dn][Pn] (float64 tensor) from the four feature tensors; srcs/dsts and
-    psrc/pdst are int64 tensors of the data and pattern endpoints."""
+    psrc/pdst are int64 tensors of the data and pattern endpoints.  cnull: the
+    optional C-null term as test.py:93-97 and 139-140 state it (the reference
+    leaves it out): cn_q = max(||pe_q||, max_e L(ce)[q][e]) normalised by a
+    log-softmax over q, subtracted from both fills in every iteration."""
     Dn, Pn, Pe, De = dnf.shape[0], pnf.shape[0], pef.shape[0], def_.shape[0]
     T = Pn if iters is None else iters
     cv_t = _cdist(pnf, dnf)                     # [Pn][Dn]
@@ -51,15 +54,25 @@ def match(dnf, def_, pnf, pef, srcs, dsts, psrc, pdst, iters=None):
     vrmax = vr_t.amax(1)
     rmax_t = _edge_max(vfmax, re_t, srcs, Dn)
     fmax_t = _edge_max(vrmax, fe_t, dsts, Dn)
+    cn = None
+    if cnull and Pe > 0:
+        cn = torch.sqrt((pef ** 2).sum(-1))
+        if De > 0:
+            cn = torch.maximum(cn, ce_t.amax(1))
+        cn = cn - torch.logsumexp(cn, dim=0)
     for _ in range(T):
         vf_t = mu_t[pdst] - fmax_t
         vr_t = mu_t[psrc] - rmax_t
         fe_t = vr_t[:, srcs] - ce_t
         re_t = vf_t[:, srcs] - ce_t
         vfmax = vf_t.amax(1)
+        if cn is not None:
+            vfmax = vfmax - cn
         re_t = _L(re_t)
         rmax_t = _edge_max(vfmax, re_t, srcs, Dn)
         vrmax = vr_t.amax(1)
+        if cn is not None:
+            vrmax = vrmax - cn
         fe_t = _L(fe_t)
         fmax_t = _edge_max(vrmax, fe_t, dsts, Dn)
         mu_t = -cv_t
@@ -68,12 +81,12 @@ def match(dnf, def_, pnf, pef, srcs, dsts, psrc, pdst, iters=None):
     return mu_t.T.contiguous()
 
 
-def match_graphs(d, p, iters=None, requires_grad=True):
+def match_graphs(d, p, iters=None, requires_grad=True, cnull=False):
     """match() on host graphs (graph.Graph); returns (mu, [dnf, def, pnf, pef])."""
     import numpy as np
 
     t = lambda a: torch.tensor(np.asarray(a), dtype=torch.float64, requires_grad=requires_grad)
     i = lambda a: torch.tensor(np.asarray(a).astype(np.int64))
     feats = [t(d.node_feats), t(d.edge_feats), t(p.node_feats), t(p.edge_feats)]
-    mu = match(*feats, i(d.srcs), i(d.dsts), i(p.srcs), i(p.dsts), iters)
+    mu = match(*feats, i(d.srcs), i(d.dsts), i(p.srcs), i(p.dsts), iters, cnull)
     return mu, feats

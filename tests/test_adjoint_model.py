@@ -35,3 +35,17 @@ def test_adjoint_model_vs_autograd_golden(name):
 def test_adjoint_model_few_iterations(iters):
     d, p, _ = graph.workload("rmat8_5_9")
     _check(d, p, iters, seed=iters)
+
+
+@pytest.mark.parametrize("name", ["tiny", "irregular", "er300"])
+def test_reference_cnull_vs_oracle(name):
+    """The torch re-implementation with the C-null term gives the oracle's mu
+    with the same option (the reference for the term's adjoint)."""
+    from oracle import oracle
+
+    d, p, _ = load_golden(name)
+    mu, _ = adjoint_ref.match_graphs(d, p, requires_grad=False, cnull=True)
+    ref = oracle.match(d, p, cnull=True)
+    assert np.abs(mu.numpy() - ref).max() <= 1e-10 * max(1.0, np.abs(ref).max())
+    plain = oracle.match(d, p)
+    assert np.abs(ref - plain).max() > 0 or name == "tiny"  # the term changes something

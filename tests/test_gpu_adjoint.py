@@ -26,9 +26,9 @@ FP64_REL = 1e-9
 MIXED_REL = 2e-3  # relative Frobenius norm, per feature array
 
 
-def _grads(d, p, gmu, prec="fp64", iters=-1, every=4, repeat=1):
+def _grads(d, p, gmu, prec="fp64", iters=-1, every=4, repeat=1, cnull=False):
     data = matcher.DataGraph(d)
-    plan = matcher.Plan(data, p, prec, iters)
+    plan = matcher.Plan(data, p, prec, iters, cnull=cnull)
     try:
         mu = plan.record(checkpoint_every=every)
         gs = [plan.backward(torch.from_numpy(gmu)) for _ in range(repeat)]
@@ -254,3 +254,45 @@ def test_rmat12_finite_differences_200(cuda):
     finally:
         plan.close()
         data.close()
+
+
+@pytest.mark.parametrize("name", ["irregular", "er300"])
+def test_cnull_vs_autograd_reference(cuda, name):
+    """The C-null option: the term is made of the pattern edge features' norms
+    (its log-softmax alternative never exceeds them), so its gradient reaches
+    those features.  FP64 against torch autograd through the reference's
+    passes with the term, mixed within its bound, and central differences on
+    the pattern edge features."""
+    import adjoint_ref
+
+    d, p, _ = load_golden(name)
+    gmu = np.random.default_rng(4).normal(size=(d.num_nodes, p.num_nodes))
+    mu_t, feats = adjoint_ref.match_graphs(d, p, cnull=True)
+    (mu_t * torch.from_numpy(gmu)).sum().backward()
+    ref = [f.grad.numpy() for f in feats]
+    mu64, g64 = _grads(d, p, gmu, "fp64", cnull=True)
+    assert _rel(mu64, mu_t.detach().numpy()) <= 1e-10
+    for a, b in zip(g64, ref):
+        assert _rel(a, b) <= FP64_REL, _rel(a, b)
+    _, g32 = _grads(d, p, gmu, "mixed", cnull=True)
+    # relative to each array's gradient, or to a thousandth of the largest one
+    # where an array's gradient all but vanishes (the fills win everywhere)
+    big = max(np.linalg.norm(b) for b in ref)
+    for a, b in zip(g32, ref):
+        assert np.linalg.norm(a - b) <= MIXED_REL * max(np.linalg.norm(b), 1e-3 * big)
+
+    def f():
+        return float((matcher.match(d, p, "fp64", cnull=True) * gmu).sum())
+
+    h = 1e-5
+    a = p.edge_feats
+    scale = max(1e-3, np.abs(g64[3]).max())
+    for i in np.argsort(-np.abs(g64[3]).ravel())[:4].tolist():
+        idx = np.unravel_index(i, a.shape)
+        x0 = a[idx]
+        a[idx] = x0 + h
+        fp = f()
+        a[idx] = x0 - h
+        fm = f()
+        a[idx] = x0
+        assert abs((fp - fm) / (2 * h) - g64[3][idx]) <= 1e-5 * scale

@@ -313,17 +313,6 @@ def test_cnull_vs_oracle(cuda, prec, case):
         assert _argmax_same(mu, ref, tol=1e-5)
 
 
-def test_cnull_rejected_by_adjoint(cuda):
-    d, p, _ = load_golden("er300")
-    data = matcher.DataGraph(d)
-    plan = matcher.Plan(data, p, "fp64", cnull=True)
-    with pytest.raises(AcgError) as e:
-        plan.record()
-    assert e.value.status == 5
-    plan.close()
-    data.close()
-
-
 # (data vertices, data edges, edge feature dim, pattern vertices, pattern edges,
 #  vertex feature dim)
 TC_SHAPES = [(300, 3000, 17, 6, 10, 13), (1000, 127, 17, 4, 5, 1), (2000, 20000, 1, 5, 8, 3),
