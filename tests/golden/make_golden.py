@@ -7,7 +7,7 @@ Thrust's OpenMP backend by oracle/Makefile's `ref` target, output captured in
 binary by oracle/ref_shim) prints for that pair.  Needs a checkout of the
 reference sources, named by the environment variable ACG_REFERENCE_DIR:
 
-    ACG_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
+    ACG_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -91,14 +91,43 @@ def tiny():
     return data, pat
 
 
-CASES = {"georgiy": georgiy, "er300": er300, "rmat9": rmat9, "irregular": irregular, "tiny": tiny}
+def small_data():
+    """A pattern larger than the data graph (9 vertices / 12 edges against 5 /
+    8, with self-loops on both sides); Pn*Dn = 45 < Pe*De = 96, so the
+    reference's quirk negation stays inside its buffers."""
+    rng = np.random.default_rng(13)
+    ds = np.array([0, 1, 2, 3, 4, 1, 2, 0], np.uint64)
+    dd = np.array([1, 2, 3, 4, 0, 3, 2, 4], np.uint64)
+    data = Graph(rng.normal(size=(5, 13)), rng.normal(size=(8, 17)), ds, dd)
+    ps = np.array([i for i in range(9)] + [0, 2, 8], np.uint64)
+    pd = np.array([(i + 1) % 9 for i in range(9)] + [5, 7, 8], np.uint64)
+    return data, Graph(rng.normal(size=(9, 13)), rng.normal(size=(12, 17)), ps, pd)
 
 
-def main():
+def one_data_vertex():
+    """One data vertex with two parallel self-loops; a 3-vertex path pattern."""
+    rng = np.random.default_rng(17)
+    data = Graph(rng.normal(size=(1, 13)), rng.normal(size=(2, 17)),
+                 np.array([0, 0], np.uint64), np.array([0, 0], np.uint64))
+    pat = Graph(rng.normal(size=(3, 13)), rng.normal(size=(2, 17)),
+                np.array([0, 1], np.uint64), np.array([1, 2], np.uint64))
+    return data, pat
+
+
+CASES = {"georgiy": georgiy, "er300": er300, "rmat9": rmat9, "irregular": irregular, "tiny": tiny,
+         "small_data": small_data, "one_data_vertex": one_data_vertex}
+
+
+def main(names=None):
+    """Regenerate the named cases (all when none are named); the manifest keeps
+    the entries of the others."""
     _build.build()
     oracle.build(str(REF))
-    manifest = {}
+    mpath = HERE / "manifest.json"
+    manifest = json.loads(mpath.read_text()) if mpath.exists() else {}
     for name, fn in CASES.items():
+        if names and name not in names:
+            continue
         d, p = fn()
         out = HERE / name
         out.mkdir(exist_ok=True)
@@ -113,8 +142,9 @@ def main():
             "max_abs_mu": float(np.abs(mu).max()),
         }
         print(name, manifest[name])
-    (HERE / "manifest.json").write_text(json.dumps(manifest, indent=1) + "\n")
+    manifest = {k: manifest[k] for k in CASES if k in manifest}
+    mpath.write_text(json.dumps(manifest, indent=1) + "\n")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])
