@@ -48,13 +48,16 @@ struct VwStage {
 // psrc[pe], pdst[pe], in_off[pn + 1], in_q[pe], out_off[pn + 1], out_q[pe])
 // are at pat, for stages of vps vertices.  Returns the terms per lane (a
 // multiple of 4) and fills out[terms * 32]; 0 when the pattern takes the tile
-// form (more than 64 pattern vertices or padded edge columns).
+// form (more than 64 pattern vertices or padded edge columns) or the stage is
+// too large for the word's fields.
 inline int vertex_warp_schedule(const int* pat, int pn, int pe, int pp, int pnp, int vps,
                                 std::vector<uint32_t>* out) {
   out->clear();
-  if (pn <= 0 || pn > 64 || pp > 64) return 0;
+  if (pn <= 0 || pn > 64 || pp > 64 || vps <= 0) return 0;
   const int ppl = pn <= 32 ? 1 : 2;
   const VwStage G(pp, pnp, false, vps);  // offsets of M, Y, CV (the same for FP32 and FP64)
+  // every offset and slot must fit its field of the word
+  if (G.oC + vps * pnp > 0x1000 || vps * (32 * ppl + 1) > 0x200) return 0;
   const int* inoff = pat + 2 * pe;
   const int* inq = inoff + pn + 1;
   const int* outoff = inq + pe;

@@ -174,8 +174,12 @@ def test_schedule_invariants(probe):
 
 
 def test_schedule_tile_form_shapes(probe):
-    """More than 64 pattern vertices or padded edge columns take the tile form."""
-    cases = [(4, 65, 4, 68, [(0, 1)]), (4, 10, 68, 12, [(0, 1)] * 65)]
+    """More than 64 pattern vertices or padded edge columns take the tile form,
+    and so does a stage whose slots (9 bits) or offsets (12 bits) would not fit
+    the schedule word."""
+    cases = [(4, 65, 4, 68, [(0, 1)]), (4, 10, 68, 12, [(0, 1)] * 65),
+             (8, 40, 64, 40, [(0, 1)] * 60),   # slots 8 x 65 > 512
+             (15, 32, 64, 32, [(0, 1)] * 60)]  # CV offsets 15 x (4 x 64 + 32) > 4096
     res, _, _ = _run(probe, cases)
     for nt, words in res:
         assert nt == 0 and words.size == 0
