@@ -19,6 +19,8 @@ every pattern).  Prints one JSON line:
   cpu_baseline  the CPU oracle (a pass-by-pass restatement of the reference)
               on a bounded sample of the workload, scaled to a whole match,
               on all host threads and on one
+  configs     short runs of the many-pattern batch and of the adjoint (the
+              lines of --batch and --adjoint, with fewer steps)
 
 ``--impl reference`` times the CPU oracle instead (the reference program's
 own CPU build needs its sources, which only the development machine has).
@@ -92,6 +94,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the short batch and adjoint runs carried on the main line")
     ap.add_argument("--batch", action="store_true",
                     help="the many-pattern workload instead: R-MAT 20 with 64 planted patterns "
                          "(Pn 4..48, Pe 2..4 Pn), batched against sequential single matches")
@@ -495,8 +499,31 @@ def run_ours(args, ws, rank, local):
                 "value": round(ms1, 1), "unit": "ms", "cores": 1,
                 "sample_s": round(info1["sample_s"], 2),
                 "thread_scaling": round(ms1 / ms, 2)}
+    # ---- the many-pattern and gradient configurations, short runs (N=1 only)
+    if ws == 1 and not args.no_configs:
+        result["configs"] = other_configs(args, local)
     if rank == 0:
         print(json.dumps(result), flush=True)
+
+
+def other_configs(args, local) -> dict:
+    """Short runs of the batch (64 patterns against R-MAT 20) and the adjoint
+    (R-MAT 16, 12 / 24 pattern) legs, carried on the main line so that one
+    default run records every configuration; `bench.py --batch` / `--adjoint`
+    time them with the full step counts.  A leg that fails reports its error."""
+    import argparse as _ap
+
+    out = {}
+    for name, fn, steps in (("batch", batch_result, 2), ("adjoint", adjoint_result, 5)):
+        a = _ap.Namespace(**vars(args))
+        a.steps, a.warmup, a.fp64_sample = steps, 1, 8
+        t0 = time.time()
+        try:
+            out[name] = fn(a, 1, local)
+        except Exception as e:  # noqa: BLE001 -- the main line must still print
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+        out[name]["wall_s"] = round(time.time() - t0, 1)
+    return out
 
 
 # -------------------------------------------------------------- reference
@@ -547,6 +574,13 @@ def run_reference(args, ws, rank):
 def run_batch(args, ws, rank, local):
     """One data graph against many patterns: one acg_batch launch (all patterns,
     one CUDA graph) against the same patterns matched one after another."""
+    out = batch_result(args, ws, local)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def batch_result(args, ws, local) -> dict:
+    """The measurements of run_batch as one dict (the bench line's fields)."""
     import numpy as np
     import torch
 
@@ -621,8 +655,7 @@ def run_batch(args, ws, rank, local):
                     for k, i in enumerate(sub) for j in range(pats[i].num_nodes))
     total_pn = sum(pats[i].num_nodes for i in sub)
     value = n / (ms_batch * 1e-3)
-    if rank == 0:
-        print(json.dumps({
+    return {
             "metric": f"patterns matched per second (one data graph, {n} patterns, batched, "
                       f"{prec} precision)",
             "value": round(value, 2), "unit": "patterns/s", "n_gpus": ws, "steps": args.steps,
@@ -648,7 +681,7 @@ def run_batch(args, ws, rank, local):
             "max_abs_dmu_vs_fp64_sample": err64,
             "planted_recovered_fp64_sample": f"{recovered} of {total_pn}",
             "clocks": clk.summary(),
-        }), flush=True)
+    }
 
 
 def run_adjoint(args, ws, rank, local):
@@ -656,6 +689,13 @@ def run_adjoint(args, ws, rank, local):
     against the backward (acg_backward) of one match.  Loss: the sum of mu --
     the log of the normalised assignment probability -- over the planted
     (data vertex, pattern vertex) pairs, so grad_mu is one-hot there."""
+    out = adjoint_result(args, ws, local)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def adjoint_result(args, ws, local) -> dict:
+    """The measurements of run_adjoint as one dict (the bench line's fields)."""
     import numpy as np
     import torch
 
@@ -710,8 +750,7 @@ def run_adjoint(args, ws, rank, local):
     rel = {n: float(np.linalg.norm(a - b) / max(1e-300, np.linalg.norm(b)))
            for n, a, b in zip(names, grads[args.precision], grads["fp64"])}
     r = res[args.precision]
-    if rank == 0:
-        print(json.dumps({
+    return {
             "metric": "backward time / forward time of one match (gradients of the planted-pair "
                       "log-probabilities w.r.t. all four feature arrays)",
             "value": r["backward_over_forward"], "unit": "x", "n_gpus": ws, "steps": args.steps,
@@ -726,7 +765,7 @@ def run_adjoint(args, ws, rank, local):
             "timings": res,
             "grad_rel_frobenius_vs_fp64": rel,
             "clocks": clk_summary,
-        }), flush=True)
+    }
 
 
 def main():
